@@ -1,0 +1,193 @@
+"""ctypes mirror of ``include/fsph.h`` and the loader of ``libfsph.so``.
+
+The structs here must match the header field for field; ``tests/test_abi.py``
+checks their sizes against the library's own ``sizeof`` report.  Loading is
+strict: if the CUDA library has not been built, :func:`lib` raises -- there is
+no CPU fallback behind this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libfsph.so")
+
+# fsph_status
+OK, INVALID_ARG, OOM, CUDA_ERROR, NAN_DETECTED, TIMEOUT, NOT_CONVERGED, NOT_INITIALIZED, UNSUPPORTED, NO_DEVICE = range(10)
+# fsph_solver
+SOLVER_WCSPH, SOLVER_PBF = 0, 1
+# fsph_error_mode
+ERR_ONE_SIDED, ERR_TWO_SIDED = 0, 1
+# fsph_where
+HOST, DEVICE = 0, 1
+# fsph_array (numbering of rxParticleSystemBase::rxParticleArray, rx_ps.h:68-116)
+RX_POSITION = 0
+RX_VELOCITY = 1
+RX_FORCE = 3
+RX_DENSITY = 4
+RX_PRESSURE = 5
+RX_ATTRIBUTE = 7
+RX_PREDICT_POS = 8
+RX_PREDICT_VEL = 9
+RX_SCALING_FACTOR = 10
+RX_CORRECTION = 11
+RX_VORTICITY = 18
+FSPH_SORTED_ID = 64
+
+VECTOR_ARRAYS = {RX_POSITION, RX_VELOCITY, RX_FORCE, RX_PREDICT_POS, RX_PREDICT_VEL, RX_CORRECTION, RX_VORTICITY}
+
+STATUS_NAMES = {
+    OK: "FSPH_OK", INVALID_ARG: "FSPH_INVALID_ARG", OOM: "FSPH_OOM", CUDA_ERROR: "FSPH_CUDA_ERROR",
+    NAN_DETECTED: "FSPH_NAN_DETECTED", TIMEOUT: "FSPH_TIMEOUT", NOT_CONVERGED: "FSPH_NOT_CONVERGED",
+    NOT_INITIALIZED: "FSPH_NOT_INITIALIZED", UNSUPPORTED: "FSPH_UNSUPPORTED", NO_DEVICE: "FSPH_NO_DEVICE",
+}
+
+
+class FsphParams(ctypes.Structure):
+    _fields_ = [
+        ("solver", ctypes.c_int),
+        ("max_particles", ctypes.c_int),
+        ("h", ctypes.c_float),
+        ("mass", ctypes.c_float),
+        ("rest_dens", ctypes.c_float),
+        ("particle_radius", ctypes.c_float),
+        ("box_min", ctypes.c_double * 3),
+        ("box_max", ctypes.c_double * 3),
+        ("gravity", ctypes.c_float * 3),
+        ("viscosity", ctypes.c_float),
+        ("gas_k", ctypes.c_float),
+        ("epsilon", ctypes.c_float),
+        ("eta", ctypes.c_float),
+        ("min_iter", ctypes.c_int),
+        ("max_iter", ctypes.c_int),
+        ("error_mode", ctypes.c_int),
+        ("use_ap", ctypes.c_int),
+        ("ap_k", ctypes.c_float),
+        ("ap_n", ctypes.c_float),
+        ("ap_q", ctypes.c_float),
+        ("xsph_c", ctypes.c_float),
+        ("vort_eps", ctypes.c_float),
+        ("cell_skin", ctypes.c_float),
+        ("use_graph", ctypes.c_int),
+        ("warm_start", ctypes.c_int),
+        ("clamp_constraint", ctypes.c_int),
+        ("reserved", ctypes.c_int * 6),
+    ]
+
+    def to_dict(self) -> dict:
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if hasattr(v, "__len__") else v
+        return d
+
+
+class FsphEnv(ctypes.Structure):
+    _fields_ = [
+        ("solver", ctypes.c_int),
+        ("max_particles", ctypes.c_int),
+        ("boundary_cen", ctypes.c_double * 3),
+        ("boundary_ext", ctypes.c_double * 3),
+        ("dens", ctypes.c_float),
+        ("mass", ctypes.c_float),
+        ("kernel_particles", ctypes.c_float),
+        ("viscosity", ctypes.c_float),
+        ("gas_k", ctypes.c_float),
+        ("epsilon", ctypes.c_float),
+        ("eta", ctypes.c_float),
+        ("min_iter", ctypes.c_int),
+        ("max_iter", ctypes.c_int),
+        ("use_ap", ctypes.c_int),
+        ("ap_k", ctypes.c_float),
+        ("ap_n", ctypes.c_float),
+        ("ap_q", ctypes.c_float),
+        ("gravity_y", ctypes.c_float),
+    ]
+
+
+class FsphStepStats(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int),
+        ("grid_builds", ctypes.c_int),
+        ("density_error", ctypes.c_float),
+        ("density_error_one_sided", ctypes.c_float),
+        ("density_error_two_sided", ctypes.c_float),
+        ("density_error_max", ctypes.c_float),
+        ("status", ctypes.c_int),
+        ("reserved", ctypes.c_int * 3),
+    ]
+
+
+# Every symbol include/fsph.h declares (checked by tests/test_abi.py).
+EXPORTS = [
+    "fsph_abi_version", "fsph_status_string", "fsph_last_error", "fsph_params_from_env",
+    "fsph_params_default", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params",
+    "fsph_num_particles", "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats",
+    "fsph_get_array", "fsph_device_ptr", "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda",
+    "fsph_pbf_eval_correction", "fsph_sph_eval_forces", "fsph_time_pass",
+]
+
+# fsph_pass
+PASS_LAMBDA, PASS_CORRECTION, PASS_GRID = 0, 1, 2
+
+_LIB = None
+
+
+def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
+    c_int, c_float, c_void_p, c_char_p = ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_char_p
+    P = ctypes.POINTER
+    L.fsph_abi_version.restype = c_int
+    L.fsph_status_string.restype = c_char_p
+    L.fsph_status_string.argtypes = [c_int]
+    L.fsph_last_error.restype = c_char_p
+    L.fsph_last_error.argtypes = [c_void_p]
+    L.fsph_params_from_env.argtypes = [P(FsphEnv), P(FsphParams)]
+    L.fsph_params_default.argtypes = [P(FsphParams)]
+    L.fsph_params_default.restype = None
+    L.fsph_create.argtypes = [P(FsphParams), P(c_void_p)]
+    L.fsph_destroy.argtypes = [c_void_p]
+    L.fsph_set_params.argtypes = [c_void_p, P(FsphParams)]
+    L.fsph_get_params.argtypes = [c_void_p, P(FsphParams)]
+    L.fsph_num_particles.argtypes = [c_void_p]
+    L.fsph_set_particles.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int]
+    L.fsph_set_array.argtypes = [c_void_p, c_int, c_void_p, c_int, c_int, c_int]
+    L.fsph_step.argtypes = [c_void_p, c_float, c_void_p, P(FsphStepStats)]
+    L.fsph_last_stats.argtypes = [c_void_p, P(FsphStepStats)]
+    L.fsph_get_array.argtypes = [c_void_p, c_int, c_void_p, c_int, c_void_p]
+    L.fsph_device_ptr.argtypes = [c_void_p, c_int]
+    L.fsph_device_ptr.restype = c_void_p
+    L.fsph_sync.argtypes = [c_void_p]
+    L.fsph_neighbors.argtypes = [c_void_p, c_void_p, c_void_p, ctypes.c_longlong, P(ctypes.c_longlong)]
+    L.fsph_pbf_eval_lambda.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+    L.fsph_pbf_eval_correction.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p]
+    L.fsph_sph_eval_forces.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    L.fsph_time_pass.argtypes = [c_void_p, c_int, c_int, P(c_float)]
+    for name in ["fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",
+                 "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats", "fsph_get_array",
+                 "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda", "fsph_pbf_eval_correction",
+                 "fsph_sph_eval_forces", "fsph_params_from_env"]:
+        getattr(L, name).restype = c_int
+    return L
+
+
+def lib(path: str | None = None) -> ctypes.CDLL:
+    """Load libfsph.so (built by ``fltk_sph_ice_gb300.build``); raise if absent."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.isfile(p):
+        raise RuntimeError(
+            f"libfsph.so not found at {p}: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()'); there is no CPU fallback")
+    L = _declare(ctypes.CDLL(p, mode=ctypes.RTLD_GLOBAL))
+    if path is None:
+        _LIB = L
+    return L
+
+
+class FsphError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status

@@ -1,0 +1,1020 @@
+/*
+ * fsph_api.cu -- the C ABI of include/fsph.h: context, parameters, particle
+ * data, the step orchestration and the parity entry points.
+ *
+ * Step orchestration replaces rxPBDSPH_GPU::Update (rx_sph_pbd_gpu.cpp:790-957)
+ * and rxSPH_GPU::Update (rx_sph_gpu.cpp:756-923).  Differences by design:
+ *   - no host round trip inside the PBF loop: the lambda kernel reduces the
+ *     density error and decides on the device whether to continue; with
+ *     use_graph the whole step is one CUDA graph whose iteration loop is a
+ *     conditional WHILE node (the reference synchronised and copied the scan
+ *     result to the host every iteration, rx_sph.cu:668-691);
+ *   - the grid is built once per step on x* (cell width h (1 + skin)) and
+ *     rebuilt inside the loop only when a particle has moved more than
+ *     skin * h since the build (a conditional IF node), instead of at every
+ *     iteration (rx_sph_pbd_gpu.cpp:876); the neighbour criterion is always
+ *     evaluated on the current x*, so the neighbour sets are the same;
+ *   - particles stay in cell order across steps; getters map back to the
+ *     caller's particle order through the device slot -> particle index map;
+ *   - no GL buffers and no CPU neighbour mirror (rx_sph_pbd_gpu.cpp:962-1011).
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fsph.h"
+#include "fsph_kernels.cuh"
+
+using namespace fsph;
+
+namespace {
+const double kPi = 3.14159265358979323846;
+}
+
+struct BufSet {
+    float4 *pos = nullptr, *vel = nullptr;
+    unsigned int *id = nullptr, *attr = nullptr;
+};
+
+struct fsph_ctx {
+    fsph_params P{};
+    DevParams dp{};
+    int n = 0;
+    int cap = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr, s2 = nullptr, s3 = nullptr;
+    BufSet set[2];
+    float4 *ppos[2] = {nullptr, nullptr};
+    float4 *xb = nullptr, *acc = nullptr, *vort = nullptr;
+    float *dens = nullptr, *pres = nullptr;
+    unsigned int *key = nullptr, *rank = nullptr, *perm = nullptr;
+    unsigned int *count = nullptr, *cell_start = nullptr, *block_sums = nullptr;
+    unsigned int ncells = 0;
+    int gdim[3] = {0, 0, 0};
+    DevCtl *ctl = nullptr;
+    DevCtl *ctl_host = nullptr;
+    unsigned int *flag = nullptr;      /* input-validation flag */
+    unsigned int *flag_host = nullptr;
+    ErrPartial *epart = nullptr;
+    float *dpart = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    bool graph_valid = false;
+    float graph_dt = 0.0f;
+    int graph_n = -1;
+    bool stats_pending = false;
+    std::string err;
+};
+
+namespace {
+
+#define FSPH_CUDA(ctx, call)                                                                  \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            (ctx)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                  \
+            return e_ == cudaErrorMemoryAllocation ? FSPH_OOM : FSPH_CUDA_ERROR;              \
+        }                                                                                     \
+    } while (0)
+
+#define FSPH_TRY(expr)             \
+    do {                           \
+        int st_ = (expr);          \
+        if (st_ != FSPH_OK) return st_; \
+    } while (0)
+
+int fail(fsph_ctx *c, int st, const std::string &msg) {
+    if (c) c->err = msg;
+    return st;
+}
+
+/* ---------------- parameters ---------------- */
+
+double poly6_coef(double h) { return 315.0 / (64.0 * kPi * std::pow(h, 9.0)); }
+
+int validate(const fsph_params &p, std::string &why) {
+    if (p.solver != FSPH_SOLVER_WCSPH && p.solver != FSPH_SOLVER_PBF) { why = "unknown solver"; return FSPH_INVALID_ARG; }
+    if (p.max_particles < 0) { why = "max_particles < 0"; return FSPH_INVALID_ARG; }
+    if (!(p.h > 0.0f) || !std::isfinite(p.h)) { why = "h must be positive and finite"; return FSPH_INVALID_ARG; }
+    if (!(p.mass > 0.0f)) { why = "mass must be positive"; return FSPH_INVALID_ARG; }
+    if (!(p.rest_dens > 0.0f)) { why = "rest_dens must be positive"; return FSPH_INVALID_ARG; }
+    if (p.particle_radius < 0.0f) { why = "particle_radius < 0"; return FSPH_INVALID_ARG; }
+    for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(p.box_min[a]) || !std::isfinite(p.box_max[a])) { why = "box not finite"; return FSPH_INVALID_ARG; }
+        if (!(p.box_max[a] - p.box_min[a] > 2.0 * p.particle_radius)) { why = "box thinner than a particle"; return FSPH_INVALID_ARG; }
+    }
+    if (p.solver == FSPH_SOLVER_PBF) {
+        if (p.max_iter < 1) { why = "max_iter must be >= 1"; return FSPH_INVALID_ARG; }
+        if (p.min_iter < 0) { why = "min_iter < 0"; return FSPH_INVALID_ARG; }
+        if (!(p.epsilon >= 0.0f)) { why = "epsilon < 0"; return FSPH_INVALID_ARG; }
+        if (p.error_mode != FSPH_ERR_ONE_SIDED && p.error_mode != FSPH_ERR_TWO_SIDED) { why = "error_mode"; return FSPH_INVALID_ARG; }
+        if (p.use_ap && !(p.ap_q > 0.0f && p.ap_q < 1.0f)) { why = "ap_q must lie in (0, 1)"; return FSPH_INVALID_ARG; }
+    }
+    if (p.cell_skin < 0.0f || p.cell_skin > 1.0f) { why = "cell_skin must lie in [0, 1]"; return FSPH_INVALID_ARG; }
+    if (p.warm_start != 0) { why = "warm_start requires the learned-warm-start build"; return FSPH_UNSUPPORTED; }
+    return FSPH_OK;
+}
+
+/* Grid geometry: cell width h (1 + skin), the box padded by one cell. */
+void grid_geometry(const fsph_params &p, double &cw, double org[3], int g[3]) {
+    double skin = std::max((double)p.cell_skin, 1e-3);
+    cw = (double)p.h * (1.0 + skin);
+    for (int a = 0; a < 3; ++a) {
+        org[a] = p.box_min[a] - cw;
+        g[a] = (int)std::ceil((p.box_max[a] - p.box_min[a]) / cw) + 2;
+        if (g[a] < 3) g[a] = 3;
+    }
+}
+
+DevParams make_dev(const fsph_params &p, int n, float dt) {
+    DevParams d{};
+    d.n = n;
+    d.h = p.h;
+    d.h2 = p.h * p.h;
+    d.mass = p.mass;
+    d.rest_dens = p.rest_dens;
+    d.inv_rest_dens = 1.0f / p.rest_dens;
+    double h = (double)p.h;
+    d.aw = (float)poly6_coef(h);
+    d.ag = (float)(-45.0 / (kPi * std::pow(h, 6.0)));
+    d.al = (float)(45.0 / (kPi * std::pow(h, 6.0)));
+    double r = (double)p.particle_radius;
+    d.wall_lo = make_float3((float)(p.box_min[0] + r), (float)(p.box_min[1] + r), (float)(p.box_min[2] + r));
+    d.wall_hi = make_float3((float)(p.box_max[0] - r), (float)(p.box_max[1] - r), (float)(p.box_max[2] - r));
+    d.gravity = make_float3(p.gravity[0], p.gravity[1], p.gravity[2]);
+    d.viscosity = p.viscosity;
+    d.gas_k = p.gas_k;
+    d.epsilon = p.epsilon;
+    d.eta = p.eta;
+    d.min_iter = p.min_iter;
+    d.max_iter = p.max_iter;
+    d.error_mode = p.error_mode;
+    d.clamp_constraint = p.clamp_constraint;
+    d.use_ap = p.use_ap;
+    d.ap_k = p.ap_k;
+    d.ap_n = p.ap_n;
+    if (p.use_ap) {
+        float dq = p.ap_q * p.h;
+        double q = h * h - (double)dq * (double)dq;
+        double wq = poly6_coef(h) * q * q * q;
+        d.inv_wq = (float)(1.0 / wq);
+    }
+    d.xsph_c = p.xsph_c;
+    d.vort_eps = p.vort_eps;
+    double cw, org[3];
+    int g[3];
+    grid_geometry(p, cw, org, g);
+    d.grid_origin = make_float3((float)org[0], (float)org[1], (float)org[2]);
+    d.inv_cw = (float)(1.0 / cw);
+    d.gx = g[0]; d.gy = g[1]; d.gz = g[2];
+    double skin_len = (cw - h) * 0.999;
+    d.skin2 = (float)(skin_len * skin_len);
+    d.dt = dt;
+    d.inv_dt = dt != 0.0f ? 1.0f / dt : 0.0f;
+    return d;
+}
+
+template <class T>
+int dalloc(fsph_ctx *c, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    FSPH_CUDA(c, cudaMalloc((void **)p, count * sizeof(T)));
+    return FSPH_OK;
+}
+
+void free_particles(fsph_ctx *c) {
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(c->set[k].pos); cudaFree(c->set[k].vel); cudaFree(c->set[k].id); cudaFree(c->set[k].attr);
+        c->set[k] = BufSet{};
+        cudaFree(c->ppos[k]); c->ppos[k] = nullptr;
+    }
+    cudaFree(c->xb); cudaFree(c->acc); cudaFree(c->vort); cudaFree(c->dens); cudaFree(c->pres);
+    cudaFree(c->key); cudaFree(c->rank); cudaFree(c->perm); cudaFree(c->epart); cudaFree(c->dpart);
+    c->xb = c->acc = c->vort = nullptr;
+    c->dens = c->pres = nullptr;
+    c->key = c->rank = c->perm = nullptr;
+    c->epart = nullptr;
+    c->dpart = nullptr;
+}
+
+void free_grid(fsph_ctx *c) {
+    cudaFree(c->count); cudaFree(c->cell_start); cudaFree(c->block_sums);
+    c->count = c->cell_start = c->block_sums = nullptr;
+    c->ncells = 0;
+}
+
+void drop_graph(fsph_ctx *c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
+    c->graph_valid = false;
+}
+
+int alloc_particles(fsph_ctx *c, int cap) {
+    free_particles(c);
+    size_t n = (size_t)std::max(cap, 1);
+    for (int k = 0; k < 2; ++k) {
+        FSPH_TRY(dalloc(c, &c->set[k].pos, n)); FSPH_TRY(dalloc(c, &c->set[k].vel, n));
+        FSPH_TRY(dalloc(c, &c->set[k].id, n)); FSPH_TRY(dalloc(c, &c->set[k].attr, n));
+        FSPH_TRY(dalloc(c, &c->ppos[k], n));
+    }
+    FSPH_TRY(dalloc(c, &c->xb, n)); FSPH_TRY(dalloc(c, &c->acc, n)); FSPH_TRY(dalloc(c, &c->vort, n));
+    FSPH_TRY(dalloc(c, &c->dens, n)); FSPH_TRY(dalloc(c, &c->pres, n));
+    FSPH_TRY(dalloc(c, &c->key, n)); FSPH_TRY(dalloc(c, &c->rank, n)); FSPH_TRY(dalloc(c, &c->perm, n));
+    FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n)));
+    FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n)));
+    for (int k = 0; k < 2; ++k) {
+        FSPH_CUDA(c, cudaMemsetAsync(c->set[k].pos, 0, n * sizeof(float4), c->stream));
+        FSPH_CUDA(c, cudaMemsetAsync(c->set[k].vel, 0, n * sizeof(float4), c->stream));
+        FSPH_CUDA(c, cudaMemsetAsync(c->set[k].attr, 0, n * sizeof(unsigned int), c->stream));
+        FSPH_CUDA(c, cudaMemsetAsync(c->ppos[k], 0, n * sizeof(float4), c->stream));
+    }
+    FSPH_CUDA(c, cudaMemsetAsync(c->acc, 0, n * sizeof(float4), c->stream));
+    FSPH_CUDA(c, cudaMemsetAsync(c->vort, 0, n * sizeof(float4), c->stream));
+    FSPH_CUDA(c, cudaMemsetAsync(c->dens, 0, n * sizeof(float), c->stream));
+    FSPH_CUDA(c, cudaMemsetAsync(c->pres, 0, n * sizeof(float), c->stream));
+    c->cap = cap;
+    return FSPH_OK;
+}
+
+int alloc_grid(fsph_ctx *c) {
+    double cw, org[3];
+    int g[3];
+    grid_geometry(c->P, cw, org, g);
+    double cells = (double)g[0] * g[1] * g[2];
+    if (cells > (double)(1u << 28))
+        return fail(c, FSPH_INVALID_ARG, "box / h gives more than 2^28 grid cells");
+    unsigned int nc = (unsigned int)cells;
+    if (nc == c->ncells && c->count) {
+        std::memcpy(c->gdim, g, sizeof(g));
+        return FSPH_OK;
+    }
+    free_grid(c);
+    FSPH_TRY(dalloc(c, &c->count, nc));
+    FSPH_TRY(dalloc(c, &c->cell_start, (size_t)nc + 1));
+    FSPH_TRY(dalloc(c, &c->block_sums, scan_blocks(nc)));
+    FSPH_CUDA(c, cudaMemsetAsync(c->count, 0, (size_t)nc * sizeof(unsigned int), c->stream));
+    c->ncells = nc;
+    std::memcpy(c->gdim, g, sizeof(g));
+    return FSPH_OK;
+}
+
+/* ---------------- building blocks of a step ---------------- */
+
+/* counting sort of the slots of x (device order) by cell: leaves perm */
+void enqueue_sort(fsph_ctx *c, const DevParams &p, const float4 *x, cudaStream_t s) {
+    launch_hash(p, x, c->key, c->rank, c->count, s);
+    launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
+    launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+}
+
+/* the grid rebuild used inside the loop and after it (positions = current x*) */
+void enqueue_rebuild(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
+    BufSet &I = c->set[it], &O = c->set[1 - it];
+    launch_hash_parity(p, c->ppos[0], c->ppos[1], c->ctl, c->key, c->rank, c->count, s);
+    launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
+    launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+    launch_rebuild_gather(p.n, c->perm, c->ctl, I.pos, c->ppos[0], c->ppos[1], I.id, I.attr, c->dens, O.pos, O.vel,
+                          O.id, O.attr, c->pres, s);
+    launch_rebuild_copy(p.n, c->ctl, O.pos, O.vel, O.id, O.attr, c->pres, I.pos, c->ppos[0], c->ppos[1], c->xb, I.id,
+                        I.attr, c->dens, s);
+}
+
+bool pbf_prepass(const fsph_ctx *c) { return c->P.viscosity != 0.0f; }
+bool pbf_finalize_ext(const fsph_ctx *c) { return c->P.xsph_c != 0.0f || c->P.vort_eps != 0.0f; }
+
+/* PBF: pre-pass, prediction, first grid build; returns the set that carries
+ * the particles through the iterations. */
+int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
+    cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s);
+    int src = 0, it = 1;
+    const float4 *acc = nullptr;
+    if (pbf_prepass(c)) {
+        enqueue_sort(c, p, c->set[0].pos, s);
+        Gather g{};
+        g.n4 = 2; g.n1 = 2;
+        g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+        g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+        g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
+        g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
+        launch_gather(p.n, c->perm, g, nullptr, s);
+        launch_pbf_density(p, c->cell_start, c->set[1].pos, c->dens, s);
+        launch_pbf_visc(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->acc, s);
+        acc = c->acc;
+        src = 1; it = 0;
+    }
+    launch_predict_hash(p, c->set[src].pos, c->set[src].vel, acc, c->ppos[1], c->key, c->rank, c->count, s);
+    launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
+    launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+    Gather g{};
+    g.n4 = 3; g.n1 = 2;
+    g.src4[0] = c->set[src].pos; g.dst4[0] = c->set[it].pos;
+    g.src4[1] = c->ppos[1]; g.dst4[1] = c->ppos[0];
+    g.src4[2] = c->ppos[1]; g.dst4[2] = c->xb;
+    g.src1[0] = c->set[src].id; g.dst1[0] = c->set[it].id;
+    g.src1[1] = c->set[src].attr; g.dst1[1] = c->set[it].attr;
+    launch_gather(p.n, c->perm, g, c->ctl, s);
+    return it;
+}
+
+void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
+    launch_finalize(p, c->set[it].pos, c->ppos[0], c->ppos[1], c->ctl, c->set[it].id, c->set[it].attr,
+                    c->set[0].pos, c->set[0].vel, c->set[0].id, c->set[0].attr, s);
+    if (pbf_finalize_ext(c)) {
+        launch_xsph_vort(p, c->cell_start, c->set[0].pos, c->set[0].vel, c->dens, c->set[1].vel, c->vort, s);
+        launch_vort_apply(p, c->cell_start, c->set[0].pos, c->vort, c->dens, c->set[1].vel, c->set[0].vel, s);
+    }
+}
+
+int pbf_step_eager(fsph_ctx *c, const DevParams &p) {
+    cudaStream_t s = c->stream;
+    int it = enqueue_pbf_pre(c, p, s);
+    for (int k = 0;; ++k) {
+        launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+        launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0,
+                          nullptr, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        if (c->ctl_host->done || k > p.max_iter + 1) break;
+        if (c->ctl_host->rebuild) enqueue_rebuild(c, p, it, s);
+    }
+    if (pbf_finalize_ext(c) && c->ctl_host->rebuild) enqueue_rebuild(c, p, it, s);
+    enqueue_pbf_post(c, p, it, s);
+    return FSPH_OK;
+}
+
+int add_conditional(fsph_ctx *c, cudaGraph_t g, const cudaGraphNode_t *deps, size_t ndeps,
+                    cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraphNode_t *node,
+                    cudaGraph_t *body) {
+    /* the params union has no usable default constructor: zero raw storage */
+    alignas(cudaGraphNodeParams) unsigned char raw[sizeof(cudaGraphNodeParams)];
+    std::memset(raw, 0, sizeof(raw));
+    cudaGraphNodeParams *cp = reinterpret_cast<cudaGraphNodeParams *>(raw);
+    cp->type = cudaGraphNodeTypeConditional;
+    cp->conditional.handle = h;
+    cp->conditional.type = type;
+    cp->conditional.size = 1;
+    FSPH_CUDA(c, cudaGraphAddNode(node, g, deps, nullptr, ndeps, cp));
+    *body = cp->conditional.phGraph_out[0];
+    return FSPH_OK;
+}
+
+/* Capture one PBF step into a graph:
+ *   pre-pass -> WHILE(h_while){ IF(h_rb){rebuild}; lambda; correction }
+ *            -> [IF(h_rb2){rebuild}] -> finalize (+ XSPH / vorticity)      */
+int build_pbf_graph(fsph_ctx *c, const DevParams &p) {
+    drop_graph(c);
+    cudaStream_t s = c->stream;
+    cudaGraph_t g;
+    FSPH_CUDA(c, cudaGraphCreate(&g, 0));
+    c->graph = g;
+    FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    int it = enqueue_pbf_pre(c, p, s);
+
+    cudaStreamCaptureStatus st;
+    cudaGraph_t capg;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    FSPH_CUDA(c, cudaStreamGetCaptureInfo(s, &st, nullptr, &capg, &deps, nullptr, &ndeps));
+    cudaGraphConditionalHandle hw, hrb, hrb2;
+    FSPH_CUDA(c, cudaGraphConditionalHandleCreate(&hw, capg, 1, cudaGraphCondAssignDefault));
+    cudaGraphNode_t wnode;
+    cudaGraph_t wbody;
+    std::vector<cudaGraphNode_t> dv(deps, deps + ndeps);
+    FSPH_TRY(add_conditional(c, capg, dv.data(), dv.size(), hw, cudaGraphCondTypeWhile, &wnode, &wbody));
+
+    FSPH_CUDA(c, cudaGraphConditionalHandleCreate(&hrb, wbody, 0, cudaGraphCondAssignDefault));
+    cudaGraphNode_t inode;
+    cudaGraph_t ibody;
+    FSPH_TRY(add_conditional(c, wbody, nullptr, 0, hrb, cudaGraphCondTypeIf, &inode, &ibody));
+    FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(c->s3, ibody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    enqueue_rebuild(c, p, it, c->s3);
+    FSPH_CUDA(c, cudaStreamEndCapture(c->s3, &ibody));
+
+    const bool ext = pbf_finalize_ext(c);
+    hrb2 = 0;
+    if (ext) FSPH_CUDA(c, cudaGraphConditionalHandleCreate(&hrb2, capg, 0, cudaGraphCondAssignDefault));
+    FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(c->s2, wbody, &inode, nullptr, 1, cudaStreamCaptureModeRelaxed));
+    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, hw, 1, c->s2);
+    launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, hrb, hrb2, ext ? 3 : 1,
+                      nullptr, c->s2);
+    FSPH_CUDA(c, cudaStreamEndCapture(c->s2, &wbody));
+    FSPH_CUDA(c, cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+
+    if (ext) {
+        cudaGraphNode_t pnode;
+        cudaGraph_t pbody;
+        FSPH_TRY(add_conditional(c, capg, &wnode, 1, hrb2, cudaGraphCondTypeIf, &pnode, &pbody));
+        FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(c->s3, pbody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        enqueue_rebuild(c, p, it, c->s3);
+        FSPH_CUDA(c, cudaStreamEndCapture(c->s3, &pbody));
+        FSPH_CUDA(c, cudaStreamUpdateCaptureDependencies(s, &pnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    }
+    enqueue_pbf_post(c, p, it, s);
+    FSPH_CUDA(c, cudaStreamEndCapture(s, &g));
+    FSPH_CUDA(c, cudaGraphInstantiate(&c->gexec, g, 0));
+    c->graph_valid = true;
+    c->graph_dt = p.dt;
+    c->graph_n = p.n;
+    return FSPH_OK;
+}
+
+int sph_step(fsph_ctx *c, const DevParams &p) {
+    cudaStream_t s = c->stream;
+    FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
+    enqueue_sort(c, p, c->set[0].pos, s);
+    Gather g{};
+    g.n4 = 2; g.n1 = 2;
+    g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+    g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+    g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
+    g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
+    launch_gather(p.n, c->perm, g, c->ctl, s);
+    launch_sph_density(p, c->cell_start, c->set[1].pos, c->dens, c->pres, s);
+    launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->acc, s);
+    launch_sph_integrate(p, c->set[1].pos, c->set[1].vel, c->acc, c->set[1].id, c->set[1].attr, c->set[0].pos,
+                         c->set[0].vel, c->set[0].id, c->set[0].attr, s);
+    return FSPH_OK;
+}
+
+int check_launch(fsph_ctx *c) {
+    FSPH_CUDA(c, cudaGetLastError());
+    return FSPH_OK;
+}
+
+void fill_stats(fsph_ctx *c, fsph_step_stats *st) {
+    std::memset(st, 0, sizeof(*st));
+    const DevCtl &h = *c->ctl_host;
+    st->iterations = (int)h.iter;
+    st->grid_builds = (int)h.builds;
+    st->density_error_one_sided = h.err1;
+    st->density_error_two_sided = h.err2;
+    st->density_error_max = h.errmax;
+    st->density_error = c->P.error_mode ? h.err2 : h.err1;
+    st->status = FSPH_OK;
+    if (c->P.solver == FSPH_SOLVER_PBF) {
+        if (h.nan_flag) st->status = FSPH_NAN_DETECTED;
+        else if (st->density_error > c->P.eta) st->status = FSPH_NOT_CONVERGED;
+    }
+}
+
+/* Load n host/device float4 positions (and optional velocities) in particle order. */
+int load_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int where) {
+    cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    size_t b = (size_t)n * sizeof(float4);
+    if (n > 0) {
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, pos4, b, k, c->stream));
+        if (vel4) FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, vel4, b, k, c->stream));
+        else FSPH_CUDA(c, cudaMemsetAsync(c->set[0].vel, 0, b, c->stream));
+        FSPH_CUDA(c, cudaMemsetAsync(c->set[0].attr, 0, (size_t)n * 4, c->stream));
+        launch_iota(n, c->set[0].id, c->stream);
+    }
+    if (n != c->n) c->graph_valid = false;
+    c->n = n;
+    return check_launch(c);
+}
+
+/* Build the grid on device positions x (length n, current slot order) and
+ * gather x (and w) into set[1].pos / ppos[0] / xb, ids into set[1].id. */
+int build_on(fsph_ctx *c, const DevParams &p, const float4 *x) {
+    cudaStream_t s = c->stream;
+    enqueue_sort(c, p, x, s);
+    Gather g{};
+    g.n4 = 3; g.n1 = 2;
+    g.src4[0] = x; g.dst4[0] = c->set[1].pos;
+    g.src4[1] = x; g.dst4[1] = c->ppos[0];
+    g.src4[2] = x; g.dst4[2] = c->xb;
+    g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
+    g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
+    launch_gather(p.n, c->perm, g, nullptr, s);
+    return check_launch(c);
+}
+
+int copy_out_scalar(fsph_ctx *c, const float *dev_sorted_src, const unsigned int *id, float *host_dst, int n) {
+    float *tmp = reinterpret_cast<float *>(c->key);  /* key is free after a build */
+    launch_unsort1(n, id, reinterpret_cast<const unsigned int *>(dev_sorted_src), reinterpret_cast<unsigned int *>(tmp),
+                   c->stream);
+    FSPH_CUDA(c, cudaMemcpyAsync(host_dst, tmp, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+    return FSPH_OK;
+}
+
+}  // namespace
+
+/* ======================================================================== */
+/* C ABI                                                                    */
+/* ======================================================================== */
+extern "C" {
+
+int fsph_abi_version(void) { return FSPH_ABI_VERSION; }
+
+const char *fsph_status_string(int status) {
+    switch (status) {
+    case FSPH_OK: return "FSPH_OK";
+    case FSPH_INVALID_ARG: return "FSPH_INVALID_ARG";
+    case FSPH_OOM: return "FSPH_OOM";
+    case FSPH_CUDA_ERROR: return "FSPH_CUDA_ERROR";
+    case FSPH_NAN_DETECTED: return "FSPH_NAN_DETECTED";
+    case FSPH_TIMEOUT: return "FSPH_TIMEOUT";
+    case FSPH_NOT_CONVERGED: return "FSPH_NOT_CONVERGED";
+    case FSPH_NOT_INITIALIZED: return "FSPH_NOT_INITIALIZED";
+    case FSPH_UNSUPPORTED: return "FSPH_UNSUPPORTED";
+    case FSPH_NO_DEVICE: return "FSPH_NO_DEVICE";
+    }
+    return "FSPH_UNKNOWN";
+}
+
+const char *fsph_last_error(const fsph_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+void fsph_params_default(fsph_params *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->solver = FSPH_SOLVER_PBF;
+    o->max_particles = 0;
+    o->h = 0.0457f;
+    o->mass = 0.02f;
+    o->rest_dens = 998.29f;
+    o->particle_radius = 0.01f;
+    for (int a = 0; a < 3; ++a) { o->box_min[a] = -0.5; o->box_max[a] = 0.5; }
+    o->gravity[1] = -9.82f; /* rxParticleSystemBase constructor, rx_ps.h:165 */
+    o->viscosity = 0.0f;
+    o->gas_k = 3.0f;
+    o->epsilon = 0.001f;  /* rxSPHEnviroment defaults, rx_sph.h:152-160 */
+    o->eta = 0.05f;
+    o->min_iter = 2;
+    o->max_iter = 10;
+    o->error_mode = FSPH_ERR_ONE_SIDED;
+    o->use_ap = 1;
+    o->ap_k = 0.1f;
+    o->ap_n = 4.0f;
+    o->ap_q = 0.2f;
+    o->cell_skin = 0.02f;
+    o->use_graph = 1;
+}
+
+int fsph_params_from_env(const fsph_env *e, fsph_params *o) {
+    if (!e || !o) return FSPH_INVALID_ARG;
+    if (!(e->dens > 0) || !(e->mass > 0) || !(e->kernel_particles > 0) || e->max_particles <= 0) return FSPH_INVALID_ARG;
+    fsph_params_default(o);
+    o->solver = e->solver;
+    o->max_particles = e->max_particles;
+    /* h = (3 kp m / (4 pi rho))^(1/3), r = (pi / (6 kp))^(1/3) h
+     * (rx_sph_pbd.cpp:110-115, rx_sph_cpu.cpp:100-104), in RXREAL storage */
+    float volume = (float)e->max_particles * e->mass / e->dens;
+    float h = (float)std::pow((3.0 * e->kernel_particles * volume) / (4.0 * e->max_particles * kPi), 1.0 / 3.0);
+    float r = (float)(std::pow(kPi / (6.0 * e->kernel_particles), 1.0 / 3.0) * h);
+    o->h = h;
+    o->particle_radius = r;
+    o->mass = e->mass;
+    /* rho0 := calRestDensity(h): poly6 sum over a lattice of spacing 2r
+     * (rx_sph_pbd.cpp:1035-1049), float accumulation */
+    float l = 2.0f * r;
+    int nn = (int)std::ceil(h / l) + 1;
+    double aw = poly6_coef((double)h);
+    float r0 = 0.0f;
+    for (int x = -nn; x <= nn; ++x)
+        for (int y = -nn; y <= nn; ++y)
+            for (int z = -nn; z <= nn; ++z) {
+                double dx = (double)(x * l), dy = (double)(y * l), dz = (double)(z * l);
+                double rr = std::sqrt(dx * dx + dy * dy + dz * dz);
+                double w = (rr <= (double)h) ? aw * std::pow((double)h * h - rr * rr, 3.0) : 0.0;
+                r0 = (float)((double)r0 + (double)e->mass * w);
+            }
+    o->rest_dens = r0;
+    for (int a = 0; a < 3; ++a) {
+        o->box_min[a] = e->boundary_cen[a] - e->boundary_ext[a];
+        o->box_max[a] = e->boundary_cen[a] + e->boundary_ext[a];
+    }
+    o->gravity[0] = 0.0f; o->gravity[1] = e->gravity_y; o->gravity[2] = 0.0f;
+    o->viscosity = e->viscosity;
+    o->gas_k = e->gas_k;
+    o->epsilon = e->epsilon;
+    o->eta = e->eta;
+    o->min_iter = e->min_iter;
+    o->max_iter = e->max_iter;
+    o->error_mode = FSPH_ERR_TWO_SIDED; /* the CPU path's error (rx_sph_pbd.cpp:450) */
+    o->use_ap = e->use_ap;
+    o->ap_k = e->ap_k; o->ap_n = e->ap_n; o->ap_q = e->ap_q;
+    return FSPH_OK;
+}
+
+int fsph_create(const fsph_params *params, fsph_ctx **out) {
+    if (!params || !out) return FSPH_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return FSPH_NO_DEVICE;
+    }
+    std::string why;
+    int st = validate(*params, why);
+    if (st != FSPH_OK) return st;
+    fsph_ctx *c = new (std::nothrow) fsph_ctx();
+    if (!c) return FSPH_OOM;
+    c->P = *params;
+    cudaGetDevice(&c->device);
+    auto bail = [&](int s) { fsph_destroy(c); return s; };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(FSPH_CUDA_ERROR);
+    if (cudaStreamCreateWithFlags(&c->s2, cudaStreamNonBlocking) != cudaSuccess) return bail(FSPH_CUDA_ERROR);
+    if (cudaStreamCreateWithFlags(&c->s3, cudaStreamNonBlocking) != cudaSuccess) return bail(FSPH_CUDA_ERROR);
+    if (cudaMalloc((void **)&c->ctl, sizeof(DevCtl)) != cudaSuccess) return bail(FSPH_OOM);
+    if (cudaMallocHost((void **)&c->ctl_host, sizeof(DevCtl)) != cudaSuccess) return bail(FSPH_OOM);
+    std::memset(c->ctl_host, 0, sizeof(DevCtl));
+    if (cudaMalloc((void **)&c->flag, sizeof(unsigned int)) != cudaSuccess) return bail(FSPH_OOM);
+    if (cudaMallocHost((void **)&c->flag_host, sizeof(unsigned int)) != cudaSuccess) return bail(FSPH_OOM);
+    cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), c->stream);
+    if ((st = alloc_particles(c, params->max_particles)) != FSPH_OK) return bail(st);
+    if ((st = alloc_grid(c)) != FSPH_OK) return bail(st);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(FSPH_CUDA_ERROR);
+    *out = c;
+    return FSPH_OK;
+}
+
+int fsph_destroy(fsph_ctx *c) {
+    if (!c) return FSPH_INVALID_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graph(c);
+    free_particles(c);
+    free_grid(c);
+    cudaFree(c->ctl);
+    if (c->ctl_host) cudaFreeHost(c->ctl_host);
+    cudaFree(c->flag);
+    if (c->flag_host) cudaFreeHost(c->flag_host);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->s2) cudaStreamDestroy(c->s2);
+    if (c->s3) cudaStreamDestroy(c->s3);
+    delete c;
+    return FSPH_OK;
+}
+
+int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
+    if (!c || !p) return FSPH_INVALID_ARG;
+    std::string why;
+    int st = validate(*p, why);
+    if (st != FSPH_OK) return fail(c, st, why);
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    int old_cap = c->P.max_particles;
+    c->P = *p;
+    drop_graph(c);
+    if (p->max_particles != old_cap) {
+        if (c->n > p->max_particles) return fail(c, FSPH_INVALID_ARG, "max_particles below the current particle count");
+        /* keep the particles across the reallocation */
+        std::vector<float4> hp((size_t)c->n), hv((size_t)c->n);
+        if (c->n) {
+            FSPH_TRY(fsph_get_array(c, FSPH_POSITION, hp.data(), FSPH_HOST, nullptr));
+            FSPH_TRY(fsph_get_array(c, FSPH_VELOCITY, hv.data(), FSPH_HOST, nullptr));
+        }
+        int n = c->n;
+        FSPH_TRY(alloc_particles(c, p->max_particles));
+        c->n = 0;
+        FSPH_TRY(load_particles(c, (const float *)hp.data(), (const float *)hv.data(), n, FSPH_HOST));
+    }
+    FSPH_TRY(alloc_grid(c));
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FSPH_OK;
+}
+
+int fsph_get_params(const fsph_ctx *c, fsph_params *o) {
+    if (!c || !o) return FSPH_INVALID_ARG;
+    *o = c->P;
+    return FSPH_OK;
+}
+
+int fsph_num_particles(const fsph_ctx *c) { return c ? c->n : -1; }
+
+int fsph_set_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int where) {
+    if (!c) return FSPH_INVALID_ARG;
+    if (n < 0 || n > c->cap) return fail(c, FSPH_INVALID_ARG, "particle count outside [0, max_particles]");
+    if (n > 0 && !pos4) return fail(c, FSPH_INVALID_ARG, "null positions");
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    FSPH_TRY(load_particles(c, pos4, vel4, n, where));
+    /* finiteness is checked on the device, where the data now is */
+    FSPH_CUDA(c, cudaMemsetAsync(c->flag, 0, sizeof(unsigned int), c->stream));
+    if (n > 0) launch_check_finite(n, c->set[0].pos, c->set[0].vel, c->flag, c->stream);
+    FSPH_CUDA(c, cudaMemcpyAsync(c->flag_host, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    FSPH_TRY(check_launch(c));
+    if (*c->flag_host) {
+        c->n = 0;
+        return fail(c, FSPH_NAN_DETECTED, "non-finite input position or velocity");
+    }
+    return FSPH_OK;
+}
+
+int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count, int where) {
+    if (!c || !data) return FSPH_INVALID_ARG;
+    if (start < 0 || count < 0 || start + count > c->n) return fail(c, FSPH_INVALID_ARG, "range outside [0, n)");
+    if (type != FSPH_POSITION && type != FSPH_VELOCITY && type != FSPH_ATTRIBUTE)
+        return fail(c, FSPH_INVALID_ARG, "settable arrays: POSITION, VELOCITY, ATTRIBUTE");
+    cudaStream_t s = c->stream;
+    int n = c->n;
+    /* bring the home arrays to particle order, then overwrite the range */
+    launch_unsort4(n, c->set[0].id, c->set[0].pos, c->set[1].pos, 0, s);
+    launch_unsort4(n, c->set[0].id, c->set[0].vel, c->set[1].vel, 0, s);
+    launch_unsort1(n, c->set[0].id, c->set[0].attr, c->set[1].attr, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    launch_iota(n, c->set[0].id, s);
+    cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (type == FSPH_POSITION)
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos + start, data, (size_t)count * 16, k, s));
+    else if (type == FSPH_VELOCITY)
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel + start, data, (size_t)count * 16, k, s));
+    else
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr + start, data, (size_t)count * 4, k, s));
+    FSPH_TRY(check_launch(c));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    return FSPH_OK;
+}
+
+int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
+    if (!c) return FSPH_INVALID_ARG;
+    if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
+    cudaStream_t user = (cudaStream_t)stream;
+    cudaEvent_t ev = nullptr;
+    if (user && user != c->stream) {
+        /* order the step after the caller's work on its stream */
+        FSPH_CUDA(c, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        FSPH_CUDA(c, cudaEventRecord(ev, user));
+        FSPH_CUDA(c, cudaStreamWaitEvent(c->stream, ev, 0));
+    }
+    DevParams p = make_dev(c->P, c->n, dt);
+    c->dp = p;
+    if (c->P.solver == FSPH_SOLVER_WCSPH) {
+        FSPH_TRY(sph_step(c, p));
+    } else if (c->P.use_graph) {
+        if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n) FSPH_TRY(build_pbf_graph(c, p));
+        FSPH_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    } else {
+        FSPH_TRY(pbf_step_eager(c, p));
+    }
+    FSPH_TRY(check_launch(c));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, c->stream));
+    if (ev) {
+        FSPH_CUDA(c, cudaEventRecord(ev, c->stream));
+        FSPH_CUDA(c, cudaStreamWaitEvent(user, ev, 0));
+        cudaEventDestroy(ev);
+    }
+    if (stats) {
+        FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+        fill_stats(c, stats);
+        if (stats->status == FSPH_NAN_DETECTED) return fail(c, FSPH_NAN_DETECTED, "NaN in density or position");
+    }
+    return FSPH_OK;
+}
+
+int fsph_last_stats(fsph_ctx *c, fsph_step_stats *stats) {
+    if (!c || !stats) return FSPH_INVALID_ARG;
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    fill_stats(c, stats);
+    return FSPH_OK;
+}
+
+int fsph_sync(fsph_ctx *c) {
+    if (!c) return FSPH_INVALID_ARG;
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    return FSPH_OK;
+}
+
+int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
+    if (!c || !dst) return FSPH_INVALID_ARG;
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    int n = c->n;
+    if (n == 0) return FSPH_OK;
+    cudaStream_t s = c->stream;
+    (void)stream;
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    const unsigned int *id = c->set[0].id;
+    /* staging in device memory: the rank / key arrays are free between steps */
+    float4 *t4 = c->set[1].pos;
+    bool vec = true;
+    switch (type) {
+    case FSPH_POSITION: launch_unsort4(n, id, c->set[0].pos, t4, 1, s); break;
+    case FSPH_VELOCITY: launch_unsort4(n, id, c->set[0].vel, t4, 1, s); break;
+    case FSPH_FORCE: launch_unsort4(n, id, c->acc, t4, 1, s); break;
+    case FSPH_VORTICITY: launch_unsort4(n, id, c->vort, t4, 1, s); break;
+    case FSPH_PREDICT_POS: launch_unsort4(n, id, c->ppos[c->ctl_host->parity & 1], t4, 1, s); break;
+    case FSPH_CORRECTION: {
+        /* position change of the last iteration (after wall projection) */
+        unsigned int par = c->ctl_host->parity & 1;
+        launch_unsort4(n, id, c->ppos[par], t4, 1, s);
+        launch_unsort4(n, id, c->ppos[1 - par], c->set[1].vel, 1, s);
+        std::vector<float4> a((size_t)n), b((size_t)n);
+        FSPH_CUDA(c, cudaMemcpyAsync(a.data(), t4, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(b.data(), c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        for (int i = 0; i < n; ++i) { a[i].x -= b[i].x; a[i].y -= b[i].y; a[i].z -= b[i].z; a[i].w = 0.0f; }
+        if (where == FSPH_HOST) std::memcpy(dst, a.data(), (size_t)n * 16);
+        else FSPH_CUDA(c, cudaMemcpy(dst, a.data(), (size_t)n * 16, cudaMemcpyHostToDevice));
+        return FSPH_OK;
+    }
+    case FSPH_DENSITY:
+    case FSPH_PRESSURE:
+    case FSPH_ATTRIBUTE: {
+        vec = false;
+        const unsigned int *src = type == FSPH_DENSITY ? reinterpret_cast<const unsigned int *>(c->dens)
+                                  : type == FSPH_PRESSURE ? reinterpret_cast<const unsigned int *>(c->pres)
+                                                          : c->set[0].attr;
+        launch_unsort1(n, id, src, c->set[1].id, s);
+        break;
+    }
+    case FSPH_SCALING_FACTOR:
+        vec = false;
+        launch_unsort_w(n, id, c->ppos[1 - (c->ctl_host->parity & 1)], reinterpret_cast<float *>(c->set[1].id), s);
+        break;
+    case FSPH_SORTED_ID:
+        vec = false;
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[1].id, id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        break;
+    default:
+        return fail(c, FSPH_INVALID_ARG, "unknown array type");
+    }
+    FSPH_TRY(check_launch(c));
+    const void *src = vec ? (const void *)t4 : (const void *)c->set[1].id;
+    size_t bytes = (size_t)n * (vec ? 16 : 4);
+    FSPH_CUDA(c, cudaMemcpyAsync(dst, src, bytes, where == FSPH_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    return FSPH_OK;
+}
+
+const void *fsph_device_ptr(fsph_ctx *c, int type) {
+    if (!c) return nullptr;
+    switch (type) {
+    case FSPH_POSITION: return c->set[0].pos;
+    case FSPH_VELOCITY: return c->set[0].vel;
+    case FSPH_FORCE: return c->acc;
+    case FSPH_DENSITY: return c->dens;
+    case FSPH_PRESSURE: return c->pres;
+    case FSPH_ATTRIBUTE: return c->set[0].attr;
+    case FSPH_VORTICITY: return c->vort;
+    case FSPH_SORTED_ID: return c->set[0].id;
+    }
+    c->err = "no device pointer for this array type";
+    return nullptr;
+}
+
+int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long long *total) {
+    if (!c || !offsets || !total) return FSPH_INVALID_ARG;
+    int n = c->n;
+    *total = 0;
+    if (n == 0) { offsets[0] = 0; return FSPH_OK; }
+    DevParams p = make_dev(c->P, n, 1.0f);
+    cudaStream_t s = c->stream;
+    FSPH_TRY(build_on(c, p, c->set[0].pos));
+    unsigned int *cnt = c->rank;
+    launch_nb_count(p, c->cell_start, c->set[1].pos, cnt, s);
+    std::vector<unsigned int> hc((size_t)n), ho((size_t)n + 1);
+    FSPH_CUDA(c, cudaMemcpyAsync(hc.data(), cnt, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    unsigned long long t = 0;
+    for (int i = 0; i < n; ++i) { ho[i] = (unsigned int)t; t += hc[i]; }
+    if (t > 0xffffffffull) return fail(c, FSPH_INVALID_ARG, "more than 2^32 neighbour entries");
+    ho[n] = (unsigned int)t;
+    unsigned int *doff = c->key;
+    int *dout = nullptr;
+    FSPH_CUDA(c, cudaMemcpyAsync(doff, ho.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaMallocAsync((void **)&dout, std::max<size_t>(t, 1) * 4, s));
+    launch_nb_fill(p, c->cell_start, c->set[1].pos, c->set[1].id, doff, dout, s);
+    std::vector<int> hidx((size_t)t), hid((size_t)n);
+    FSPH_CUDA(c, cudaMemcpyAsync(hidx.data(), dout, (size_t)t * 4, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(hid.data(), c->set[1].id, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaFreeAsync(dout, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(check_launch(c));
+    /* rows to particle order, ascending indices within a row */
+    std::vector<unsigned int> cntp((size_t)n + 1, 0);
+    for (int d = 0; d < n; ++d) cntp[(size_t)hid[d] + 1] = hc[d];
+    for (int i = 0; i < n; ++i) cntp[i + 1] += cntp[i];
+    for (int i = 0; i <= n; ++i) offsets[i] = (int)cntp[i];
+    *total = (long long)t;
+    if (indices && cap >= (long long)t) {
+        for (int d = 0; d < n; ++d) {
+            int pi = hid[d];
+            int *row = indices + cntp[pi];
+            std::copy(hidx.begin() + ho[d], hidx.begin() + ho[d] + hc[d], row);
+            std::sort(row, row + hc[d]);
+        }
+    }
+    return FSPH_OK;
+}
+
+int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
+    if (!c || !avg_ms || reps <= 0) return FSPH_INVALID_ARG;
+    if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
+    if (c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "pass timing covers the PBF passes");
+    DevParams p = make_dev(c->P, c->n, c->dp.dt > 0.0f ? c->dp.dt : 1e-3f);
+    cudaStream_t s = c->stream;
+    /* the state after a step: x* = x in the home set, already cell-ordered */
+    FSPH_TRY(build_on(c, p, c->set[0].pos));
+    FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
+    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+    cudaEvent_t e0, e1;
+    FSPH_CUDA(c, cudaEventCreate(&e0));
+    FSPH_CUDA(c, cudaEventCreate(&e1));
+    FSPH_CUDA(c, cudaEventRecord(e0, s));
+    for (int k = 0; k < reps; ++k) {
+        if (pass == FSPH_PASS_LAMBDA) {
+            launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+        } else if (pass == FSPH_PASS_CORRECTION) {
+            launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0,
+                              nullptr, s);
+        } else if (pass == FSPH_PASS_GRID) {
+            enqueue_sort(c, p, c->set[1].pos, s);
+            Gather g{};
+            g.n4 = 3; g.n1 = 1;
+            g.src4[0] = c->set[1].pos; g.dst4[0] = c->set[1].vel;
+            g.src4[1] = c->set[1].pos; g.dst4[1] = c->ppos[1];
+            g.src4[2] = c->set[1].pos; g.dst4[2] = c->acc;
+            g.src1[0] = c->set[1].id; g.dst1[0] = c->set[1].attr;
+            launch_gather(p.n, c->perm, g, nullptr, s);
+        } else {
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            return fail(c, FSPH_INVALID_ARG, "unknown pass");
+        }
+    }
+    FSPH_CUDA(c, cudaEventRecord(e1, s));
+    FSPH_CUDA(c, cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    FSPH_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    FSPH_TRY(check_launch(c));
+    *avg_ms = ms / (float)reps;
+    return FSPH_OK;
+}
+
+int fsph_pbf_eval_lambda(fsph_ctx *c, const float *pos4, int n, float *dens, float *lambda) {
+    if (!c || !pos4 || !dens || !lambda) return FSPH_INVALID_ARG;
+    FSPH_TRY(fsph_set_particles(c, pos4, nullptr, n, FSPH_HOST));
+    if (n == 0) return FSPH_OK;
+    DevParams p = make_dev(c->P, n, 1.0f);
+    cudaStream_t s = c->stream;
+    FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
+    FSPH_TRY(build_on(c, p, c->set[0].pos));
+    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+    FSPH_TRY(check_launch(c));
+    FSPH_TRY(copy_out_scalar(c, c->dens, c->set[1].id, dens, n));
+    launch_unsort_w(n, c->set[1].id, c->ppos[0], reinterpret_cast<float *>(c->key), s);
+    FSPH_CUDA(c, cudaMemcpyAsync(lambda, c->key, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    return FSPH_OK;
+}
+
+int fsph_pbf_eval_correction(fsph_ctx *c, const float *pos4, const float *lambda, int n, float dt, float *dp4) {
+    if (!c || !pos4 || !lambda || !dp4) return FSPH_INVALID_ARG;
+    FSPH_TRY(fsph_set_particles(c, pos4, nullptr, n, FSPH_HOST));
+    if (n == 0) return FSPH_OK;
+    DevParams p = make_dev(c->P, n, dt);
+    cudaStream_t s = c->stream;
+    FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
+    /* lambda rides in x*.w, in particle order before the sort */
+    float *dl = reinterpret_cast<float *>(c->pres);
+    FSPH_CUDA(c, cudaMemcpyAsync(dl, lambda, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    launch_pack_w(n, c->set[0].pos, dl, s);
+    FSPH_TRY(build_on(c, p, c->set[0].pos));
+    launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0, c->acc, s);
+    FSPH_TRY(check_launch(c));
+    launch_unsort4(n, c->set[1].id, c->acc, c->set[0].vel, 1, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(dp4, c->set[0].vel, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    /* the context's particles are left at the given positions, zero velocity */
+    FSPH_TRY(fsph_set_particles(c, pos4, nullptr, n, FSPH_HOST));
+    return FSPH_OK;
+}
+
+int fsph_sph_eval_forces(fsph_ctx *c, const float *pos4, const float *vel4, int n, float *dens, float *pres,
+                         float *acc4) {
+    if (!c || !pos4 || !dens || !pres || !acc4) return FSPH_INVALID_ARG;
+    FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
+    if (n == 0) return FSPH_OK;
+    DevParams p = make_dev(c->P, n, 1.0f);
+    cudaStream_t s = c->stream;
+    enqueue_sort(c, p, c->set[0].pos, s);
+    Gather g{};
+    g.n4 = 2; g.n1 = 1;
+    g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+    g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+    g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
+    launch_gather(n, c->perm, g, nullptr, s);
+    launch_sph_density(p, c->cell_start, c->set[1].pos, c->dens, c->pres, s);
+    launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->acc, s);
+    FSPH_TRY(check_launch(c));
+    FSPH_TRY(copy_out_scalar(c, c->dens, c->set[1].id, dens, n));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(copy_out_scalar(c, c->pres, c->set[1].id, pres, n));
+    launch_unsort4(n, c->set[1].id, c->acc, c->set[0].vel, 1, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(acc4, c->set[0].vel, (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
+    return FSPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+/*
+ * fsph_internal.cuh -- device-side types shared by the fluid-step kernels.
+ *
+ * Data layout in HBM (all arrays in DEVICE order, i.e. sorted by grid cell,
+ * re-sorted at every grid build and carried sorted across steps):
+ *   pos[N], vel[N]      float4  x, v (w unused)
+ *   ppos[2][N]          float4  x* ping-pong; .w of the read buffer carries the
+ *                               particle's lambda between the lambda and
+ *                               correction passes of one iteration
+ *   xb[N]               float4  x* at the last grid build (skin test)
+ *   dens[N], pres[N]    float
+ *   id[N], attr[N]      u32/i32 device slot -> particle index, user tag
+ *   cell_start[C+1]     u32     dense grid, cell c holds slots
+ *                               [cell_start[c], cell_start[c+1])
+ * The grid is a dense cell table over the wall box padded by one cell on
+ * every side (cell width h (1 + skin)), linear index (z Gy + y) Gx + x -- the
+ * reference's hash (rx_cu_common.cu:121-144) without its clamping -- so the
+ * three cells x-1..x+1 of one (y, z) row are one contiguous slot range and a
+ * 27-cell neighbourhood is nine ranges.
+ */
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fsph {
+
+/* Launch-time constants of one solver; passed by value to every kernel. */
+struct DevParams {
+    int n;
+    float h, h2, mass, rest_dens, inv_rest_dens;
+    float aw, ag, al;           /* poly6, spiky-gradient, visc-Laplacian coefficients */
+    float3 wall_lo, wall_hi;    /* box_min + r, box_max - r */
+    float3 gravity;
+    float viscosity, gas_k;
+    float epsilon, eta;
+    int min_iter, max_iter, error_mode, clamp_constraint;
+    int use_ap;
+    float ap_k, ap_n, inv_wq;   /* s_corr = -k (W(r) / W(q h))^n dt^2 */
+    float xsph_c, vort_eps;
+    float3 grid_origin;
+    float inv_cw;
+    int gx, gy, gz;
+    float skin2;                /* (cell_skin * h)^2 */
+    float dt, inv_dt;
+};
+
+/* Device control block of one context: the loop state that the reference
+ * kept on the host (rx_sph_pbd_gpu.cpp:874-921). */
+struct DevCtl {
+    unsigned int iter;          /* iterations executed in this step */
+    unsigned int done;          /* 1 when the loop must stop */
+    unsigned int rebuild;       /* 1 when the grid must be rebuilt before the next pass */
+    unsigned int builds;        /* grid builds in this step */
+    unsigned int ticket;        /* last-block-done counter of the reducing kernels */
+    unsigned int ticket2;
+    unsigned int parity;        /* which ppos buffer holds the current x* */
+    unsigned int nan_flag;
+    unsigned int disp2_bits;    /* max |x* - xb|^2 of the last correction pass (float bits) */
+    unsigned int pad;
+    float err1, err2, errmax;   /* errors of the last lambda pass */
+    float pad2;
+};
+
+/* Per-block partial sums of the lambda pass (one-sided, two-sided, max). */
+struct ErrPartial {
+    float s1, s2, mx, pad;
+};
+
+__host__ __device__ inline float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ inline float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ inline float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ inline float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+__device__ inline float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ inline float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+/* Box-wall projection keeping the particle radius: clamp each axis to
+ * [box_min + r, box_max - r].  This is the contact point of the reference's
+ * rxSolidBox::GetDistanceR / AABB_point_dist (rx_sph_solid.cpp:44-108,
+ * 244-262) for faces, edges and corners alike; velocity is not reflected,
+ * as in rx_sph_pbd.cpp:1392. */
+__device__ inline float3 wall_project(float3 x, const DevParams &p) {
+    x.x = fminf(fmaxf(x.x, p.wall_lo.x), p.wall_hi.x);
+    x.y = fminf(fmaxf(x.y, p.wall_lo.y), p.wall_hi.y);
+    x.z = fminf(fmaxf(x.z, p.wall_lo.z), p.wall_hi.z);
+    return x;
+}
+
+/* Cell coordinates of a position, clamped to the interior cells [1, G-2] so
+ * that every 27-cell neighbourhood stays inside the padded table. */
+__device__ inline int3 cell_of(float3 x, const DevParams &p) {
+    float fx = (x.x - p.grid_origin.x) * p.inv_cw;
+    float fy = (x.y - p.grid_origin.y) * p.inv_cw;
+    float fz = (x.z - p.grid_origin.z) * p.inv_cw;
+    int cx = (fx == fx) ? (int)floorf(fminf(fmaxf(fx, 1.0f), (float)(p.gx - 2))) : 1;
+    int cy = (fy == fy) ? (int)floorf(fminf(fmaxf(fy, 1.0f), (float)(p.gy - 2))) : 1;
+    int cz = (fz == fz) ? (int)floorf(fminf(fmaxf(fz, 1.0f), (float)(p.gz - 2))) : 1;
+    return make_int3(cx, cy, cz);
+}
+
+__device__ inline unsigned int cell_index(int3 c, const DevParams &p) {
+    return ((unsigned int)c.z * (unsigned int)p.gy + (unsigned int)c.y) * (unsigned int)p.gx + (unsigned int)c.x;
+}
+
+/* Slot range [s, e) of the three cells x-1..x+1 in row (y + dy, z + dz). */
+__device__ inline void row_range(const unsigned int *__restrict__ cell_start, int3 c, int dy, int dz,
+                                 const DevParams &p, unsigned int &s, unsigned int &e) {
+    unsigned int base = ((unsigned int)(c.z + dz) * (unsigned int)p.gy + (unsigned int)(c.y + dy)) * (unsigned int)p.gx +
+                        (unsigned int)c.x;
+    s = __ldg(cell_start + base - 1);
+    e = __ldg(cell_start + base + 2);
+}
+
+/* Warp/block reductions. */
+__device__ inline float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ inline float warp_max(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+}  // namespace fsph

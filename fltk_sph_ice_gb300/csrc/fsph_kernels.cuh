@@ -1,0 +1,95 @@
+/*
+ * fsph_kernels.cuh -- host-callable launchers of the fluid-step kernels
+ * (defined in fsph_kernels.cu).  Every launcher enqueues on `s` and returns
+ * without synchronising.
+ */
+#pragma once
+#include "fsph_internal.cuh"
+
+namespace fsph {
+
+constexpr int kBlock = 256;
+constexpr int kScanTile = 4096; /* cells per block of the first scan phase */
+
+inline unsigned int blocks_for(long long n, int b = kBlock) { return (unsigned int)((n + b - 1) / b); }
+inline unsigned int scan_blocks(unsigned int ncells) { return (ncells + kScanTile - 1) / kScanTile; }
+
+/* ---- grid build: counting sort on the 64-bit key (cell << 32 | previous slot) ---- */
+/* x* = walls(x + dt (v + dt a)), a = gravity when acc == NULL; then key + rank. */
+void launch_predict_hash(const DevParams &p, const float4 *pos, const float4 *vel, const float4 *acc,
+                         float4 *ppos_out, unsigned int *key, unsigned int *rank, unsigned int *count,
+                         cudaStream_t s);
+void launch_hash(const DevParams &p, const float4 *x, unsigned int *key, unsigned int *rank, unsigned int *count,
+                 cudaStream_t s);
+/* exclusive scan of count[C] into cell_start[C+1]; zeroes count for the next build */
+void launch_scan(unsigned int *count, unsigned int *cell_start, unsigned int *block_sums, unsigned int ncells,
+                 cudaStream_t s);
+/* perm[cell_start[key] + rank] = slot, then each cell's slots sorted ascending */
+void launch_scatter_sort(const DevParams &p, const unsigned int *key, const unsigned int *rank,
+                         const unsigned int *cell_start, unsigned int *perm, unsigned int ncells, cudaStream_t s);
+
+/* dst[d] = src[perm[d]] for up to 6 float4 and 4 u32 streams (perm == NULL: plain copy) */
+struct Gather {
+    const float4 *src4[6];
+    float4 *dst4[6];
+    const unsigned int *src1[4];
+    unsigned int *dst1[4];
+    int n4, n1;
+};
+void launch_gather(int n, const unsigned int *perm, const Gather &g, DevCtl *count_build, cudaStream_t s);
+
+/* in-loop rebuild (the current x* buffer is chosen on the device by ctl->parity) */
+void launch_hash_parity(const DevParams &p, const float4 *ppos0, const float4 *ppos1, const DevCtl *ctl,
+                        unsigned int *key, unsigned int *rank, unsigned int *count, cudaStream_t s);
+void launch_rebuild_gather(int n, const unsigned int *perm, const DevCtl *ctl, const float4 *pos, const float4 *ppos0,
+                           const float4 *ppos1, const unsigned int *id, const unsigned int *attr, const float *dens,
+                           float4 *t_pos, float4 *t_x, unsigned int *t_id, unsigned int *t_attr, float *t_dens,
+                           cudaStream_t s);
+void launch_rebuild_copy(int n, DevCtl *ctl, const float4 *t_pos, const float4 *t_x, const unsigned int *t_id,
+                         const unsigned int *t_attr, const float *t_dens, float4 *pos, float4 *ppos0, float4 *ppos1,
+                         float4 *xb, unsigned int *id, unsigned int *attr, float *dens, cudaStream_t s);
+
+/* ---- PBF ---- */
+void launch_pbf_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
+                        cudaStream_t s);
+void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
+                     const float *dens, float4 *acc, cudaStream_t s);
+void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1, float *dens,
+                   DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
+                   cudaStream_t s);
+void launch_correction(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1,
+                       const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,
+                       unsigned long long if_handle2, int use_graph, float4 *dp_out, cudaStream_t s);
+void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
+                     const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,
+                     float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, cudaStream_t s);
+void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
+                      const float *dens, float4 *vel_out, float4 *vort, cudaStream_t s);
+void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
+                       const float *dens, const float4 *vel_in, float4 *vel_out, cudaStream_t s);
+
+/* ---- WCSPH ---- */
+void launch_sph_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
+                        float *pres, cudaStream_t s);
+void launch_sph_force(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
+                      const float *dens, const float *pres, float4 *acc, cudaStream_t s);
+void launch_sph_integrate(const DevParams &p, const float4 *pos_b, const float4 *vel_b, const float4 *acc,
+                          const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a, float4 *vel_a,
+                          unsigned int *id_a, unsigned int *attr_a, cudaStream_t s);
+
+/* ---- neighbour sets under the reference criterion ---- */
+void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const float4 *pos, unsigned int *cnt,
+                     cudaStream_t s);
+void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
+                    const unsigned int *offsets, int *out, cudaStream_t s);
+
+/* ---- particle order <-> device order ---- */
+void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s);
+void launch_unsort1(int n, const unsigned int *id, const unsigned int *src, unsigned int *dst, cudaStream_t s);
+void launch_unsort_w(int n, const unsigned int *id, const float4 *src, float *dst, cudaStream_t s);
+void launch_iota(int n, unsigned int *dst, cudaStream_t s);
+void launch_pack_w(int n, float4 *dst, const float *w, cudaStream_t s);
+/* *flag |= 1 when any x/y/z of a (or b, if given) is not finite */
+void launch_check_finite(int n, const float4 *a, const float4 *b, unsigned int *flag, cudaStream_t s);
+
+}  // namespace fsph

@@ -1,0 +1,229 @@
+"""Python mirror of the reference's particle-system operator surface.
+
+rxParticleSystemBase (rx_ps.h:55-333) with its concrete solvers rxSPH
+(WCSPH, rx_sph.h:202-426) and rxPBDSPH (PBF, rx_sph.h:1027-1274): the same
+method names and meanings (Set, Update, GetArrayVBO, SetArrayVBO,
+SetParticlesToCell / GetNeights, SetGravity, SetIterations ...), implemented
+over the C ABI of libfsph.so (include/fsph.h).  Errors raise FsphError with
+the library's status and message; nothing here computes physics.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import abi
+from .abi import FsphError
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class rxParticleSystemBase:
+    """One GPU fluid context (fsph_ctx)."""
+
+    solver = abi.SOLVER_PBF
+
+    def __init__(self, params: abi.FsphParams):
+        self.L = abi.lib()
+        p = abi.FsphParams.from_buffer_copy(params)
+        p.solver = self.solver
+        self._ctx = ctypes.c_void_p()
+        st = self.L.fsph_create(ctypes.byref(p), ctypes.byref(self._ctx))
+        if st != abi.OK:
+            raise FsphError(st, "fsph_create failed")
+        self.last_stats = abi.FsphStepStats()
+
+    # -- lifetime -------------------------------------------------------
+    def close(self):
+        if getattr(self, "_ctx", None) and self._ctx.value:
+            self.L.fsph_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int, what: str):
+        if st != abi.OK:
+            msg = self.L.fsph_last_error(self._ctx)
+            raise FsphError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._ctx
+
+    # -- Initialize / parameters -----------------------------------------
+    @classmethod
+    def from_env(cls, env: abi.FsphEnv):
+        """rxPBDSPH::Initialize / rxSPH::Initialize derivation from a scene env."""
+        p = abi.FsphParams()
+        L = abi.lib()
+        e = abi.FsphEnv.from_buffer_copy(env)
+        e.solver = cls.solver
+        st = L.fsph_params_from_env(ctypes.byref(e), ctypes.byref(p))
+        if st != abi.OK:
+            raise FsphError(st, "fsph_params_from_env")
+        return cls(p)
+
+    def GetParams(self) -> abi.FsphParams:
+        p = abi.FsphParams()
+        self._check(self.L.fsph_get_params(self._ctx, ctypes.byref(p)), "fsph_get_params")
+        return p
+
+    def SetParams(self, p: abi.FsphParams):
+        q = abi.FsphParams.from_buffer_copy(p)
+        q.solver = self.solver
+        self._check(self.L.fsph_set_params(self._ctx, ctypes.byref(q)), "fsph_set_params")
+
+    def SetGravity(self, g: float):
+        """rx_ps.h:227 -- gravity (0, g, 0)."""
+        p = self.GetParams()
+        p.gravity[0], p.gravity[1], p.gravity[2] = 0.0, g, 0.0
+        self.SetParams(p)
+
+    def SetIterations(self, i: int):
+        """rx_ps.h:220 -- solver iteration cap."""
+        p = self.GetParams()
+        p.max_iter = int(i)
+        self.SetParams(p)
+
+    def GetNumParticles(self) -> int:
+        return int(self.L.fsph_num_particles(self._ctx))
+
+    def GetMaxParticles(self) -> int:
+        return int(self.GetParams().max_particles)
+
+    def GetParticleRadius(self) -> float:
+        return float(self.GetParams().particle_radius)
+
+    # -- particle data ---------------------------------------------------
+    def Set(self, pos, vel=None) -> bool:
+        """rxParticleSystemBase::Set (rx_ps.cpp:30-59); pos/vel (N,3) or (N,4)."""
+        pos4 = _as4(pos)
+        vel4 = None if vel is None else _as4(vel)
+        self._check(self.L.fsph_set_particles(self._ctx, _ptr(pos4), _ptr(vel4), pos4.shape[0], abi.HOST),
+                    "fsph_set_particles")
+        return True
+
+    def SetArrayVBO(self, type_: int, data, start: int = 0, count: int | None = None):
+        """SetArrayVBO (rx_ps.h:260-262): overwrite `count` particles from `start`."""
+        if type_ == abi.RX_ATTRIBUTE:
+            arr = np.ascontiguousarray(data, dtype=np.int32).reshape(-1)
+        else:
+            arr = _as4(data)
+        n = arr.shape[0] if count is None else int(count)
+        self._check(self.L.fsph_set_array(self._ctx, type_, _ptr(arr), int(start), n, abi.HOST), "fsph_set_array")
+
+    def GetArrayVBO(self, type_: int, d2h: bool = True) -> np.ndarray:
+        """GetArrayVBO (rx_ps.h:259): a copy of one array in particle order."""
+        n = self.GetNumParticles()
+        if type_ in abi.VECTOR_ARRAYS:
+            out = np.zeros((n, 4), dtype=np.float32)
+        elif type_ in (abi.RX_ATTRIBUTE, abi.FSPH_SORTED_ID):
+            out = np.zeros(n, dtype=np.int32)
+        else:
+            out = np.zeros(n, dtype=np.float32)
+        if n:
+            self._check(self.L.fsph_get_array(self._ctx, type_, _ptr(out), abi.HOST, None), "fsph_get_array")
+        return out
+
+    def GetParticle(self) -> np.ndarray:
+        return self.GetArrayVBO(abi.RX_POSITION)
+
+    def GetParticleDevice(self) -> int:
+        """Borrowed device pointer (device order) to the positions."""
+        return int(self.L.fsph_device_ptr(self._ctx, abi.RX_POSITION) or 0)
+
+    # -- step ------------------------------------------------------------
+    def Update(self, dt: float, step: int = 0, stats: bool = True) -> bool:
+        """rxParticleSystemBase::Update (rx_ps.h:254): advance one step."""
+        st = self.L.fsph_step(self._ctx, float(dt), None, ctypes.byref(self.last_stats) if stats else None)
+        self._check(st, "fsph_step")
+        return True
+
+    def Sync(self):
+        self._check(self.L.fsph_sync(self._ctx), "fsph_sync")
+
+    def LastStats(self) -> abi.FsphStepStats:
+        self._check(self.L.fsph_last_stats(self._ctx, ctypes.byref(self.last_stats)), "fsph_last_stats")
+        return self.last_stats
+
+    # -- neighbours --------------------------------------------------------
+    def GetNeights(self):
+        """Neighbour sets of the current positions (GetNeights, rx_sph.h:1196) as
+        CSR (offsets[n+1], indices), particle indices ascending in each row."""
+        n = self.GetNumParticles()
+        off = np.zeros(n + 1, dtype=np.int32)
+        total = ctypes.c_longlong(0)
+        self._check(self.L.fsph_neighbors(self._ctx, _ptr(off), None, 0, ctypes.byref(total)), "fsph_neighbors")
+        idx = np.zeros(max(total.value, 1), dtype=np.int32)
+        self._check(self.L.fsph_neighbors(self._ctx, _ptr(off), _ptr(idx), total.value, ctypes.byref(total)),
+                    "fsph_neighbors")
+        return off, idx[:total.value]
+
+    SetParticlesToCell = GetNeights
+
+
+class rxSPH(rxParticleSystemBase):
+    """WCSPH solver (rxSPH / rxSPH_GPU)."""
+
+    solver = abi.SOLVER_WCSPH
+
+    def EvalForces(self, pos, vel):
+        """calDensity + calForce on the given state (rx_sph_cpu.cpp:495-656)."""
+        pos4, vel4 = _as4(pos), _as4(vel)
+        n = pos4.shape[0]
+        d = np.zeros(n, np.float32)
+        p = np.zeros(n, np.float32)
+        a = np.zeros((n, 4), np.float32)
+        self._check(self.L.fsph_sph_eval_forces(self._ctx, _ptr(pos4), _ptr(vel4), n, _ptr(d), _ptr(p), _ptr(a)),
+                    "fsph_sph_eval_forces")
+        return d, p, a
+
+
+class rxPBDSPH(rxParticleSystemBase):
+    """PBF solver (rxPBDSPH / rxPBDSPH_GPU)."""
+
+    solver = abi.SOLVER_PBF
+
+    def EvalScalingFactor(self, pos):
+        """calScalingFactor on the given predicted positions (rx_sph_pbd.cpp:699-914)."""
+        pos4 = _as4(pos)
+        n = pos4.shape[0]
+        d = np.zeros(n, np.float32)
+        lam = np.zeros(n, np.float32)
+        self._check(self.L.fsph_pbf_eval_lambda(self._ctx, _ptr(pos4), n, _ptr(d), _ptr(lam)),
+                    "fsph_pbf_eval_lambda")
+        return d, lam
+
+    def EvalPositionCorrection(self, pos, lam, dt: float):
+        """calPositionCorrection (rx_sph_pbd.cpp:925-1026)."""
+        pos4 = _as4(pos)
+        lam = np.ascontiguousarray(lam, dtype=np.float32)
+        n = pos4.shape[0]
+        dp = np.zeros((n, 4), np.float32)
+        self._check(self.L.fsph_pbf_eval_correction(self._ctx, _ptr(pos4), _ptr(lam), n, float(dt), _ptr(dp)),
+                    "fsph_pbf_eval_correction")
+        return dp
+
+
+def _as4(a) -> np.ndarray:
+    a = np.asarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] not in (3, 4):
+        raise ValueError("expected an (N, 3) or (N, 4) array")
+    if a.shape[1] == 3:
+        b = np.zeros((a.shape[0], 4), dtype=np.float32)
+        b[:, :3] = a
+        a = b
+    return np.ascontiguousarray(a)

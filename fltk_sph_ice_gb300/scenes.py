@@ -1,0 +1,223 @@
+"""Seeded synthetic scenes: the replacement of the reference's scene loader.
+
+The reference fills its particles through rxSPHConfig::SetLiquidBox ->
+rxParticleSystemBase::AddBox (rx_sph_config.h:257-269, rx_ps.cpp:195-261): a
+cubic lattice with a small uniform jitter drawn from ``srand(time(NULL))``.
+Here the same kind of block is drawn from a counter-based generator
+(SplitMix64 of (seed, stream, particle index)), so a scene is the same bytes
+on every machine and in every process, and the CPU oracle and the GPU run
+start from identical states.
+
+Workloads (the configurations the fluid step is measured on):
+  wcsph_dam_break      32^3 WCSPH dam break; h = 0.0457, m = 0.02, rho0 = 998.29,
+                       k = 3, mu = 3.5 / rho0, dt = 1e-3, 200 steps
+  pbf_dam_break        64^3 PBF dam break; eps = 100, 4 iterations, s_corr k=0.1 n=4
+                       q=0.2, XSPH c = 0.01, vorticity 1e-4, dt = 0.0016
+  pbf_double_dam_break 1,048,576 particles in two 64x64x128 blocks (the benchmark
+                       workload); iterate to mean one-sided density error <= 0.1 %
+  batched_scenes       256 independent PBF scenes, N_s log-uniform in [2048, 65536]
+
+Geometry: every lattice has spacing h/2 (about 33 neighbours per particle),
+the particle radius used by the walls is h/4 (half the spacing), and the
+boxes are sized so the stated blocks fit at the stated h; the particle mass
+is the one for which the h/2 lattice sums to rho0 (PBF configurations).
+Box sides are the longest side divided by powers of two (or within a factor
+sqrt(2) above one): the reference's CPU grid rounds every axis to a
+power-of-two cell count (rx_nnsearch.h:174-217) and, when an axis rounds
+down, leaves the far end of the box outside the grid, where its neighbour
+query then misses neighbours.  With these ratios its grid covers the box and
+its neighbour sets are the geometric ones.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from . import abi
+
+H_DEFAULT = 0.0457
+REST_DENS = 998.29
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    """SplitMix64 finaliser (Steele, Lea, Flood 2014), vectorised over uint64."""
+    with np.errstate(over="ignore"):
+        z = (x + np.uint64(0x9E3779B97F4A7C15)) & _M64
+        z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+        z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, stream: int, idx: np.ndarray) -> np.ndarray:
+    """U[0,1) doubles, one per index, from (seed, stream, idx)."""
+    with np.errstate(over="ignore"):
+        base = splitmix64(np.array([(seed * 0x100000001B3 + stream) & 0xFFFFFFFFFFFFFFFF], dtype=np.uint64))[0]
+        x = splitmix64((idx.astype(np.uint64) * np.uint64(0xD1B54A32D192ED03)) ^ base)
+    return (x >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def poly6(r: np.ndarray, h: float) -> np.ndarray:
+    aw = 315.0 / (64.0 * math.pi * h ** 9)
+    q = h * h - r * r
+    return np.where((r >= 0) & (r <= h), aw * q * q * q, 0.0)
+
+
+def lattice_mass(h: float, spacing: float, rest_dens: float = REST_DENS) -> float:
+    """Mass for which a cubic lattice of the given spacing has density rest_dens
+    (the inverse of calRestDensity, rx_sph_pbd.cpp:1035-1049)."""
+    n = int(math.ceil(h / spacing)) + 1
+    ax = np.arange(-n, n + 1) * spacing
+    x, y, z = np.meshgrid(ax, ax, ax, indexing="ij")
+    s = poly6(np.sqrt(x * x + y * y + z * z), h).sum()
+    return float(rest_dens / s)
+
+
+def lattice_block(origin, dims, spacing: float, jitter: float, seed: int, stream: int) -> np.ndarray:
+    """float32 (N, 4) positions of a jittered cubic lattice, x fastest
+    (the loop order of AddBox, rx_ps.cpp:215-240), w = 0."""
+    nx, ny, nz = (int(d) for d in dims)
+    n = nx * ny * nz
+    idx = np.arange(n, dtype=np.int64)
+    i = idx % nx
+    j = (idx // nx) % ny
+    k = idx // (nx * ny)
+    pos = np.zeros((n, 4), dtype=np.float64)
+    for a, (o, c) in enumerate(zip(origin, (i, j, k))):
+        u = uniform(seed, stream * 3 + a, idx)
+        pos[:, a] = o + c * spacing + (2.0 * u - 1.0) * jitter
+    return pos.astype(np.float32)
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    pos: np.ndarray          # (N, 4) float32
+    vel: np.ndarray          # (N, 4) float32
+    params: abi.FsphParams
+    dt: float
+    steps: int
+    fixed_iters: int = 0     # > 0: run exactly this many PBF iterations per step
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+
+def pbf_params(h: float, box_min, box_max, n: int, **kw) -> abi.FsphParams:
+    p = abi.FsphParams()
+    p.solver = abi.SOLVER_PBF
+    p.max_particles = n
+    p.h = h
+    p.rest_dens = REST_DENS
+    p.mass = lattice_mass(h, 0.5 * h)
+    p.particle_radius = 0.25 * h
+    for a in range(3):
+        p.box_min[a] = box_min[a]
+        p.box_max[a] = box_max[a]
+    p.gravity[0], p.gravity[1], p.gravity[2] = 0.0, -9.81, 0.0
+    p.viscosity = 0.0
+    p.gas_k = 3.0
+    p.epsilon = 100.0
+    p.eta = 1e-3
+    p.min_iter = 2
+    p.max_iter = 100
+    p.error_mode = abi.ERR_ONE_SIDED
+    p.use_ap = 1
+    p.ap_k, p.ap_n, p.ap_q = 0.1, 4.0, 0.2
+    p.xsph_c = 0.01
+    p.vort_eps = 1e-4
+    p.cell_skin = 0.02
+    p.use_graph = 1
+    p.warm_start = 0
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _block_origin(box_min, h):
+    s = 0.5 * h
+    return [b + 0.5 * s + 0.01 * h for b in box_min]
+
+
+def wcsph_dam_break(n_side: int = 32, h: float = H_DEFAULT, seed: int = 1) -> Scene:
+    """32^3 WCSPH dam break.  The stated [0,1]x[0,0.6]x[0,0.4] box cannot hold a
+    32^3 block at spacing h/2 (0.73 m per side), so the box is enlarged to
+    [0,2]x[0,1.2]x[0,1.0].  mu = 3.5 / rho0: the reference multiplies an
+    acceleration by mu (rx_sph_cpu.cpp:626-633), and mu = 3.5 is unstable at dt = 1e-3."""
+    s = 0.5 * h
+    scale = max(1.0, n_side / 32.0)
+    box_min = [0.0, 0.0, 0.0]
+    box_max = [2.0 * scale, 1.2 * scale, 1.0 * scale]
+    pos = lattice_block(_block_origin(box_min, h), (n_side, n_side, n_side), s, 0.01 * h, seed, 0)
+    p = pbf_params(h, box_min, box_max, pos.shape[0])
+    p.solver = abi.SOLVER_WCSPH
+    p.mass = 0.02
+    p.rest_dens = REST_DENS
+    p.gas_k = 3.0
+    p.viscosity = 3.5 / REST_DENS
+    p.xsph_c = 0.0
+    p.vort_eps = 0.0
+    return Scene("wcsph_dam_break", pos, np.zeros_like(pos), p, 1e-3, 200)
+
+
+def pbf_dam_break(n_side: int = 64, h: float = H_DEFAULT, seed: int = 2) -> Scene:
+    """64^3 PBF dam break with 4 fixed iterations.  The stated 1x1x0.5 box
+    cannot hold a 64^3 block at spacing h/2 (1.46 m), so it is scaled by 3."""
+    s = 0.5 * h
+    ext = n_side * s
+    box_min = [0.0, 0.0, 0.0]
+    L = max(1.0, 2.05 * ext)
+    box_max = [L, L, 0.5 * L]
+    pos = lattice_block(_block_origin(box_min, h), (n_side, n_side, n_side), s, 0.01 * h, seed, 0)
+    p = pbf_params(h, box_min, box_max, pos.shape[0])
+    return Scene("pbf_dam_break", pos, np.zeros_like(pos), p, 0.0016, 500, fixed_iters=4)
+
+
+def pbf_double_dam_break(block=(64, 64, 128), h: float = H_DEFAULT, seed: int = 3,
+                         eta: float = 1e-3) -> Scene:
+    """Two water columns at opposite ends of a long box collapsing toward each
+    other; with the default 64x64x128 blocks, 1,048,576 particles.  The box is
+    L x L/4 x L/2 with L = 4.1 block widths (blocks need by <= bx, bz <= 2 bx)."""
+    s = 0.5 * h
+    bx, by, bz = block
+    if by > bx or bz > 2 * bx:
+        raise ValueError("block must satisfy by <= bx and bz <= 2 bx")
+    L = 4.1 * bx * s
+    box_min = [0.0, 0.0, 0.0]
+    box_max = [L, 0.25 * L, 0.5 * L]
+    o = _block_origin(box_min, h)
+    a = lattice_block(o, block, s, 0.01 * h, seed, 0)
+    o2 = [box_max[0] - o[0] - (bx - 1) * s, o[1], o[2]]
+    b = lattice_block(o2, block, s, 0.01 * h, seed, 1)
+    pos = np.concatenate([a, b])
+    p = pbf_params(h, box_min, box_max, pos.shape[0], eta=eta)
+    return Scene("pbf_double_dam_break", pos, np.zeros_like(pos), p, 0.0016, 500)
+
+
+def batched_scenes(count: int = 256, seed: int = 4, n_lo: int = 2048, n_hi: int = 65536) -> list[Scene]:
+    """Independent PBF scenes: N_s log-uniform in [n_lo, n_hi], box side
+    uniform in [0.3, 1.0]^3, fill fraction uniform in [0.2, 0.5]; spacing
+    (fill V / N_s)^(1/3) and h = 2 spacing, so every scene keeps ~33 neighbours."""
+    idx = np.arange(count, dtype=np.int64)
+    un = uniform(seed, 100, idx)
+    ub = [uniform(seed, 101 + a, idx) for a in range(3)]
+    uf = uniform(seed, 104, idx)
+    out = []
+    for s_i in range(count):
+        n_target = int(round(math.exp(math.log(n_lo) + un[s_i] * (math.log(n_hi) - math.log(n_lo)))))
+        L = [0.3 + 0.7 * ub[a][s_i] for a in range(3)]
+        fill = 0.2 + 0.3 * uf[s_i]
+        vol = fill * L[0] * L[1] * L[2]
+        sp = (vol / n_target) ** (1.0 / 3.0)
+        ext = [L[a] * fill ** (1.0 / 3.0) for a in range(3)]
+        dims = [max(2, int(round(e / sp))) for e in ext]
+        h = 2.0 * sp
+        box_max = [max(L[a], dims[a] * sp + 0.05 * h) for a in range(3)]
+        pos = lattice_block(_block_origin([0, 0, 0], h), dims, sp, 0.01 * h, seed + 1000 + s_i, 0)
+        p = pbf_params(h, [0, 0, 0], box_max, pos.shape[0])
+        out.append(Scene(f"batched_{s_i}", pos, np.zeros_like(pos), p, 0.0016, 500, fixed_iters=4))
+    return out

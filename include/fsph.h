@@ -1,0 +1,242 @@
+/*
+ * fsph.h -- C ABI of the GB300-native fluid step (hashed-grid neighbour search,
+ * WCSPH density/pressure/viscosity pass, PBF density-constraint iterations).
+ *
+ * This ABI replaces the reference's thin C layer between its C++ particle
+ * classes and CUDA (the `Cu*` functions declared in rx_cu_funcs.cuh:24-253,
+ * fluid subset rx_cu_funcs.cuh:54-135) and carries the operator surface of
+ * rxParticleSystemBase (rx_ps.h:55-333) / rxSPH (rx_sph.h:202-426) /
+ * rxPBDSPH (rx_sph.h:1027-1274): create + Initialize, SetArrayVBO-style
+ * setters, Update(dt), GetArrayVBO-style getters, neighbour access.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Vector arrays are float4 per particle
+ *    (x, y, z, w) -- the reference's DIM = 4 stride (rx_ps.h:31-33); scalar
+ *    arrays are one float per particle.
+ *  - Every call returns an fsph_status; no exception crosses the ABI.  The
+ *    text of the last error of a context is fsph_last_error(ctx).
+ *  - `stream` arguments are a cudaStream_t passed as void* (NULL = the
+ *    context's own stream).  Work is asynchronous on that stream except where
+ *    a call says it synchronises (getters into host memory, stats).
+ *  - One context per host thread at a time.  There is no CPU fallback: a
+ *    context cannot be created without a CUDA device.
+ */
+#ifndef FSPH_H
+#define FSPH_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FSPH_ABI_VERSION 1
+
+/* Status codes.  The reference printed CUDA errors and discarded them
+ * (RX_CUCHECK / RX_CUERROR, rx_cuda_utils.h:22-54). */
+typedef enum fsph_status {
+    FSPH_OK = 0,
+    FSPH_INVALID_ARG = 1,
+    FSPH_OOM = 2,
+    FSPH_CUDA_ERROR = 3,
+    FSPH_NAN_DETECTED = 4,
+    FSPH_TIMEOUT = 5,
+    FSPH_NOT_CONVERGED = 6,
+    FSPH_NOT_INITIALIZED = 7,
+    FSPH_UNSUPPORTED = 8,
+    FSPH_NO_DEVICE = 9
+} fsph_status;
+
+typedef enum fsph_solver {
+    FSPH_SOLVER_WCSPH = 0, /* rxSPH::Update (rx_sph_cpu.cpp:323-380) */
+    FSPH_SOLVER_PBF = 1    /* rxPBDSPH::Update (rx_sph_pbd.cpp:377-484) */
+} fsph_solver;
+
+/* Density-error definition used by the PBF convergence test.
+ * ONE_SIDED = mean(max(rho - rho0, 0) / rho0), the reference GPU form
+ * (rx_pbdsph_kernel.cu:431-441); TWO_SIDED = mean(|rho - rho0| / rho0), the
+ * reference CPU form (rx_sph_pbd.cpp:448-454). */
+typedef enum fsph_error_mode {
+    FSPH_ERR_ONE_SIDED = 0,
+    FSPH_ERR_TWO_SIDED = 1
+} fsph_error_mode;
+
+/* Where a host-side pointer argument lives. */
+typedef enum fsph_where {
+    FSPH_HOST = 0,
+    FSPH_DEVICE = 1
+} fsph_where;
+
+/* Particle arrays; numbering follows rxParticleSystemBase::rxParticleArray
+ * (rx_ps.h:68-116) so reference callers keep their constants. */
+typedef enum fsph_array {
+    FSPH_POSITION = 0,        /* float4 */
+    FSPH_VELOCITY = 1,        /* float4 */
+    FSPH_FORCE = 3,           /* float4, acceleration of the last force pass */
+    FSPH_DENSITY = 4,         /* float */
+    FSPH_PRESSURE = 5,        /* float, WCSPH only */
+    FSPH_ATTRIBUTE = 7,       /* int (stored as 32-bit), user tag carried with the particle */
+    FSPH_PREDICT_POS = 8,     /* float4, PBF x* */
+    FSPH_PREDICT_VEL = 9,     /* float4, PBF v* */
+    FSPH_SCALING_FACTOR = 10, /* float, PBF lambda */
+    FSPH_CORRECTION = 11,     /* float4, PBF delta-p of the last iteration */
+    FSPH_VORTICITY = 18,      /* float4, omega of the last finalize pass */
+    FSPH_SORTED_ID = 64       /* int, device order -> particle index (device_ptr only) */
+} fsph_array;
+
+/* Solver parameters.  Mirrors rxSPHEnviroment (rx_sph.h:95-182) after the
+ * reference's Initialize has derived h, r and rho0 from it; use
+ * fsph_params_from_env for that derivation, or fill the derived values
+ * directly (explicit h / rho0 / m, as the benchmark configurations do). */
+typedef struct fsph_params {
+    int solver;              /* fsph_solver */
+    int max_particles;
+    float h;                 /* effective (kernel) radius */
+    float mass;              /* particle mass */
+    float rest_dens;         /* rho0 */
+    float particle_radius;   /* wall clearance of the box projection */
+    double box_min[3];       /* fluid box (rxSolidBox boundary, rx_sph_pbd.cpp:168) */
+    double box_max[3];
+    float gravity[3];        /* acceleration, e.g. (0, -9.81, 0) */
+    float viscosity;         /* mu; WCSPH viscosity term, PBF pre-pass viscosity */
+    float gas_k;             /* WCSPH gas stiffness, p = k (rho - rho0) */
+    /* PBF */
+    float epsilon;           /* CFM relaxation in lambda = -C / (sum |grad C|^2 + epsilon) */
+    float eta;               /* density-error tolerance of the iteration loop */
+    int min_iter;
+    int max_iter;
+    int error_mode;          /* fsph_error_mode */
+    int use_ap;              /* tensile-instability correction s_corr on/off */
+    float ap_k, ap_n, ap_q;  /* s_corr = -k (W(r) / W(q h))^n dt^2 */
+    float xsph_c;            /* XSPH velocity smoothing c (0 = off) */
+    float vort_eps;          /* vorticity confinement epsilon (0 = off) */
+    /* GPU grid */
+    float cell_skin;         /* cell width = h (1 + cell_skin); the grid is rebuilt
+                                inside a step only when a particle moved more than
+                                cell_skin * h since the last build */
+    int use_graph;           /* 1: capture the step (with a device-side while loop) in a CUDA graph */
+    int warm_start;          /* 0: plain; 1: learned MLP warm start of the PBF iterations */
+    int clamp_constraint;    /* 0: C = rho/rho0 - 1 as the reference (rx_sph_pbd.cpp:751);
+                                1: unilateral C = max(rho/rho0 - 1, 0) (opt-in, not the reference) */
+    int reserved[6];
+} fsph_params;
+
+/* Scene description in the reference's own terms (rxSPHEnviroment). */
+typedef struct fsph_env {
+    int solver;
+    int max_particles;
+    double boundary_cen[3];
+    double boundary_ext[3];
+    float dens, mass, kernel_particles, viscosity, gas_k;
+    float epsilon, eta;
+    int min_iter, max_iter;
+    int use_ap;
+    float ap_k, ap_n, ap_q;
+    float gravity_y;
+} fsph_env;
+
+/* Per-step statistics (the reference's g_iIterations / g_fEta,
+ * rx_sph_pbd.cpp:461-462, plus both error definitions). */
+typedef struct fsph_step_stats {
+    int iterations;               /* constraint iterations executed */
+    int grid_builds;              /* grid builds inside the step (>= 1) */
+    float density_error;          /* error of the last iteration, params.error_mode */
+    float density_error_one_sided;
+    float density_error_two_sided;
+    float density_error_max;      /* max_i |rho_i - rho0| / rho0 */
+    int status;                   /* FSPH_OK, FSPH_NOT_CONVERGED, FSPH_NAN_DETECTED */
+    int reserved[3];
+} fsph_step_stats;
+
+typedef struct fsph_ctx fsph_ctx;
+
+/* ---- version / errors ---- */
+int fsph_abi_version(void);
+const char *fsph_status_string(int status);
+const char *fsph_last_error(const fsph_ctx *ctx);
+
+/* ---- parameters ---- */
+/* rxPBDSPH::Initialize / rxSPH::Initialize derivation (rx_sph_pbd.cpp:102-201,
+ * rx_sph_cpu.cpp:92-166): h from kernel_particles, r, rho0 by calRestDensity,
+ * box = cen -/+ ext.  Fills the remaining fields with defaults. */
+int fsph_params_from_env(const fsph_env *env, fsph_params *out);
+/* Defaults for every field (solver PBF, no particles). */
+void fsph_params_default(fsph_params *out);
+
+/* ---- context (Initialize / Finalize) ---- */
+int fsph_create(const fsph_params *params, fsph_ctx **out);
+int fsph_destroy(fsph_ctx *ctx);
+int fsph_set_params(fsph_ctx *ctx, const fsph_params *params);
+int fsph_get_params(const fsph_ctx *ctx, fsph_params *out);
+int fsph_num_particles(const fsph_ctx *ctx);
+
+/* ---- particle data (Set / SetArrayVBO) ---- */
+/* Replace all particles: pos4/vel4 hold n float4 in particle order (vel4 may
+ * be NULL for zero velocity).  Like rxParticleSystemBase::Set (rx_ps.cpp:30-59)
+ * this resets the particle count to n (n <= max_particles). */
+int fsph_set_particles(fsph_ctx *ctx, const float *pos4, const float *vel4, int n, int where);
+/* Overwrite `count` particles from index `start` of one array
+ * (SetArrayVBO, rx_ps.h:260-262).  FSPH_POSITION, FSPH_VELOCITY, FSPH_ATTRIBUTE. */
+int fsph_set_array(fsph_ctx *ctx, int type, const void *data, int start, int count, int where);
+
+/* ---- step (Update) ---- */
+/* Advance one step of dt.  stats may be NULL (then nothing synchronises);
+ * otherwise the call waits for the step and fills stats.  Returns
+ * FSPH_INVALID_ARG when there are no particles (the reference's Update
+ * returns false for N = 0, rx_sph_pbd_gpu.cpp:818). */
+int fsph_step(fsph_ctx *ctx, float dt, void *stream, fsph_step_stats *stats);
+/* Stats of the last step (synchronises). */
+int fsph_last_stats(fsph_ctx *ctx, fsph_step_stats *stats);
+
+/* ---- access (GetArrayVBO / GetParticleDevice) ---- */
+/* Copy one array out in particle order (index = the order given to
+ * fsph_set_particles).  dst holds n float4 / n floats; where says whether dst
+ * is host (synchronises) or device memory. */
+int fsph_get_array(fsph_ctx *ctx, int type, void *dst, int where, void *stream);
+/* Borrowed device pointer to an internal array, in DEVICE order (see
+ * FSPH_SORTED_ID for the device slot -> particle index map); valid until the
+ * next fsph_step / fsph_set_particles.  NULL on error. */
+const void *fsph_device_ptr(fsph_ctx *ctx, int type);
+/* Synchronise the context's stream. */
+int fsph_sync(fsph_ctx *ctx);
+
+/* ---- neighbour sets (GetNeights / SetParticlesToCell, rx_sph.h:1196) ---- */
+/* Neighbour sets of the current positions under the reference criterion
+ * fl32(|x_i - x_j|^2 evaluated in double) <= fl32(h*h), self included
+ * (rx_nnsearch.h:487-515).  CSR in particle order: offsets[n+1]; indices
+ * (particle indices, ascending within each row) holds at most cap entries;
+ * *total receives the number of entries.  Synchronises. */
+int fsph_neighbors(fsph_ctx *ctx, int *offsets, int *indices, long long cap, long long *total);
+
+/* ---- single passes, for parity checks against the CPU path ---- */
+/* PBF lambda pass on the given positions (rxPBDSPH::calScalingFactor,
+ * rx_sph_pbd.cpp:699-914): density and scaling factor per particle. Host arrays. */
+int fsph_pbf_eval_lambda(fsph_ctx *ctx, const float *pos4, int n, float *dens, float *lambda);
+/* PBF position-correction pass (rxPBDSPH::calPositionCorrection,
+ * rx_sph_pbd.cpp:925-1026) for given positions and lambdas.  Host arrays. */
+int fsph_pbf_eval_correction(fsph_ctx *ctx, const float *pos4, const float *lambda, int n,
+                             float dt, float *dp4);
+/* WCSPH density + force passes (rxSPH::calDensity / calForce,
+ * rx_sph_cpu.cpp:495-656).  Host arrays; acc4 receives the acceleration. */
+int fsph_sph_eval_forces(fsph_ctx *ctx, const float *pos4, const float *vel4, int n,
+                         float *dens, float *pres, float *acc4);
+
+/* ---- measurement ---- */
+typedef enum fsph_pass {
+    FSPH_PASS_LAMBDA = 0,      /* one lambda pass (density + constraint + error reduction) */
+    FSPH_PASS_CORRECTION = 1,  /* one position-correction pass */
+    FSPH_PASS_GRID = 2         /* one grid build (hash, scan, scatter, cell sort, reorder) */
+} fsph_pass;
+/* Time `reps` back-to-back launches of one pass of the current PBF state
+ * with CUDA events on the context's stream; *avg_ms receives the mean time
+ * of one launch.  The state is advanced as the passes would advance it
+ * (corrections are applied), so call it after the steps to be kept.
+ * No counterpart in the reference (its timing was the GUI's RXTIMER splits,
+ * rx_sph.h:40-58). */
+int fsph_time_pass(fsph_ctx *ctx, int pass, int reps, float *avg_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FSPH_H */

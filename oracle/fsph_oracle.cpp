@@ -1,0 +1,647 @@
+/*
+ * fsph_oracle.cpp -- CPU ORACLE of the fluid step.  TEST INFRASTRUCTURE ONLY:
+ * loaded by tests/, by __graft_entry__.smoke() as the checker, and by the
+ * CPU-baseline leg of bench.py.  The product (libfsph.so) never links,
+ * loads or calls it.
+ *
+ * A restatement of the reference's CPU fluid path, templated on the storage
+ * precision T:
+ *   T = float  : the reference's own arithmetic -- float particle arrays and
+ *                float accumulators (RXREAL), per-pair geometry and kernel
+ *                values in double (the reference's Vec3 / rx_kernel.h).
+ *   T = double : the same algorithm entirely in double (the FP64 oracle used
+ *                to report the error of every FP32 result).
+ *
+ * Followed, function by function:
+ *   kernels        rx_kernel.h:29-80 (poly6), 133-203 (spiky gradient), 236-324 (visc Laplacian)
+ *   rest density   rx_sph_pbd.cpp:1035-1049 (calRestDensity)
+ *   derivation     rx_sph_pbd.cpp:102-201 (rxPBDSPH::Initialize), rx_sph_cpu.cpp:92-166
+ *   neighbours     rx_nnsearch.h:454-515 (GetNN / getNeighborsInCell): the set
+ *                  {j : fl32(|xi-xj|^2 in double) <= fl32(h*h)}, self included
+ *   walls          rx_sph_solid.cpp:44-108 (AABB_point_dist), 244-262 (GetDistanceR),
+ *                  rx_sph_pbd.cpp:1374-1398 (calCollisionSolid: position only)
+ *   WCSPH          rx_sph_cpu.cpp:323-380 (Update), 495-552 (calDensity),
+ *                  558-656 (calForce), 1040-1077 (integrate)
+ *   PBF            rx_sph_pbd.cpp:377-484 (Update), 599-646 (calDensity),
+ *                  651-689 (calForceExtAndVisc), 699-914 (calScalingFactor, with the
+ *                  k = i self term), 925-1026 (calPositionCorrection, s_corr with dt^2),
+ *                  1409-1446 (integrate)
+ *   XSPH           rx_pbdsph_kernel.cu:1090-1162 (xsphVisocosity; GPU-only in the reference)
+ *   vorticity      absent from the reference (only a flag, rx_ps.h:161); restated from
+ *                  Macklin & Mueller, "Position Based Fluids", SIGGRAPH 2013, eq. 15-16,
+ *                  which rx_sph.h:1281 cites.
+ *
+ * Deliberate, documented choices where the reference is ambiguous:
+ *   - neighbour lists are kept in ascending particle index (the reference's
+ *     within-cell order depends on an unstable std::sort, rx_nnsearch.h:257);
+ *   - the convergence error may be the one-sided GPU form or the two-sided
+ *     CPU form (fsph_params.error_mode);
+ *   - the iteration count reported is the number of constraint iterations
+ *     executed (the reference's g_iIterations is one less when the loop ends
+ *     by its early break, rx_sph_pbd.cpp:456-459).
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/fsph.h"
+
+namespace {
+
+const double kPi = 3.14159265358979323846;
+
+struct V3 {
+    double x, y, z;
+};
+inline V3 v3(double a, double b, double c) { return V3{a, b, c}; }
+inline V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V3 operator*(double s, V3 a) { return v3(s * a.x, s * a.y, s * a.z); }
+inline V3 operator/(V3 a, double s) { return v3(a.x / s, a.y / s, a.z / s); }
+inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+
+/* Kernel coefficients and values (rx_kernel.h): the coefficient is computed
+ * in double from the float radius, as the reference's Initialize does. */
+struct Kern {
+    double h, aw, ag, al;
+    explicit Kern(double h_) : h(h_) {
+        aw = 315.0 / (64.0 * kPi * std::pow(h, 9.0));
+        ag = -45.0 / (kPi * std::pow(h, 6.0));
+        al = 45.0 / (kPi * std::pow(h, 6.0));
+    }
+    double W(double r) const {
+        if (r >= 0.0 && r <= h) { double q = h * h - r * r; return aw * q * q * q; }
+        return 0.0;
+    }
+    /* scalar s with grad W = s * rij */
+    double G(double r) const {
+        if (r > 0.0 && r <= h) { double q = h - r; return ag * q * q / r; }
+        return 0.0;
+    }
+    double L(double r) const {
+        if (r > 0.0 && r <= h) return al * (h - r);
+        return 0.0;
+    }
+};
+
+template <class T>
+inline void acc_add(T &a, double term) { a = (T)((double)a + term); }
+
+template <class T>
+struct Solver {
+    fsph_params P;
+    int n = 0;
+    std::vector<T> pos, vel, ppos, pvel, frc, dens, pres, lam, dp, vort;
+    std::vector<int> noff, nidx; /* neighbour CSR */
+    Kern K;
+    int last_iters = 0;
+    double last_err1 = 0, last_err2 = 0, last_errmax = 0;
+
+    explicit Solver(const fsph_params &p) : P(p), K(p.h) {}
+
+    void resize(int n_) {
+        n = n_;
+        pos.assign(4 * (size_t)n, 0); vel.assign(4 * (size_t)n, 0);
+        ppos.assign(4 * (size_t)n, 0); pvel.assign(4 * (size_t)n, 0);
+        frc.assign(4 * (size_t)n, 0); dp.assign(4 * (size_t)n, 0); vort.assign(4 * (size_t)n, 0);
+        dens.assign(n, 0); pres.assign(n, 0); lam.assign(n, 0);
+    }
+
+    V3 at(const std::vector<T> &a, int i) const {
+        return v3((double)a[4 * (size_t)i], (double)a[4 * (size_t)i + 1], (double)a[4 * (size_t)i + 2]);
+    }
+
+    /* Neighbour sets on positions p (rx_nnsearch.h:454-515): every j with
+     * fl(|xi - xj|^2) <= fl(h*h), the squared distance evaluated in double and
+     * rounded to T.  Binning uses cells of width >= h, so the 27 cells around
+     * a particle hold every candidate; lists are ascending in j. */
+    void neighbors(const std::vector<T> &p) {
+        const T hT = (T)P.h;
+        const T h2 = hT * hT;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) {
+                double v = (double)p[4 * (size_t)i + k];
+                lo[k] = std::min(lo[k], v); hi[k] = std::max(hi[k], v);
+            }
+        const double cw = (double)P.h * 1.0001;
+        int g[3];
+        for (int k = 0; k < 3; ++k) g[k] = std::max(1, (int)std::floor((hi[k] - lo[k]) / cw) + 1);
+        const size_t C = (size_t)g[0] * g[1] * g[2];
+        std::vector<int> cnt(C + 1, 0), cellOf(n), order(n);
+        auto cell3 = [&](int i, int c[3]) {
+            for (int k = 0; k < 3; ++k) {
+                int v = (int)std::floor(((double)p[4 * (size_t)i + k] - lo[k]) / cw);
+                c[k] = std::min(std::max(v, 0), g[k] - 1);
+            }
+        };
+        for (int i = 0; i < n; ++i) {
+            int c[3]; cell3(i, c);
+            cellOf[i] = (int)(((size_t)c[2] * g[1] + c[1]) * g[0] + c[0]);
+            cnt[cellOf[i] + 1]++;
+        }
+        for (size_t c = 0; c < C; ++c) cnt[c + 1] += cnt[c];
+        {
+            std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+            for (int i = 0; i < n; ++i) order[fill[cellOf[i]]++] = i;
+        }
+        std::vector<std::vector<int>> lists(n);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int i = 0; i < n; ++i) {
+            int c[3]; cell3(i, c);
+            V3 xi = at(p, i);
+            std::vector<int> &L = lists[i];
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        int z = c[2] + dz, y = c[1] + dy, x = c[0] + dx;
+                        if (x < 0 || y < 0 || z < 0 || x >= g[0] || y >= g[1] || z >= g[2]) continue;
+                        size_t cc = ((size_t)z * g[1] + y) * g[0] + x;
+                        for (int s = cnt[cc]; s < cnt[cc + 1]; ++s) {
+                            int j = order[s];
+                            V3 d = xi - at(p, j);
+                            T d2 = (T)dot(d, d);
+                            if (d2 <= h2) L.push_back(j);
+                        }
+                    }
+            std::sort(L.begin(), L.end());
+        }
+        noff.assign(n + 1, 0);
+        for (int i = 0; i < n; ++i) noff[i + 1] = noff[i] + (int)lists[i].size();
+        nidx.resize(noff[n]);
+        for (int i = 0; i < n; ++i) std::copy(lists[i].begin(), lists[i].end(), nidx.begin() + noff[i]);
+    }
+
+    /* Box-wall projection keeping the particle radius from every face
+     * (rxSolidBox::GetDistanceR -> AABB_point_dist with sgn = 1, contact =
+     * pos + n |d|).  Velocity is left unchanged: the reflection is commented
+     * out in the reference (rx_sph_pbd.cpp:1392). */
+    V3 wall(V3 pos) const {
+        const double r = (double)(T)P.particle_radius;
+        double cen[3], sl[3];
+        for (int k = 0; k < 3; ++k) {
+            cen[k] = 0.5 * (P.box_max[k] + P.box_min[k]);
+            sl[k] = 0.5 * (P.box_max[k] - P.box_min[k]);
+        }
+        double sp[3] = {pos.x - cen[0], pos.y - cen[1], pos.z - cen[2]};
+        double d0[6];
+        int out = 0, last = -1;
+        for (int k = 0; k < 3; ++k) {
+            d0[2 * k] = (sp[k] - r) - (-sl[k]);
+            if (d0[2 * k] < 0.0) { out |= 1 << (2 * k); last = 2 * k; }
+            d0[2 * k + 1] = sl[k] - (sp[k] + r);
+            if (d0[2 * k + 1] < 0.0) { out |= 1 << (2 * k + 1); last = 2 * k + 1; }
+        }
+        if (!out) return pos; /* inside: contact only when d == 0, which is pos itself */
+        int c = __builtin_popcount(out);
+        double p[3] = {pos.x, pos.y, pos.z};
+        if (c == 1) {
+            int ax = last / 2;
+            double nrm = (last % 2 == 0) ? 1.0 : -1.0; /* inward face normal */
+            p[ax] = p[ax] + nrm * std::fabs(d0[last]);
+            return v3(p[0], p[1], p[2]);
+        }
+        double x[3] = {0, 0, 0};
+        for (int k = 0; k < 3; ++k) {
+            if (out & (1 << (2 * k))) x[k] = d0[2 * k];
+            else if (out & (1 << (2 * k + 1))) x[k] = -d0[2 * k + 1];
+        }
+        double nx = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+        double u[3] = {x[0] / nx, x[1] / nx, x[2] / nx};
+        for (int k = 0; k < 3; ++k) p[k] = p[k] + (-u[k]) * std::fabs(-nx);
+        return v3(p[0], p[1], p[2]);
+    }
+
+    /* v += dt a; x += dt v; walls (rxPBDSPH::integrate / rxSPH::integrate). */
+    void integrate(const std::vector<T> &x0, const std::vector<T> &v0, const std::vector<T> &a0,
+                   std::vector<T> &x1, std::vector<T> &v1, T dt) {
+        for (int i = 0; i < n; ++i) {
+            V3 x = at(x0, i), v = at(v0, i), a = at(a0, i);
+            v = v + (double)dt * a;
+            x = x + (double)dt * v;
+            x = wall(x);
+            size_t b = 4 * (size_t)i;
+            x1[b] = (T)x.x; x1[b + 1] = (T)x.y; x1[b + 2] = (T)x.z;
+            v1[b] = (T)v.x; v1[b + 1] = (T)v.y; v1[b + 2] = (T)v.z;
+        }
+    }
+
+    /* rho_i = sum_j m W(r_ij), self included. */
+    void density(const std::vector<T> &p, std::vector<T> &rho) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            V3 xi = at(p, i);
+            T acc = 0;
+            for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                V3 d = xi - at(p, nidx[s]);
+                T r = (T)std::sqrt(dot(d, d));
+                acc_add(acc, (double)(T)P.mass * K.W((double)r));
+            }
+            rho[i] = acc;
+        }
+    }
+
+    /* ---------------- PBF ---------------- */
+    /* a_i = mu sum_{j != i} m (v_j - v_i) / rho_i lapW(r) + g (rx_sph_pbd.cpp:651-689). */
+    void ext_visc(const std::vector<T> &p, const std::vector<T> &v, const std::vector<T> &rho,
+                  std::vector<T> &f) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            V3 xi = at(p, i), vi = at(v, i);
+            V3 fev = v3(0, 0, 0);
+            for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                int j = nidx[s];
+                if (j == i) continue;
+                V3 d = xi - at(p, j), vji = at(v, j) - vi;
+                T r = (T)std::sqrt(dot(d, d));
+                fev = fev + ((double)(T)P.mass * K.L((double)r)) * (vji / (double)rho[i]);
+            }
+            V3 force = (double)(T)P.viscosity * fev;
+            force = force + v3((double)(T)P.gravity[0], (double)(T)P.gravity[1], (double)(T)P.gravity[2]);
+            size_t b = 4 * (size_t)i;
+            acc_add(f[b], force.x); acc_add(f[b + 1], force.y); acc_add(f[b + 2], force.z);
+        }
+    }
+
+    /* lambda_i = -C_i / (sum_k |grad_k C_i|^2 + eps), C_i = rho_i / rho0 - 1,
+     * with the k = i term |sum_j grad W_ij / rho0|^2 (rx_sph_pbd.cpp:699-914). */
+    void lambda_pass(const std::vector<T> &p) {
+        const double r0 = (double)(T)P.rest_dens;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            V3 xi = at(p, i);
+            T rho = 0;
+            V3 gsum = v3(0, 0, 0);
+            T sd = 0;
+            for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                int j = nidx[s];
+                V3 d = xi - at(p, j);
+                T r = (T)std::sqrt(dot(d, d));
+                acc_add(rho, (double)(T)P.mass * K.W((double)r));
+                V3 g = (K.G((double)r) * d) / r0;
+                gsum = gsum + g;
+                if (j != i) acc_add(sd, dot(g, g));
+            }
+            acc_add(sd, dot(gsum, gsum));
+            T C = (T)((double)rho / r0) - (T)1;
+            if (P.clamp_constraint && C < (T)0) C = (T)0;
+            dens[i] = rho;
+            lam[i] = (T)(-(double)C / ((double)sd + (double)(T)P.epsilon));
+        }
+    }
+
+    /* dp_i = sum_j (lambda_i + lambda_j + s_corr) grad W_ij / rho0,
+     * s_corr = -k (W(r)/W(q h))^n dt^2 (rx_sph_pbd.cpp:925-1026). */
+    void correction_pass(const std::vector<T> &p, T dt) {
+        const double r0 = (double)(T)P.rest_dens;
+        const T dq = (T)P.ap_q * (T)P.h;
+        const T wq = (T)K.W((double)dq);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            V3 xi = at(p, i);
+            V3 acc = v3(0, 0, 0);
+            for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                int j = nidx[s];
+                V3 d = xi - at(p, j);
+                T r = (T)std::sqrt(dot(d, d));
+                if ((double)r > (double)(T)P.h) continue;
+                T sc = 0;
+                if (P.use_ap) {
+                    T ww = (T)(K.W((double)r) / (double)wq);
+                    sc = (T)(-(double)(T)P.ap_k * std::pow((double)ww, (double)(T)P.ap_n)) * dt * dt;
+                }
+                T coef = lam[i] + lam[j] + sc;
+                acc = acc + ((double)coef * K.G((double)r) / r0) * d;
+            }
+            size_t b = 4 * (size_t)i;
+            dp[b] = (T)acc.x; dp[b + 1] = (T)acc.y; dp[b + 2] = (T)acc.z; dp[b + 3] = 0;
+        }
+    }
+
+    void errors(double &e1, double &e2, double &emax) const {
+        const double r0 = (double)(T)P.rest_dens;
+        double s1 = 0, s2 = 0, m = 0;
+        for (int i = 0; i < n; ++i) {
+            double e = ((double)dens[i] - r0) / r0;
+            s1 += e > 0 ? e : 0.0;
+            s2 += std::fabs(e);
+            m = std::max(m, std::fabs(e));
+        }
+        e1 = n ? s1 / n : 0.0; e2 = n ? s2 / n : 0.0; emax = m;
+    }
+
+    /* One PBF step (rxPBDSPH::Update, rx_sph_pbd.cpp:377-484) plus the XSPH
+     * and vorticity extensions.  fixed_iters > 0 runs exactly that many
+     * iterations instead of the tolerance loop.  Returns iterations executed. */
+    int pbf_step(T dt, int fixed_iters) {
+        std::fill(frc.begin(), frc.end(), (T)0);
+        neighbors(pos);
+        density(pos, dens);
+        ext_visc(pos, vel, dens, frc);
+        integrate(pos, vel, frc, ppos, pvel, dt);
+
+        int it = 0;
+        double e1 = 1, e2 = 1, em = 1;
+        for (;;) {
+            neighbors(ppos);
+            lambda_pass(ppos);
+            correction_pass(ppos, dt);
+            for (size_t k = 0; k < ppos.size(); ++k) { ppos[k] += dp[k]; pvel[k] = 0; frc[k] = 0; }
+            integrate(ppos, pvel, frc, ppos, pvel, dt);
+            errors(e1, e2, em);
+            ++it;
+            double err = (P.error_mode == FSPH_ERR_TWO_SIDED) ? e2 : e1;
+            if (fixed_iters > 0) {
+                if (it >= fixed_iters) break;
+                continue;
+            }
+            /* loop test of rx_sph_pbd.cpp:425,456 restated on the executed count */
+            if (it >= P.max_iter) break;
+            if (err <= (double)P.eta && it >= std::max(P.min_iter, 1)) break;
+        }
+        last_iters = it; last_err1 = e1; last_err2 = e2; last_errmax = em;
+
+        /* v = (x* - x) / dt, x = x* (rx_sph_pbd.cpp:464-471) */
+        for (size_t k = 0; k < pos.size(); ++k) {
+            vel[k] = (ppos[k] - pos[k]) / dt;
+            pos[k] = ppos[k];
+        }
+        if (P.xsph_c != 0.0f || P.vort_eps != 0.0f) finalize_extensions(dt);
+        return it;
+    }
+
+    /* XSPH (rx_pbdsph_kernel.cu:1090-1162) and vorticity confinement
+     * (Macklin & Mueller 2013, eq. 15-16), both evaluated on the velocities
+     * v = (x* - x)/dt and the densities of the last lambda pass:
+     *   w_i   = sum_j (v_j - v_i) x grad_j W(x_i - x_j),  grad_j = -grad_i
+     *   eta_i = sum_j (m / rho_j) (|w_j| - |w_i|) grad_i W(x_i - x_j)
+     *   N_i   = eta_i / |eta_i|,  f_i = eps (N_i x w_i)
+     *   v_i  <- v_i + c sum_j (m / rho_j)(v_j - v_i) W(r_ij) + dt f_i        */
+    void finalize_extensions(T dt) {
+        neighbors(pos);
+        const double m = (double)(T)P.mass;
+        std::vector<T> vnew(vel);
+        std::vector<double> wmag(n, 0.0);
+        std::vector<V3> w(n);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            V3 xi = at(pos, i), vi = at(vel, i);
+            V3 om = v3(0, 0, 0), xs = v3(0, 0, 0);
+            for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                int j = nidx[s];
+                if (j == i) continue;
+                V3 d = xi - at(pos, j);
+                T r = (T)std::sqrt(dot(d, d));
+                V3 vij = at(vel, j) - vi;
+                V3 gi = K.G((double)r) * d;
+                om = om + cross(vij, -1.0 * gi);
+                xs = xs + (m / (double)dens[j] * K.W((double)r)) * vij;
+            }
+            w[i] = om;
+            wmag[i] = std::sqrt(dot(om, om));
+            size_t b = 4 * (size_t)i;
+            vnew[b] = (T)(vi.x + (double)(T)P.xsph_c * xs.x);
+            vnew[b + 1] = (T)(vi.y + (double)(T)P.xsph_c * xs.y);
+            vnew[b + 2] = (T)(vi.z + (double)(T)P.xsph_c * xs.z);
+            vort[b] = (T)om.x; vort[b + 1] = (T)om.y; vort[b + 2] = (T)om.z; vort[b + 3] = 0;
+        }
+        if (P.vort_eps != 0.0f) {
+#pragma omp parallel for schedule(static)
+            for (int i = 0; i < n; ++i) {
+                V3 xi = at(pos, i);
+                V3 eta = v3(0, 0, 0);
+                for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                    int j = nidx[s];
+                    if (j == i) continue;
+                    V3 d = xi - at(pos, j);
+                    T r = (T)std::sqrt(dot(d, d));
+                    eta = eta + ((m / (double)dens[j]) * (wmag[j] - wmag[i]) * K.G((double)r)) * d;
+                }
+                double en = std::sqrt(dot(eta, eta));
+                if (en > 1e-30) {
+                    V3 N = eta / en;
+                    V3 f = (double)(T)P.vort_eps * cross(N, w[i]);
+                    size_t b = 4 * (size_t)i;
+                    vnew[b] = (T)((double)vnew[b] + (double)dt * f.x);
+                    vnew[b + 1] = (T)((double)vnew[b + 1] + (double)dt * f.y);
+                    vnew[b + 2] = (T)((double)vnew[b + 2] + (double)dt * f.z);
+                }
+            }
+        }
+        vel.swap(vnew);
+    }
+
+    /* ---------------- WCSPH ---------------- */
+    /* p = k (rho - rho0); a_i = -sum m (p_i/rho_i^2 + p_j/rho_j^2) gradW
+     *   + mu sum m (v_j - v_i)/rho_j lapW + g (rx_sph_cpu.cpp:558-656). */
+    void sph_forces(const std::vector<T> &p, const std::vector<T> &v) {
+        const T r0 = (T)P.rest_dens;
+        for (int i = 0; i < n; ++i) pres[i] = (T)P.gas_k * (dens[i] - r0);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            V3 xi = at(p, i), vi = at(v, i);
+            T prsi = pres[i] / (dens[i] * dens[i]);
+            V3 fp = v3(0, 0, 0), fev = v3(0, 0, 0);
+            for (int s = noff[i]; s < noff[i + 1]; ++s) {
+                int j = nidx[s];
+                if (j == i) continue;
+                V3 d = xi - at(p, j), vji = at(v, j) - vi;
+                T r = (T)std::sqrt(dot(d, d));
+                T prsj = pres[j] / (dens[j] * dens[j]);
+                fp = fp + ((double)(T)P.mass * (double)(prsi + prsj) * K.G((double)r)) * d;
+                fev = fev + ((double)(T)P.mass * K.L((double)r)) * (vji / (double)dens[j]);
+            }
+            V3 force = (-1.0 * fp) + (double)(T)P.viscosity * fev +
+                       v3((double)(T)P.gravity[0], (double)(T)P.gravity[1], (double)(T)P.gravity[2]);
+            size_t b = 4 * (size_t)i;
+            frc[b] = (T)force.x; frc[b + 1] = (T)force.y; frc[b + 2] = (T)force.z; frc[b + 3] = 0;
+        }
+    }
+
+    void sph_step(T dt) {
+        neighbors(pos);
+        density(pos, dens);
+        sph_forces(pos, vel);
+        integrate(pos, vel, frc, pos, vel, dt);
+    }
+};
+
+template <class T>
+struct Handle {
+    Solver<T> s;
+    explicit Handle(const fsph_params &p) : s(p) {}
+};
+
+template <class T>
+void load4(std::vector<T> &dst, const float *src, int n) {
+    for (size_t k = 0; k < 4 * (size_t)n; ++k) dst[k] = src ? (T)src[k] : (T)0;
+}
+template <class T>
+void store(float *dst, const std::vector<T> &src) {
+    for (size_t k = 0; k < src.size(); ++k) dst[k] = (float)src[k];
+}
+
+}  // namespace
+
+extern "C" {
+
+/* precision: 0 = float (reference arithmetic), 1 = double (FP64 oracle).
+ * The handle is a tagged pointer to a Solver<float> or Solver<double>. */
+struct fsph_orc {
+    int prec;
+    void *s;
+};
+
+void fsph_orc_threads(int t) {
+#ifdef _OPENMP
+    omp_set_num_threads(t > 0 ? t : 1);
+#else
+    (void)t;
+#endif
+}
+
+fsph_orc *fsph_orc_create(const fsph_params *p, int prec, int n) {
+    fsph_orc *o = new fsph_orc{prec, nullptr};
+    if (prec) { auto *s = new Solver<double>(*p); s->resize(n); o->s = s; }
+    else { auto *s = new Solver<float>(*p); s->resize(n); o->s = s; }
+    return o;
+}
+
+void fsph_orc_destroy(fsph_orc *o) {
+    if (!o) return;
+    if (o->prec) delete (Solver<double> *)o->s; else delete (Solver<float> *)o->s;
+    delete o;
+}
+
+#define ORC_DISPATCH(o, expr)                                   \
+    do {                                                        \
+        if ((o)->prec) { auto *S = (Solver<double> *)(o)->s; expr; } \
+        else { auto *S = (Solver<float> *)(o)->s; expr; }        \
+    } while (0)
+
+void fsph_orc_set(fsph_orc *o, const float *pos4, const float *vel4) {
+    ORC_DISPATCH(o, { load4(S->pos, pos4, S->n); load4(S->vel, vel4, S->n); });
+}
+
+/* which: 0 pos, 1 vel, 2 dens, 3 lambda, 4 dp, 5 predicted pos, 6 force, 7 pressure, 8 vorticity */
+void fsph_orc_get(fsph_orc *o, int which, float *out) {
+    ORC_DISPATCH(o, {
+        switch (which) {
+        case 0: store(out, S->pos); break;
+        case 1: store(out, S->vel); break;
+        case 2: store(out, S->dens); break;
+        case 3: store(out, S->lam); break;
+        case 4: store(out, S->dp); break;
+        case 5: store(out, S->ppos); break;
+        case 6: store(out, S->frc); break;
+        case 7: store(out, S->pres); break;
+        case 8: store(out, S->vort); break;
+        }
+    });
+}
+
+/* Returns iterations; errs[0..2] = one-sided, two-sided, max error. */
+int fsph_orc_pbf_step(fsph_orc *o, float dt, int fixed_iters, double *errs) {
+    int it = 0;
+    ORC_DISPATCH(o, {
+        it = S->pbf_step(dt, fixed_iters);
+        if (errs) { errs[0] = S->last_err1; errs[1] = S->last_err2; errs[2] = S->last_errmax; }
+    });
+    return it;
+}
+
+void fsph_orc_sph_step(fsph_orc *o, float dt) { ORC_DISPATCH(o, S->sph_step(dt)); }
+
+/* Neighbour CSR of the given positions (ascending indices). */
+long long fsph_orc_neighbors(fsph_orc *o, const float *pos4, int *offsets, int *idx, long long cap) {
+    long long total = 0;
+    ORC_DISPATCH(o, {
+        load4(S->ppos, pos4, S->n);
+        S->neighbors(S->ppos);
+        for (int i = 0; i <= S->n; ++i) offsets[i] = S->noff[i];
+        total = (long long)S->nidx.size();
+        for (long long k = 0; k < total && k < cap; ++k) idx[k] = S->nidx[k];
+    });
+    return total;
+}
+
+void fsph_orc_pbf_lambda(fsph_orc *o, const float *pos4, float *dens, float *lam) {
+    ORC_DISPATCH(o, {
+        load4(S->ppos, pos4, S->n);
+        S->neighbors(S->ppos);
+        S->lambda_pass(S->ppos);
+        store(dens, S->dens); store(lam, S->lam);
+    });
+}
+
+void fsph_orc_pbf_correction(fsph_orc *o, const float *pos4, const float *lam, float dt, float *dp4) {
+    ORC_DISPATCH(o, {
+        load4(S->ppos, pos4, S->n);
+        for (int i = 0; i < S->n; ++i) S->lam[i] = lam[i];
+        S->neighbors(S->ppos);
+        S->correction_pass(S->ppos, dt);
+        store(dp4, S->dp);
+    });
+}
+
+void fsph_orc_sph_forces(fsph_orc *o, const float *pos4, const float *vel4, float *dens, float *pres, float *acc4) {
+    ORC_DISPATCH(o, {
+        load4(S->pos, pos4, S->n); load4(S->vel, vel4, S->n);
+        S->neighbors(S->pos);
+        S->density(S->pos, S->dens);
+        S->sph_forces(S->pos, S->vel);
+        store(dens, S->dens); store(pres, S->pres); store(acc4, S->frc);
+    });
+}
+
+/* Predict (density + ext/visc + integrate) only, the PBF pre-pass. */
+void fsph_orc_pbf_predict(fsph_orc *o, float dt, float *dens, float *frc4, float *ppos4, float *pvel4) {
+    ORC_DISPATCH(o, {
+        std::fill(S->frc.begin(), S->frc.end(), 0);
+        S->neighbors(S->pos);
+        S->density(S->pos, S->dens);
+        S->ext_visc(S->pos, S->vel, S->dens, S->frc);
+        S->integrate(S->pos, S->vel, S->frc, S->ppos, S->pvel, dt);
+        store(dens, S->dens); store(frc4, S->frc); store(ppos4, S->ppos); store(pvel4, S->pvel);
+    });
+}
+
+double fsph_orc_kernel(int which, double r, double h) {
+    Kern K(h);
+    switch (which) {
+    case 0: return K.W(r);
+    case 1: return K.G(r);
+    case 2: return K.L(r);
+    }
+    return 0.0;
+}
+
+/* Rest density by calRestDensity (rx_sph_pbd.cpp:1035-1049): poly6 sum over a
+ * cubic lattice of spacing l around the origin, in float accumulation. */
+double fsph_orc_lattice_density(double h, double mass, double spacing) {
+    Kern K((float)h);
+    float r0 = 0.0f;
+    const float l = (float)spacing;
+    int nn = (int)std::ceil((float)h / l) + 1;
+    for (int x = -nn; x <= nn; ++x)
+        for (int y = -nn; y <= nn; ++y)
+            for (int z = -nn; z <= nn; ++z) {
+                double r = std::sqrt((double)(x * l) * (x * l) + (double)(y * l) * (y * l) + (double)(z * l) * (z * l));
+                r0 = (float)((double)r0 + (double)(float)mass * K.W(r));
+            }
+    return r0;
+}
+
+void fsph_orc_wall(const fsph_params *p, const double *pos, double *out) {
+    Solver<double> s(*p);
+    V3 q = s.wall(v3(pos[0], pos[1], pos[2]));
+    out[0] = q.x; out[1] = q.y; out[2] = q.z;
+}
+
+}  // extern "C"

@@ -146,12 +146,12 @@ def _block_origin(box_min, h):
 def wcsph_dam_break(n_side: int = 32, h: float = H_DEFAULT, seed: int = 1) -> Scene:
     """32^3 WCSPH dam break.  The stated [0,1]x[0,0.6]x[0,0.4] box cannot hold a
     32^3 block at spacing h/2 (0.73 m per side), so the box is enlarged to
-    [0,2]x[0,1.2]x[0,1.0].  mu = 3.5 / rho0: the reference multiplies an
+    [0,2]x[0,1]x[0,1].  mu = 3.5 / rho0: the reference multiplies an
     acceleration by mu (rx_sph_cpu.cpp:626-633), and mu = 3.5 is unstable at dt = 1e-3."""
     s = 0.5 * h
     scale = max(1.0, n_side / 32.0)
     box_min = [0.0, 0.0, 0.0]
-    box_max = [2.0 * scale, 1.2 * scale, 1.0 * scale]
+    box_max = [2.0 * scale, 1.0 * scale, 1.0 * scale]
     pos = lattice_block(_block_origin(box_min, h), (n_side, n_side, n_side), s, 0.01 * h, seed, 0)
     p = pbf_params(h, box_min, box_max, pos.shape[0])
     p.solver = abi.SOLVER_WCSPH

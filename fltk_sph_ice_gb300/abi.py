@@ -125,7 +125,7 @@ EXPORTS = [
     "fsph_params_default", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params",
     "fsph_num_particles", "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats",
     "fsph_get_array", "fsph_device_ptr", "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda",
-    "fsph_pbf_eval_correction", "fsph_sph_eval_forces", "fsph_time_pass",
+    "fsph_pbf_eval_correction", "fsph_sph_eval_forces", "fsph_time_pass", "fsph_pbf_eval_lambda_noalloc",
 ]
 
 # fsph_pass

@@ -1018,3 +1018,14 @@ int fsph_sph_eval_forces(fsph_ctx *c, const float *pos4, const float *vel4, int 
 }
 
 }  // extern "C"
+
+/* Parameter builders shared with the allocation-free entry point (fsph_noalloc.cu). */
+namespace fsph {
+DevParams dev_params_for(const fsph_params &p, int n, float dt) { return make_dev(p, n, dt); }
+unsigned long long grid_cells_for(const fsph_params &p) {
+    double cw, org[3];
+    int g[3];
+    grid_geometry(p, cw, org, g);
+    return (unsigned long long)g[0] * (unsigned long long)g[1] * (unsigned long long)g[2];
+}
+}  // namespace fsph

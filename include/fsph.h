@@ -221,6 +221,33 @@ int fsph_pbf_eval_correction(fsph_ctx *ctx, const float *pos4, const float *lamb
 int fsph_sph_eval_forces(fsph_ctx *ctx, const float *pos4, const float *vel4, int n,
                          float *dens, float *pres, float *acc4);
 
+/* ---- allocation-free variant ---- */
+/* Largest inputs of fsph_pbf_eval_lambda_noalloc: its scratch is a fixed
+ * device array of about 10.3 MB inside the library. */
+#define FSPH_NOALLOC_MAX_PARTICLES 65536
+#define FSPH_NOALLOC_MAX_CELLS (1 << 20)
+/* The lambda pass of fsph_pbf_eval_lambda (density and scaling factor of n
+ * particles at the given positions) for callers that cannot allocate device
+ * memory: a host application that hands the whole GPU to its own memory
+ * pool, or a real-time loop where an allocation's latency or failure is not
+ * acceptable.  No counterpart in the reference.
+ *   - pos4, dens and lambda are DEVICE pointers owned by the caller
+ *     (n float4 in, n floats out each), in particle order.  No context is used.
+ *   - It allocates nothing: no cudaMalloc / cudaFree / allocating library call.
+ *     Its working memory (grid tables, sorted copies) is one file-scope
+ *     __device__ array that every GPU loading the library holds until exit.
+ *   - n <= FSPH_NOALLOC_MAX_PARTICLES and the wall box padded by one cell of
+ *     width h (1 + cell_skin) must span <= FSPH_NOALLOC_MAX_CELLS cells;
+ *     larger inputs return FSPH_INVALID_ARG without launching anything.
+ *   - The first call on a device looks up that array's device address (once
+ *     per device); make that first call before any stream capture.
+ *   - Work is enqueued on `stream` (NULL = legacy default stream) and the call
+ *     returns without waiting.  Every call shares the one array and leaves its
+ *     contents behind, so calls that overlap on the GPU (other streams, other
+ *     host threads) race: order them on one stream or synchronise between them. */
+int fsph_pbf_eval_lambda_noalloc(const fsph_params *params, const float *pos4, int n, float *dens,
+                                 float *lambda, void *stream);
+
 /* ---- measurement ---- */
 typedef enum fsph_pass {
     FSPH_PASS_LAMBDA = 0,      /* one lambda pass (density + constraint + error reduction) */

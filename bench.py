@@ -124,7 +124,7 @@ def make_scene(block=BLOCK, warm_start=0):
     p.error_mode = abi.ERR_ONE_SIDED
     p.clamp_constraint = 1
     p.min_iter = 2
-    p.max_iter = 100
+    p.max_iter = 400
     p.use_graph = 1
     p.warm_start = warm_start
     return sc

@@ -72,7 +72,8 @@ class FsphParams(ctypes.Structure):
         ("use_graph", ctypes.c_int),
         ("warm_start", ctypes.c_int),
         ("clamp_constraint", ctypes.c_int),
-        ("reserved", ctypes.c_int * 6),
+        ("walk_cells", ctypes.c_int),
+        ("reserved", ctypes.c_int * 5),
     ]
 
     def to_dict(self) -> dict:

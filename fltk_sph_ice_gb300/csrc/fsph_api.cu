@@ -54,6 +54,7 @@ struct fsph_ctx {
     float4 *xb = nullptr, *acc = nullptr, *vort = nullptr;
     float *dens = nullptr, *pres = nullptr;
     unsigned int *key = nullptr, *rank = nullptr, *perm = nullptr;
+    NbrLists nl;
     unsigned int *count = nullptr, *cell_start = nullptr, *block_sums = nullptr;
     unsigned int ncells = 0;
     int gdim[3] = {0, 0, 0};
@@ -173,8 +174,12 @@ DevParams make_dev(const fsph_params &p, int n, float dt) {
     d.grid_origin = make_float3((float)org[0], (float)org[1], (float)org[2]);
     d.inv_cw = (float)(1.0 / cw);
     d.gx = g[0]; d.gy = g[1]; d.gz = g[2];
-    double skin_len = (cw - h) * 0.999;
+    /* lists hold every pair within the cell width at the build, so they stay
+     * complete while no particle has moved more than half the skin */
+    double skin_len = 0.5 * (cw - h) * 0.999;
     d.skin2 = (float)(skin_len * skin_len);
+    d.rl2 = (float)(cw * cw);
+    d.use_lists = (p.solver == FSPH_SOLVER_PBF && !p.walk_cells) ? 1 : 0;
     d.dt = dt;
     d.inv_dt = dt != 0.0f ? 1.0f / dt : 0.0f;
     return d;
@@ -196,6 +201,8 @@ void free_particles(fsph_ctx *c) {
     }
     cudaFree(c->xb); cudaFree(c->acc); cudaFree(c->vort); cudaFree(c->dens); cudaFree(c->pres);
     cudaFree(c->key); cudaFree(c->rank); cudaFree(c->perm); cudaFree(c->epart); cudaFree(c->dpart);
+    cudaFree(c->nl.list); cudaFree(c->nl.cnt); cudaFree(c->nl.cellb);
+    c->nl = NbrLists{};
     c->xb = c->acc = c->vort = nullptr;
     c->dens = c->pres = nullptr;
     c->key = c->rank = c->perm = nullptr;
@@ -228,6 +235,8 @@ int alloc_particles(fsph_ctx *c, int cap) {
     FSPH_TRY(dalloc(c, &c->xb, n)); FSPH_TRY(dalloc(c, &c->acc, n)); FSPH_TRY(dalloc(c, &c->vort, n));
     FSPH_TRY(dalloc(c, &c->dens, n)); FSPH_TRY(dalloc(c, &c->pres, n));
     FSPH_TRY(dalloc(c, &c->key, n)); FSPH_TRY(dalloc(c, &c->rank, n)); FSPH_TRY(dalloc(c, &c->perm, n));
+    FSPH_TRY(dalloc(c, &c->nl.list, n * kListMax)); FSPH_TRY(dalloc(c, &c->nl.cnt, n));
+    FSPH_TRY(dalloc(c, &c->nl.cellb, n));
     FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n)));
     FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n)));
     for (int k = 0; k < 2; ++k) {
@@ -282,9 +291,10 @@ void enqueue_rebuild(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
     launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
     launch_rebuild_gather(p.n, c->perm, c->ctl, I.pos, c->ppos[0], c->ppos[1], I.id, I.attr, c->dens, O.pos, O.vel,
-                          O.id, O.attr, c->pres, s);
+                          O.id, O.attr, c->pres, c->key, c->nl.cellb, s);
     launch_rebuild_copy(p.n, c->ctl, O.pos, O.vel, O.id, O.attr, c->pres, I.pos, c->ppos[0], c->ppos[1], c->xb, I.id,
                         I.attr, c->dens, s);
+    launch_build_list(p, c->cell_start, c->xb, c->nl, s);
 }
 
 bool pbf_prepass(const fsph_ctx *c) { return c->P.viscosity != 0.0f; }
@@ -314,13 +324,15 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
     launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
     Gather g{};
-    g.n4 = 3; g.n1 = 2;
+    g.n4 = 3; g.n1 = 3;
     g.src4[0] = c->set[src].pos; g.dst4[0] = c->set[it].pos;
     g.src4[1] = c->ppos[1]; g.dst4[1] = c->ppos[0];
     g.src4[2] = c->ppos[1]; g.dst4[2] = c->xb;
     g.src1[0] = c->set[src].id; g.dst1[0] = c->set[it].id;
     g.src1[1] = c->set[src].attr; g.dst1[1] = c->set[it].attr;
+    g.src1[2] = c->key; g.dst1[2] = c->nl.cellb;
     launch_gather(p.n, c->perm, g, c->ctl, s);
+    launch_build_list(p, c->cell_start, c->xb, c->nl, s);
     return it;
 }
 
@@ -337,9 +349,9 @@ int pbf_step_eager(fsph_ctx *c, const DevParams &p) {
     cudaStream_t s = c->stream;
     int it = enqueue_pbf_pre(c, p, s);
     for (int k = 0;; ++k) {
-        launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+        launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
         launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0,
-                          nullptr, s);
+                          nullptr, c->nl, s);
         FSPH_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s));
         FSPH_CUDA(c, cudaStreamSynchronize(s));
         if (c->ctl_host->done || k > p.max_iter + 1) break;
@@ -402,9 +414,9 @@ int build_pbf_graph(fsph_ctx *c, const DevParams &p) {
     hrb2 = 0;
     if (ext) FSPH_CUDA(c, cudaGraphConditionalHandleCreate(&hrb2, capg, 0, cudaGraphCondAssignDefault));
     FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(c->s2, wbody, &inode, nullptr, 1, cudaStreamCaptureModeRelaxed));
-    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, hw, 1, c->s2);
+    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, hw, 1, c->nl, c->s2);
     launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, hrb, hrb2, ext ? 3 : 1,
-                      nullptr, c->s2);
+                      nullptr, c->nl, c->s2);
     FSPH_CUDA(c, cudaStreamEndCapture(c->s2, &wbody));
     FSPH_CUDA(c, cudaStreamUpdateCaptureDependencies(s, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
 
@@ -487,13 +499,15 @@ int build_on(fsph_ctx *c, const DevParams &p, const float4 *x) {
     cudaStream_t s = c->stream;
     enqueue_sort(c, p, x, s);
     Gather g{};
-    g.n4 = 3; g.n1 = 2;
+    g.n4 = 3; g.n1 = 3;
     g.src4[0] = x; g.dst4[0] = c->set[1].pos;
     g.src4[1] = x; g.dst4[1] = c->ppos[0];
     g.src4[2] = x; g.dst4[2] = c->xb;
     g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
     g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
+    g.src1[2] = c->key; g.dst1[2] = c->nl.cellb;
     launch_gather(p.n, c->perm, g, nullptr, s);
+    launch_build_list(p, c->cell_start, c->xb, c->nl, s);
     return check_launch(c);
 }
 
@@ -554,7 +568,7 @@ void fsph_params_default(fsph_params *o) {
     o->ap_k = 0.1f;
     o->ap_n = 4.0f;
     o->ap_q = 0.2f;
-    o->cell_skin = 0.02f;
+    o->cell_skin = 0.05f;
     o->use_graph = 1;
 }
 
@@ -915,17 +929,17 @@ int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
     /* the state after a step: x* = x in the home set, already cell-ordered */
     FSPH_TRY(build_on(c, p, c->set[0].pos));
     FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
-    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
     cudaEvent_t e0, e1;
     FSPH_CUDA(c, cudaEventCreate(&e0));
     FSPH_CUDA(c, cudaEventCreate(&e1));
     FSPH_CUDA(c, cudaEventRecord(e0, s));
     for (int k = 0; k < reps; ++k) {
         if (pass == FSPH_PASS_LAMBDA) {
-            launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+            launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
         } else if (pass == FSPH_PASS_CORRECTION) {
             launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0,
-                              nullptr, s);
+                              nullptr, c->nl, s);
         } else if (pass == FSPH_PASS_GRID) {
             enqueue_sort(c, p, c->set[1].pos, s);
             Gather g{};
@@ -959,7 +973,7 @@ int fsph_pbf_eval_lambda(fsph_ctx *c, const float *pos4, int n, float *dens, flo
     cudaStream_t s = c->stream;
     FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
     FSPH_TRY(build_on(c, p, c->set[0].pos));
-    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, s);
+    launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
     FSPH_TRY(check_launch(c));
     FSPH_TRY(copy_out_scalar(c, c->dens, c->set[1].id, dens, n));
     launch_unsort_w(n, c->set[1].id, c->ppos[0], reinterpret_cast<float *>(c->key), s);
@@ -980,7 +994,7 @@ int fsph_pbf_eval_correction(fsph_ctx *c, const float *pos4, const float *lambda
     FSPH_CUDA(c, cudaMemcpyAsync(dl, lambda, (size_t)n * 4, cudaMemcpyHostToDevice, s));
     launch_pack_w(n, c->set[0].pos, dl, s);
     FSPH_TRY(build_on(c, p, c->set[0].pos));
-    launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0, c->acc, s);
+    launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0, c->acc, c->nl, s);
     FSPH_TRY(check_launch(c));
     launch_unsort4(n, c->set[1].id, c->acc, c->set[0].vel, 1, s);
     FSPH_CUDA(c, cudaMemcpyAsync(dp4, c->set[0].vel, (size_t)n * 16, cudaMemcpyDeviceToHost, s));

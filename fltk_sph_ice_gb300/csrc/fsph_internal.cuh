@@ -40,9 +40,19 @@ struct DevParams {
     float3 grid_origin;
     float inv_cw;
     int gx, gy, gz;
-    float skin2;                /* (cell_skin * h)^2 */
+    float skin2;                /* squared displacement since the last build that forces a rebuild */
+    float rl2;                  /* squared neighbour-list radius (= cell width) */
+    int use_lists;              /* 1: lambda / correction passes read the neighbour lists */
     float dt, inv_dt;
 };
+
+/* Neighbour lists: up to kListMax entries per particle, transposed
+ * (entry k of slot i at [k * n + i]) so a warp's lanes read consecutive
+ * 16-bit words; an entry is (row << 12) | (j - row_start), row = the
+ * (dz, dy) index 0..8 of the 27-cell neighbourhood of the particle's build
+ * cell.  A count of kListOverflow sends the particle to the cell walk. */
+constexpr int kListMax = 64;
+constexpr unsigned char kListOverflow = 255;
 
 /* Device control block of one context: the loop state that the reference
  * kept on the host (rx_sph_pbd_gpu.cpp:874-921). */

@@ -200,11 +200,13 @@ __global__ void k_rebuild_gather(int n, const unsigned int *__restrict__ perm, c
                                  const unsigned int *__restrict__ id, const unsigned int *__restrict__ attr,
                                  const float *__restrict__ dens, float4 *__restrict__ t_pos,
                                  float4 *__restrict__ t_x, unsigned int *__restrict__ t_id,
-                                 unsigned int *__restrict__ t_attr, float *__restrict__ t_dens) {
+                                 unsigned int *__restrict__ t_attr, float *__restrict__ t_dens,
+                                 const unsigned int *__restrict__ key, unsigned int *__restrict__ cellb) {
     int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
     const float4 *x4 = ctl->parity ? ppos1 : ppos0;
     unsigned int s = perm[d];
+    if (cellb) cellb[d] = key[s];
     t_pos[d] = pos[s];
     t_x[d] = x4[s];
     t_id[d] = id[s];
@@ -233,6 +235,70 @@ __global__ void k_rebuild_copy(int n, DevCtl *ctl, const float4 *__restrict__ t_
     id[d] = t_id[d];
     attr[d] = t_attr[d];
     dens[d] = t_dens[d];
+}
+
+/* ======================================================================== */
+/* neighbour lists                                                          */
+/* ======================================================================== */
+
+/* Every slot j within the list radius (= the cell width) of slot i at the
+ * build positions xb, self included, as (row << 12) | (j - row_start). */
+__global__ void k_build_list(DevParams p, const unsigned int *__restrict__ cell_start,
+                             const float4 *__restrict__ xb, const unsigned int *__restrict__ cellb,
+                             unsigned short *__restrict__ list, unsigned char *__restrict__ cnt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const float3 xi = f3(xb[i]);
+    const int cb = (int)cellb[i];
+    int k = 0;
+    bool ovf = false;
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
+        const unsigned int s = __ldg(cell_start + base - 1), e = __ldg(cell_start + base + 2);
+        if (e - s > 4095u) ovf = true;
+        for (unsigned int j = s; j < e; ++j) {
+            float3 d = xi - f3(__ldg(xb + j));
+            if (dot3(d, d) < p.rl2) {
+                if (k < kListMax) list[(size_t)k * p.n + i] = (unsigned short)((r << 12) | (j - s));
+                ++k;
+            }
+        }
+    }
+    cnt[i] = (ovf || k > kListMax) ? kListOverflow : (unsigned char)k;
+}
+
+/* Calls f(j) for every candidate slot j of slot i: its list entries, or --
+ * for an overflowed list or when lists are off -- every slot of the 27 cells
+ * around the current position.  rs: this thread's 9 row starts in shared
+ * memory, strided by the block size. */
+template <class F>
+__device__ __forceinline__ void for_each_candidate(const DevParams &p, const unsigned int *__restrict__ cell_start,
+                                                   const unsigned short *__restrict__ list,
+                                                   const unsigned char *__restrict__ cnt,
+                                                   const unsigned int *__restrict__ cellb, int i, float3 xi,
+                                                   unsigned int *rs, F &&f) {
+    const int k = list ? (int)cnt[i] : (int)kListOverflow;
+    if (k != (int)kListOverflow) {
+        const int cb = (int)cellb[i];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
+            rs[r * blockDim.x] = __ldg(cell_start + base - 1);
+        }
+        for (int t = 0; t < k; ++t) {
+            const unsigned int e = list[(size_t)t * p.n + i];
+            f(rs[(e >> 12) * blockDim.x] + (e & 0xfffu));
+        }
+    } else {
+        const int3 c = cell_of(xi, p);
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy) {
+                unsigned int s, e;
+                row_range(cell_start, c, dy, dz, p, s, e);
+                for (unsigned int j = s; j < e; ++j) f(j);
+            }
+    }
 }
 
 /* ======================================================================== */
@@ -299,38 +365,36 @@ __global__ void k_pbf_visc(DevParams p, const unsigned int *__restrict__ cell_st
 __global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens,
                                                    DevCtl *ctl, ErrPartial *part,
-                                                   cudaGraphConditionalHandle hwhile, int use_graph) {
+                                                   cudaGraphConditionalHandle hwhile, int use_graph,
+                                                   const unsigned short *__restrict__ list,
+                                                   const unsigned char *__restrict__ cnt,
+                                                   const unsigned int *__restrict__ cellb) {
     __shared__ float sh1[kBlock / 32], sh2[kBlock / 32], shm[kBlock / 32];
+    __shared__ unsigned int s_rs[9 * kBlock];
     __shared__ int s_last;
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     float4 *pp = par ? ppos1 : ppos0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float e1 = 0.f, e2 = 0.f, em = 0.f;
     if (i < p.n) {
-        float3 xi = f3(pp[i]);
-        int3 c = cell_of(xi, p);
+        const float3 xi = f3(pp[i]);
         float wsum = 0.f, sd = 0.f;
         float3 gs = make_float3(0.f, 0.f, 0.f);
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy) {
-                unsigned int s, e;
-                row_range(cell_start, c, dy, dz, p, s, e);
-                for (unsigned int j = s; j < e; ++j) {
-                    float3 d = xi - f3(__ldcg(pp + j));
-                    float r2 = dot3(d, d);
-                    if (r2 < p.h2) {
-                        float q = p.h2 - r2;
-                        wsum += q * q * q;
-                        if (r2 > 0.0f) {
-                            float r = sqrtf(r2);
-                            float t = p.h - r;
-                            float g = p.ag * t * t / r * p.inv_rest_dens; /* grad W / rho0 = g d */
-                            gs = gs + g * d;
-                            sd += g * g * r2;
-                        }
-                    }
+        for_each_candidate(p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) {
+            const float3 d = xi - f3(__ldcg(pp + j));
+            const float r2 = dot3(d, d);
+            if (r2 < p.h2) {
+                const float q = p.h2 - r2;
+                wsum += q * q * q;
+                if (r2 > 0.0f) {
+                    const float r = sqrtf(r2);
+                    const float t = p.h - r;
+                    const float g = p.ag * t * t / r * p.inv_rest_dens; /* grad W / rho0 = g d */
+                    gs = gs + g * d;
+                    sd += g * g * r2;
                 }
             }
+        });
         float rho = p.mass * p.aw * wsum;
         sd += dot3(gs, gs);
         float C = rho * p.inv_rest_dens - 1.0f;
@@ -406,8 +470,12 @@ __global__ void __launch_bounds__(kBlock) k_correction(DevParams p, const unsign
                                                        const float4 *__restrict__ xb, DevCtl *ctl, float *part,
                                                        cudaGraphConditionalHandle hif,
                                                        cudaGraphConditionalHandle hif2, int use_graph,
-                                                       float4 *__restrict__ dp_out) {
+                                                       float4 *__restrict__ dp_out,
+                                                       const unsigned short *__restrict__ list,
+                                                       const unsigned char *__restrict__ cnt,
+                                                       const unsigned int *__restrict__ cellb) {
     __shared__ float shm[kBlock / 32];
+    __shared__ unsigned int s_rs[9 * kBlock];
     __shared__ int s_last;
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     const float4 *__restrict__ src = par ? ppos1 : ppos0;
@@ -415,35 +483,29 @@ __global__ void __launch_bounds__(kBlock) k_correction(DevParams p, const unsign
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float disp2 = 0.f;
     if (i < p.n) {
-        float4 xi4 = src[i];
-        float3 xi = f3(xi4);
+        const float4 xi4 = src[i];
+        const float3 xi = f3(xi4);
         const float li = xi4.w;
-        int3 c = cell_of(xi, p);
         float3 acc = make_float3(0.f, 0.f, 0.f);
         const float k_dt2 = -p.ap_k * p.dt * p.dt;
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy) {
-                unsigned int s, e;
-                row_range(cell_start, c, dy, dz, p, s, e);
-                for (unsigned int j = s; j < e; ++j) {
-                    float4 xj4 = __ldg(src + j);
-                    float3 d = xi - f3(xj4);
-                    float r2 = dot3(d, d);
-                    if (r2 < p.h2 && r2 > 0.0f) {
-                        float r = sqrtf(r2);
-                        float t = p.h - r;
-                        float g = p.ag * t * t / r * p.inv_rest_dens;
-                        float sc = 0.0f;
-                        if (p.use_ap) {
-                            float q = p.h2 - r2;
-                            float ww = p.aw * q * q * q * p.inv_wq;
-                            float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
-                            sc = k_dt2 * pw;
-                        }
-                        acc = acc + ((li + xj4.w + sc) * g) * d;
-                    }
+        for_each_candidate(p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) {
+            const float4 xj4 = __ldg(src + j);
+            const float3 d = xi - f3(xj4);
+            const float r2 = dot3(d, d);
+            if (r2 < p.h2 && r2 > 0.0f) {
+                const float r = sqrtf(r2);
+                const float t = p.h - r;
+                const float g = p.ag * t * t / r * p.inv_rest_dens;
+                float sc = 0.0f;
+                if (p.use_ap) {
+                    const float q = p.h2 - r2;
+                    const float ww = p.aw * q * q * q * p.inv_wq;
+                    const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
+                    sc = k_dt2 * pw;
                 }
+                acc = acc + ((li + xj4.w + sc) * g) * d;
             }
+        });
         if (dp_out) dp_out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
         float3 xn = wall_project(xi + acc, p);
         dst[i] = make_float4(xn.x, xn.y, xn.z, 0.0f);
@@ -803,9 +865,9 @@ void launch_hash_parity(const DevParams &p, const float4 *ppos0, const float4 *p
 void launch_rebuild_gather(int n, const unsigned int *perm, const DevCtl *ctl, const float4 *pos, const float4 *ppos0,
                            const float4 *ppos1, const unsigned int *id, const unsigned int *attr, const float *dens,
                            float4 *t_pos, float4 *t_x, unsigned int *t_id, unsigned int *t_attr, float *t_dens,
-                           cudaStream_t s) {
+                           const unsigned int *key, unsigned int *cellb, cudaStream_t s) {
     k_rebuild_gather<<<blocks_for(n), kBlock, 0, s>>>(n, perm, ctl, pos, ppos0, ppos1, id, attr, dens, t_pos, t_x,
-                                                      t_id, t_attr, t_dens);
+                                                      t_id, t_attr, t_dens, key, cellb);
 }
 void launch_rebuild_copy(int n, DevCtl *ctl, const float4 *t_pos, const float4 *t_x, const unsigned int *t_id,
                          const unsigned int *t_attr, const float *t_dens, float4 *pos, float4 *ppos0, float4 *ppos1,
@@ -823,16 +885,24 @@ void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const f
 }
 void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1, float *dens,
                    DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
-                   cudaStream_t s) {
+                   const NbrLists &nl, cudaStream_t s) {
     k_lambda<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
-                                                (cudaGraphConditionalHandle)while_handle, use_graph);
+                                                (cudaGraphConditionalHandle)while_handle, use_graph,
+                                                p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
+}
+void launch_build_list(const DevParams &p, const unsigned int *cell_start, const float4 *xb, const NbrLists &nl,
+                       cudaStream_t s) {
+    if (!p.use_lists) return;
+    k_build_list<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, xb, nl.cellb, nl.list, nl.cnt);
 }
 void launch_correction(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1,
                        const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,
-                       unsigned long long if_handle2, int use_graph, float4 *dp_out, cudaStream_t s) {
+                       unsigned long long if_handle2, int use_graph, float4 *dp_out, const NbrLists &nl,
+                       cudaStream_t s) {
     k_correction<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb, ctl, part,
                                                     (cudaGraphConditionalHandle)if_handle,
-                                                    (cudaGraphConditionalHandle)if_handle2, use_graph, dp_out);
+                                                    (cudaGraphConditionalHandle)if_handle2, use_graph, dp_out,
+                                                    p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
 void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
                      const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,

@@ -44,7 +44,17 @@ void launch_hash_parity(const DevParams &p, const float4 *ppos0, const float4 *p
 void launch_rebuild_gather(int n, const unsigned int *perm, const DevCtl *ctl, const float4 *pos, const float4 *ppos0,
                            const float4 *ppos1, const unsigned int *id, const unsigned int *attr, const float *dens,
                            float4 *t_pos, float4 *t_x, unsigned int *t_id, unsigned int *t_attr, float *t_dens,
-                           cudaStream_t s);
+                           const unsigned int *key, unsigned int *cellb, cudaStream_t s);
+
+/* neighbour lists (see fsph_internal.cuh) */
+struct NbrLists {
+    unsigned short *list = nullptr;  /* [kListMax][n] */
+    unsigned char *cnt = nullptr;    /* [n], kListOverflow = use the cell walk */
+    unsigned int *cellb = nullptr;   /* [n] build cell of each slot */
+};
+/* lists of every slot from the build positions xb (a no-op when p.use_lists == 0) */
+void launch_build_list(const DevParams &p, const unsigned int *cell_start, const float4 *xb, const NbrLists &nl,
+                       cudaStream_t s);
 void launch_rebuild_copy(int n, DevCtl *ctl, const float4 *t_pos, const float4 *t_x, const unsigned int *t_id,
                          const unsigned int *t_attr, const float *t_dens, float4 *pos, float4 *ppos0, float4 *ppos1,
                          float4 *xb, unsigned int *id, unsigned int *attr, float *dens, cudaStream_t s);
@@ -56,10 +66,11 @@ void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const f
                      const float *dens, float4 *acc, cudaStream_t s);
 void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1, float *dens,
                    DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
-                   cudaStream_t s);
+                   const NbrLists &nl, cudaStream_t s);
 void launch_correction(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1,
                        const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,
-                       unsigned long long if_handle2, int use_graph, float4 *dp_out, cudaStream_t s);
+                       unsigned long long if_handle2, int use_graph, float4 *dp_out, const NbrLists &nl,
+                       cudaStream_t s);
 void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
                      const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,
                      float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, cudaStream_t s);

@@ -121,7 +121,7 @@ extern "C" int fsph_pbf_eval_lambda_noalloc(const fsph_params *params, const flo
     g.src4[0] = reinterpret_cast<const float4 *>(pos4);
     g.dst4[0] = x;
     launch_gather(n, perm, g, nullptr, s);
-    launch_lambda(p, cell_start, x, x, d_sorted, ctl, part, 0ull, 0, s);
+    launch_lambda(p, cell_start, x, x, d_sorted, ctl, part, 0ull, 0, NbrLists{}, s);
     launch_unsort1(n, perm, reinterpret_cast<const unsigned int *>(d_sorted), reinterpret_cast<unsigned int *>(dens), s);
     launch_unsort_w(n, perm, x, lambda, s);
     if (cudaGetLastError() != cudaSuccess) return FSPH_CUDA_ERROR;

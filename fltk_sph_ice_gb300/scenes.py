@@ -130,7 +130,7 @@ def pbf_params(h: float, box_min, box_max, n: int, **kw) -> abi.FsphParams:
     p.ap_k, p.ap_n, p.ap_q = 0.1, 4.0, 0.2
     p.xsph_c = 0.01
     p.vort_eps = 1e-4
-    p.cell_skin = 0.02
+    p.cell_skin = 0.05
     p.use_graph = 1
     p.warm_start = 0
     for k, v in kw.items():

@@ -118,7 +118,9 @@ typedef struct fsph_params {
     int warm_start;          /* 0: plain; 1: learned MLP warm start of the PBF iterations */
     int clamp_constraint;    /* 0: C = rho/rho0 - 1 as the reference (rx_sph_pbd.cpp:751);
                                 1: unilateral C = max(rho/rho0 - 1, 0) (opt-in, not the reference) */
-    int reserved[6];
+    int walk_cells;          /* 0: PBF passes read per-particle neighbour lists built with
+                                each grid (radius = cell width); 1: walk the 27 cells every pass */
+    int reserved[5];
 } fsph_params;
 
 /* Scene description in the reference's own terms (rxSPHEnviroment). */

@@ -132,6 +132,28 @@ def test_fp64_error_report(gpu):
         assert e < 1e-5, (k, e)
 
 
+def test_neighbour_lists_match_cell_walk(gpu):
+    """Lists visit the in-range candidates of the 27-cell walk in the walk's
+    order: bit-identical passes at a build, equal steps within the parity bar."""
+    sc = scenes.pbf_double_dam_break(block=(12, 12, 24))
+    out = {}
+    for wc in (0, 1):
+        p = abi.FsphParams.from_buffer_copy(sc.params)
+        p.walk_cells = wc
+        ps = rxPBDSPH(p)
+        d, lam = ps.EvalScalingFactor(sc.pos)
+        ps.Set(sc.pos, sc.vel)
+        its = []
+        for _ in range(20):
+            ps.Update(sc.dt)
+            its.append(ps.last_stats.iterations)
+        out[wc] = (d, lam, ps.GetArrayVBO(abi.RX_POSITION), its, ps.last_stats.grid_builds)
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert_rel(out[0][2], out[1][2], 1e-5, "positions after 20 steps")
+    assert out[0][3] == out[1][3]
+
+
 def test_graph_and_eager_bit_identical(gpu):
     sc = scenes.pbf_double_dam_break(block=(12, 12, 24))
     out = []

@@ -206,6 +206,8 @@ def gpu_arm(args):
     L = abi.lib()
 
     sc = make_scene(warm_start=1 if args.warm_start else 0)
+    if args.eager:
+        sc.params.use_graph = 0
     n = sc.n
     dt = sc.dt
     ps = rxPBDSPH(sc.params)
@@ -366,6 +368,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--preroll", type=int, default=PREROLL)
     ap.add_argument("--warm-start", action="store_true")
+    ap.add_argument("--eager", action="store_true",
+                    help="host-driven iteration loop instead of the CUDA graph (same kernels; for ncu, "
+                         "which cannot profile kernels inside graphs with conditional nodes)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

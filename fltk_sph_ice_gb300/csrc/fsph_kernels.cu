@@ -268,16 +268,22 @@ __global__ void k_build_list(DevParams p, const unsigned int *__restrict__ cell_
     cnt[i] = (ovf || k > kListMax) ? kListOverflow : (unsigned char)k;
 }
 
-/* Calls f(j) for every candidate slot j of slot i: its list entries, or --
- * for an overflowed list or when lists are off -- every slot of the 27 cells
- * around the current position.  rs: this thread's 9 row starts in shared
- * memory, strided by the block size. */
-template <class F>
+/* Calls f(j, x[j]) for every candidate slot j of slot i: its list entries,
+ * or -- for an overflowed list or when lists are off -- every slot of the 27
+ * cells around the current position.  List entries are taken kBatch at a
+ * time: their indices are decoded and their positions loaded before any is
+ * used, so each thread keeps kBatch independent loads in flight (the passes
+ * are bound by load latency, not by arithmetic).  rs: this thread's 9 row
+ * starts in shared memory, strided by the block size.  Load selects the
+ * load flavour for x. */
+constexpr int kBatch = 4;
+
+template <class Load, class F>
 __device__ __forceinline__ void for_each_candidate(const DevParams &p, const unsigned int *__restrict__ cell_start,
                                                    const unsigned short *__restrict__ list,
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb, int i, float3 xi,
-                                                   unsigned int *rs, F &&f) {
+                                                   unsigned int *rs, Load &&load, F &&f) {
     const int k = list ? (int)cnt[i] : (int)kListOverflow;
     if (k != (int)kListOverflow) {
         const int cb = (int)cellb[i];
@@ -286,9 +292,20 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
             const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
             rs[r * blockDim.x] = __ldg(cell_start + base - 1);
         }
-        for (int t = 0; t < k; ++t) {
-            const unsigned int e = list[(size_t)t * p.n + i];
-            f(rs[(e >> 12) * blockDim.x] + (e & 0xfffu));
+        for (int t0 = 0; t0 < k; t0 += kBatch) {
+            unsigned int j[kBatch];
+            float4 xj[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int t = t0 + u < k ? t0 + u : k - 1;
+                const unsigned int e = __ldg(list + (size_t)t * p.n + i);
+                j[u] = rs[(e >> 12) * blockDim.x] + (e & 0xfffu);
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) xj[u] = load(j[u]);
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u)
+                if (t0 + u < k) f(j[u], xj[u]);
         }
     } else {
         const int3 c = cell_of(xi, p);
@@ -296,7 +313,7 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
             for (int dy = -1; dy <= 1; ++dy) {
                 unsigned int s, e;
                 row_range(cell_start, c, dy, dz, p, s, e);
-                for (unsigned int j = s; j < e; ++j) f(j);
+                for (unsigned int j = s; j < e; ++j) f(j, load(j));
             }
     }
 }
@@ -380,21 +397,26 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned i
         const float3 xi = f3(pp[i]);
         float wsum = 0.f, sd = 0.f;
         float3 gs = make_float3(0.f, 0.f, 0.f);
-        for_each_candidate(p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) {
-            const float3 d = xi - f3(__ldcg(pp + j));
-            const float r2 = dot3(d, d);
-            if (r2 < p.h2) {
-                const float q = p.h2 - r2;
-                wsum += q * q * q;
-                if (r2 > 0.0f) {
-                    const float r = sqrtf(r2);
-                    const float t = p.h - r;
-                    const float g = p.ag * t * t / r * p.inv_rest_dens; /* grad W / rho0 = g d */
-                    gs = gs + g * d;
-                    sd += g * g * r2;
+        const float agr = p.ag * p.inv_rest_dens;
+        /* plain (L1-cached) loads: only the .w words of pp are written by this
+         * kernel, and the neighbour loop reads x, y, z */
+        for_each_candidate(
+            p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return pp[j]; },
+            [&](unsigned int, const float4 &xj4) {
+                const float3 d = xi - f3(xj4);
+                const float r2 = dot3(d, d);
+                if (r2 < p.h2) {
+                    const float q = p.h2 - r2;
+                    wsum += q * q * q;
+                    if (r2 > 0.0f) {
+                        const float inv_r = rsqrtf(r2);
+                        const float t = p.h - r2 * inv_r;
+                        const float g = agr * t * t * inv_r; /* grad W / rho0 = g d */
+                        gs = gs + g * d;
+                        sd += g * g * r2;
+                    }
                 }
-            }
-        });
+            });
         float rho = p.mass * p.aw * wsum;
         sd += dot3(gs, gs);
         float C = rho * p.inv_rest_dens - 1.0f;
@@ -488,24 +510,27 @@ __global__ void __launch_bounds__(kBlock) k_correction(DevParams p, const unsign
         const float li = xi4.w;
         float3 acc = make_float3(0.f, 0.f, 0.f);
         const float k_dt2 = -p.ap_k * p.dt * p.dt;
-        for_each_candidate(p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) {
-            const float4 xj4 = __ldg(src + j);
-            const float3 d = xi - f3(xj4);
-            const float r2 = dot3(d, d);
-            if (r2 < p.h2 && r2 > 0.0f) {
-                const float r = sqrtf(r2);
-                const float t = p.h - r;
-                const float g = p.ag * t * t / r * p.inv_rest_dens;
-                float sc = 0.0f;
-                if (p.use_ap) {
-                    const float q = p.h2 - r2;
-                    const float ww = p.aw * q * q * q * p.inv_wq;
-                    const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
-                    sc = k_dt2 * pw;
+        const float agr = p.ag * p.inv_rest_dens;
+        const float awq = p.aw * p.inv_wq;
+        for_each_candidate(
+            p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(src + j); },
+            [&](unsigned int, const float4 &xj4) {
+                const float3 d = xi - f3(xj4);
+                const float r2 = dot3(d, d);
+                if (r2 < p.h2 && r2 > 0.0f) {
+                    const float inv_r = rsqrtf(r2);
+                    const float t = p.h - r2 * inv_r;
+                    const float g = agr * t * t * inv_r;
+                    float sc = 0.0f;
+                    if (p.use_ap) {
+                        const float q = p.h2 - r2;
+                        const float ww = awq * q * q * q;
+                        const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
+                        sc = k_dt2 * pw;
+                    }
+                    acc = acc + ((li + xj4.w + sc) * g) * d;
                 }
-                acc = acc + ((li + xj4.w + sc) * g) * d;
-            }
-        });
+            });
         if (dp_out) dp_out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
         float3 xn = wall_project(xi + acc, p);
         dst[i] = make_float4(xn.x, xn.y, xn.z, 0.0f);

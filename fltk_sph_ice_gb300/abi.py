@@ -32,10 +32,17 @@ RX_PREDICT_POS = 8
 RX_PREDICT_VEL = 9
 RX_SCALING_FACTOR = 10
 RX_CORRECTION = 11
+RX_STEP_CORRECTION = 12
 RX_VORTICITY = 18
 FSPH_SORTED_ID = 64
+FSPH_FEATURES = 65
 
-VECTOR_ARRAYS = {RX_POSITION, RX_VELOCITY, RX_FORCE, RX_PREDICT_POS, RX_PREDICT_VEL, RX_CORRECTION, RX_VORTICITY}
+VECTOR_ARRAYS = {RX_POSITION, RX_VELOCITY, RX_FORCE, RX_PREDICT_POS, RX_PREDICT_VEL, RX_CORRECTION, RX_VORTICITY,
+                 RX_STEP_CORRECTION}
+
+# learned warm start (fsph.h)
+MLP_FEATURES, MLP_HIDDEN, MLP_OUTPUTS, MLP_BLOB_SIZE = 16, 64, 3, 5476
+WARM_NONE, WARM_LEARNED = 0, 1
 
 STATUS_NAMES = {
     OK: "FSPH_OK", INVALID_ARG: "FSPH_INVALID_ARG", OOM: "FSPH_OOM", CUDA_ERROR: "FSPH_CUDA_ERROR",
@@ -73,7 +80,8 @@ class FsphParams(ctypes.Structure):
         ("warm_start", ctypes.c_int),
         ("clamp_constraint", ctypes.c_int),
         ("walk_cells", ctypes.c_int),
-        ("reserved", ctypes.c_int * 5),
+        ("collect_features", ctypes.c_int),
+        ("reserved", ctypes.c_int * 4),
     ]
 
     def to_dict(self) -> dict:
@@ -127,6 +135,8 @@ EXPORTS = [
     "fsph_num_particles", "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats",
     "fsph_get_array", "fsph_device_ptr", "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda",
     "fsph_pbf_eval_correction", "fsph_sph_eval_forces", "fsph_time_pass", "fsph_pbf_eval_lambda_noalloc",
+    "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
+    "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
 ]
 
 # fsph_pass
@@ -164,7 +174,19 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_pbf_eval_correction.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p]
     L.fsph_sph_eval_forces.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.fsph_time_pass.argtypes = [c_void_p, c_int, c_int, P(c_float)]
-    for name in ["fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",
+    L.fsph_mlp_create.argtypes = [P(c_void_p)]
+    L.fsph_mlp_destroy.argtypes = [c_void_p]
+    L.fsph_mlp_set_blob.argtypes = [c_void_p, c_void_p]
+    L.fsph_mlp_get_blob.argtypes = [c_void_p, c_void_p]
+    L.fsph_mlp_last_error.argtypes = [c_void_p]
+    L.fsph_mlp_last_error.restype = c_char_p
+    L.fsph_mlp_forward.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+    L.fsph_mlp_gradient.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, P(c_float)]
+    L.fsph_mlp_train.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p]
+    L.fsph_set_warm_start_model.argtypes = [c_void_p, c_void_p]
+    for name in ["fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob",
+                 "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
+                 "fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",
                  "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats", "fsph_get_array",
                  "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda", "fsph_pbf_eval_correction",
                  "fsph_sph_eval_forces", "fsph_params_from_env"]:

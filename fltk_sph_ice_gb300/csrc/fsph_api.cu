@@ -30,6 +30,7 @@
 
 #include "../../include/fsph.h"
 #include "fsph_kernels.cuh"
+#include "fsph_mlp.cuh"
 
 using namespace fsph;
 
@@ -62,6 +63,15 @@ struct fsph_ctx {
     DevCtl *ctl_host = nullptr;
     unsigned int *flag = nullptr;      /* input-validation flag */
     unsigned int *flag_host = nullptr;
+    /* warm start */
+    float4 *xpred = nullptr;           /* x* before the iterations, iteration order */
+    float4 *dstep = nullptr;           /* x*_final - x*_pred of the last step, home order */
+    float4 *dwarm = nullptr;           /* predicted correction for the coming step, home order */
+    float4 *tmp4 = nullptr;            /* scratch stream for reorders */
+    float *feat = nullptr;             /* [n][kFeatures], home order */
+    unsigned int *warm_valid = nullptr;
+    MlpDev *mlp_dev = nullptr;
+    bool model_loaded = false;
     ErrPartial *epart = nullptr;
     float *dpart = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -118,7 +128,7 @@ int validate(const fsph_params &p, std::string &why) {
         if (p.use_ap && !(p.ap_q > 0.0f && p.ap_q < 1.0f)) { why = "ap_q must lie in (0, 1)"; return FSPH_INVALID_ARG; }
     }
     if (p.cell_skin < 0.0f || p.cell_skin > 1.0f) { why = "cell_skin must lie in [0, 1]"; return FSPH_INVALID_ARG; }
-    if (p.warm_start != 0) { why = "warm_start requires the learned-warm-start build"; return FSPH_UNSUPPORTED; }
+    if (p.warm_start < 0 || p.warm_start > 1) { why = "warm_start must be 0 or 1"; return FSPH_INVALID_ARG; }
     return FSPH_OK;
 }
 
@@ -203,6 +213,9 @@ void free_particles(fsph_ctx *c) {
     cudaFree(c->key); cudaFree(c->rank); cudaFree(c->perm); cudaFree(c->epart); cudaFree(c->dpart);
     cudaFree(c->nl.list); cudaFree(c->nl.cnt); cudaFree(c->nl.cellb);
     c->nl = NbrLists{};
+    cudaFree(c->xpred); cudaFree(c->dstep); cudaFree(c->dwarm); cudaFree(c->tmp4); cudaFree(c->feat);
+    c->xpred = c->dstep = c->dwarm = c->tmp4 = nullptr;
+    c->feat = nullptr;
     c->xb = c->acc = c->vort = nullptr;
     c->dens = c->pres = nullptr;
     c->key = c->rank = c->perm = nullptr;
@@ -237,6 +250,10 @@ int alloc_particles(fsph_ctx *c, int cap) {
     FSPH_TRY(dalloc(c, &c->key, n)); FSPH_TRY(dalloc(c, &c->rank, n)); FSPH_TRY(dalloc(c, &c->perm, n));
     FSPH_TRY(dalloc(c, &c->nl.list, n * kListMax)); FSPH_TRY(dalloc(c, &c->nl.cnt, n));
     FSPH_TRY(dalloc(c, &c->nl.cellb, n));
+    FSPH_TRY(dalloc(c, &c->xpred, n)); FSPH_TRY(dalloc(c, &c->dstep, n)); FSPH_TRY(dalloc(c, &c->dwarm, n));
+    FSPH_TRY(dalloc(c, &c->tmp4, n)); FSPH_TRY(dalloc(c, &c->feat, n * kFeatures));
+    FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, n * sizeof(float4), c->stream));
+    FSPH_CUDA(c, cudaMemsetAsync(c->feat, 0, n * kFeatures * sizeof(float), c->stream));
     FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n)));
     FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n)));
     for (int k = 0; k < 2; ++k) {
@@ -290,44 +307,61 @@ void enqueue_rebuild(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
     launch_hash_parity(p, c->ppos[0], c->ppos[1], c->ctl, c->key, c->rank, c->count, s);
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
     launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+    const bool ws = c->P.warm_start != 0 || c->P.collect_features != 0;
+    float *t_lam = reinterpret_cast<float *>(c->rank); /* free once the scatter has run */
     launch_rebuild_gather(p.n, c->perm, c->ctl, I.pos, c->ppos[0], c->ppos[1], I.id, I.attr, c->dens, O.pos, O.vel,
-                          O.id, O.attr, c->pres, c->key, c->nl.cellb, s);
+                          O.id, O.attr, c->pres, c->key, c->nl.cellb, ws ? c->xpred : nullptr, c->tmp4, t_lam, s);
     launch_rebuild_copy(p.n, c->ctl, O.pos, O.vel, O.id, O.attr, c->pres, I.pos, c->ppos[0], c->ppos[1], c->xb, I.id,
-                        I.attr, c->dens, s);
+                        I.attr, c->dens, c->tmp4, ws ? c->xpred : nullptr, t_lam, s);
     launch_build_list(p, c->cell_start, c->xb, c->nl, s);
 }
 
 bool pbf_prepass(const fsph_ctx *c) { return c->P.viscosity != 0.0f; }
-bool pbf_finalize_ext(const fsph_ctx *c) { return c->P.xsph_c != 0.0f || c->P.vort_eps != 0.0f; }
+/* step corrections and features are produced (warm start on, or collection) */
+bool pbf_warm_active(const fsph_ctx *c) { return c->P.warm_start != 0 || c->P.collect_features != 0; }
+bool pbf_finalize_ext(const fsph_ctx *c) {
+    return c->P.xsph_c != 0.0f || c->P.vort_eps != 0.0f || pbf_warm_active(c);
+}
 
 /* PBF: pre-pass, prediction, first grid build; returns the set that carries
  * the particles through the iterations. */
 int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s);
+    const bool ws = pbf_warm_active(c);
+    /* warm-start correction of every particle, home order */
+    const float4 *dw = nullptr;
+    if (c->P.warm_start == 1) {
+        launch_mlp_infer(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, s);
+        dw = c->dwarm;
+    }
     int src = 0, it = 1;
     const float4 *acc = nullptr;
     if (pbf_prepass(c)) {
         enqueue_sort(c, p, c->set[0].pos, s);
         Gather g{};
-        g.n4 = 2; g.n1 = 2;
+        g.n4 = dw ? 3 : 2; g.n1 = 2;
         g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
         g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+        g.src4[2] = dw; g.dst4[2] = c->vort; /* vort is rewritten at the end of the step */
         g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
         g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
         launch_gather(p.n, c->perm, g, nullptr, s);
         launch_pbf_density(p, c->cell_start, c->set[1].pos, c->dens, s);
         launch_pbf_visc(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->acc, s);
         acc = c->acc;
+        if (dw) dw = c->vort;
         src = 1; it = 0;
     }
-    launch_predict_hash(p, c->set[src].pos, c->set[src].vel, acc, c->ppos[1], c->key, c->rank, c->count, s);
+    launch_predict_hash(p, c->set[src].pos, c->set[src].vel, acc, c->ppos[1], c->key, c->rank, c->count, dw,
+                        ws ? c->tmp4 : nullptr, s);
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
     launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
     Gather g{};
-    g.n4 = 3; g.n1 = 3;
+    g.n4 = ws ? 4 : 3; g.n1 = 3;
     g.src4[0] = c->set[src].pos; g.dst4[0] = c->set[it].pos;
     g.src4[1] = c->ppos[1]; g.dst4[1] = c->ppos[0];
     g.src4[2] = c->ppos[1]; g.dst4[2] = c->xb;
+    g.src4[3] = c->tmp4; g.dst4[3] = c->xpred;
     g.src1[0] = c->set[src].id; g.dst1[0] = c->set[it].id;
     g.src1[1] = c->set[src].attr; g.dst1[1] = c->set[it].attr;
     g.src1[2] = c->key; g.dst1[2] = c->nl.cellb;
@@ -337,10 +371,21 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
 }
 
 void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
+    const bool ws = pbf_warm_active(c);
     launch_finalize(p, c->set[it].pos, c->ppos[0], c->ppos[1], c->ctl, c->set[it].id, c->set[it].attr,
-                    c->set[0].pos, c->set[0].vel, c->set[0].id, c->set[0].attr, s);
+                    c->set[0].pos, c->set[0].vel, c->set[0].id, c->set[0].attr, ws ? c->xpred : nullptr,
+                    ws ? c->dstep : nullptr, s);
     if (pbf_finalize_ext(c)) {
-        launch_xsph_vort(p, c->cell_start, c->set[0].pos, c->set[0].vel, c->dens, c->set[1].vel, c->vort, s);
+        FeatureOut fo;
+        if (ws) {
+            fo.feat = c->feat;
+            fo.dstep = c->dstep;
+            fo.ppos0 = c->ppos[0];
+            fo.ppos1 = c->ppos[1];
+            fo.ctl = c->ctl;
+            fo.valid = c->warm_valid;
+        }
+        launch_xsph_vort(p, c->cell_start, c->set[0].pos, c->set[0].vel, c->dens, c->set[1].vel, c->vort, fo, s);
         launch_vort_apply(p, c->cell_start, c->set[0].pos, c->vort, c->dens, c->set[1].vel, c->set[0].vel, s);
     }
 }
@@ -487,7 +532,10 @@ int load_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int
         else FSPH_CUDA(c, cudaMemsetAsync(c->set[0].vel, 0, b, c->stream));
         FSPH_CUDA(c, cudaMemsetAsync(c->set[0].attr, 0, (size_t)n * 4, c->stream));
         launch_iota(n, c->set[0].id, c->stream);
+        /* a new state has no step history for the warm start */
+        FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, b, c->stream));
     }
+    FSPH_CUDA(c, cudaMemsetAsync(c->warm_valid, 0, sizeof(unsigned int), c->stream));
     if (n != c->n) c->graph_valid = false;
     c->n = n;
     return check_launch(c);
@@ -642,6 +690,9 @@ int fsph_create(const fsph_params *params, fsph_ctx **out) {
     std::memset(c->ctl_host, 0, sizeof(DevCtl));
     if (cudaMalloc((void **)&c->flag, sizeof(unsigned int)) != cudaSuccess) return bail(FSPH_OOM);
     if (cudaMallocHost((void **)&c->flag_host, sizeof(unsigned int)) != cudaSuccess) return bail(FSPH_OOM);
+    if (cudaMalloc((void **)&c->warm_valid, sizeof(unsigned int)) != cudaSuccess) return bail(FSPH_OOM);
+    if (cudaMalloc((void **)&c->mlp_dev, sizeof(MlpDev)) != cudaSuccess) return bail(FSPH_OOM);
+    cudaMemsetAsync(c->warm_valid, 0, sizeof(unsigned int), c->stream);
     cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), c->stream);
     if ((st = alloc_particles(c, params->max_particles)) != FSPH_OK) return bail(st);
     if ((st = alloc_grid(c)) != FSPH_OK) return bail(st);
@@ -660,6 +711,8 @@ int fsph_destroy(fsph_ctx *c) {
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     cudaFree(c->flag);
     if (c->flag_host) cudaFreeHost(c->flag_host);
+    cudaFree(c->warm_valid);
+    cudaFree(c->mlp_dev);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->s2) cudaStreamDestroy(c->s2);
     if (c->s3) cudaStreamDestroy(c->s3);
@@ -736,6 +789,9 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
     FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
     FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
     launch_iota(n, c->set[0].id, s);
+    /* the step history of the warm start no longer matches the particles */
+    FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, (size_t)n * 16, s));
+    FSPH_CUDA(c, cudaMemsetAsync(c->warm_valid, 0, sizeof(unsigned int), s));
     cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (type == FSPH_POSITION)
         FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos + start, data, (size_t)count * 16, k, s));
@@ -760,6 +816,8 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
         FSPH_CUDA(c, cudaEventRecord(ev, user));
         FSPH_CUDA(c, cudaStreamWaitEvent(c->stream, ev, 0));
     }
+    if (c->P.solver == FSPH_SOLVER_PBF && c->P.warm_start == 1 && !c->model_loaded)
+        return fail(c, FSPH_UNSUPPORTED, "warm_start = 1 needs a network (fsph_set_warm_start_model)");
     DevParams p = make_dev(c->P, c->n, dt);
     c->dp = p;
     if (c->P.solver == FSPH_SOLVER_WCSPH) {
@@ -815,6 +873,17 @@ int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
     case FSPH_VELOCITY: launch_unsort4(n, id, c->set[0].vel, t4, 1, s); break;
     case FSPH_FORCE: launch_unsort4(n, id, c->acc, t4, 1, s); break;
     case FSPH_VORTICITY: launch_unsort4(n, id, c->vort, t4, 1, s); break;
+    case FSPH_STEP_CORRECTION: launch_unsort4(n, id, c->dstep, t4, 1, s); break;
+    case FSPH_FEATURES: {
+        /* kFeatures floats per particle, staged in the (free) list storage */
+        float4 *tf = reinterpret_cast<float4 *>(c->nl.list);
+        launch_unsort_rows(n, id, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
+        FSPH_TRY(check_launch(c));
+        FSPH_CUDA(c, cudaMemcpyAsync(dst, tf, (size_t)n * kFeatures * 4,
+                                     where == FSPH_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        return FSPH_OK;
+    }
     case FSPH_PREDICT_POS: launch_unsort4(n, id, c->ppos[c->ctl_host->parity & 1], t4, 1, s); break;
     case FSPH_CORRECTION: {
         /* position change of the last iteration (after wall projection) */
@@ -917,6 +986,24 @@ int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long 
             std::sort(row, row + hc[d]);
         }
     }
+    return FSPH_OK;
+}
+
+int fsph_set_warm_start_model(fsph_ctx *c, const float *blob) {
+    if (!c || !blob) return FSPH_INVALID_ARG;
+    for (int k = 0; k < FSPH_MLP_BLOB_SIZE; ++k)
+        if (!std::isfinite(blob[k])) return fail(c, FSPH_INVALID_ARG, "non-finite network parameter");
+    float *d = nullptr;
+    FSPH_CUDA(c, cudaMalloc((void **)&d, FSPH_MLP_BLOB_SIZE * sizeof(float)));
+    cudaError_t e = cudaMemcpyAsync(d, blob, FSPH_MLP_BLOB_SIZE * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        launch_mlp_pack(d, c->mlp_dev, c->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(c, FSPH_CUDA_ERROR, std::string("warm-start model: ") + cudaGetErrorString(e));
+    c->model_loaded = true;
     return FSPH_OK;
 }
 

@@ -54,6 +54,22 @@ struct DevParams {
 constexpr int kListMax = 64;
 constexpr unsigned char kListOverflow = 255;
 
+/* Warm-start features of a particle at the end of a step, all dimensionless:
+ *   0 rho/rho0 - 1 of the last lambda pass     1 lambda rho0 h^2
+ *   2 neighbour count / 33                     3-5 mean offset to neighbours / h
+ *   6-8 v dt / h                               9-11 step correction (x*_final - x*_pred) / h
+ *   12 SPH velocity divergence * dt            13-15 colour-field gradient * h
+ * Row-major, kFeatures floats per particle. */
+constexpr int kFeatures = 16;
+struct DevCtl;
+struct FeatureOut {
+    float *feat = nullptr;             /* [n][kFeatures]; nullptr: no features */
+    const float4 *dstep = nullptr;     /* step correction, home order */
+    const float4 *ppos0 = nullptr, *ppos1 = nullptr;
+    const DevCtl *ctl = nullptr;
+    unsigned int *valid = nullptr;     /* set to 1 once features exist */
+};
+
 /* Device control block of one context: the loop state that the reference
  * kept on the host (rx_sph_pbd_gpu.cpp:874-921). */
 struct DevCtl {

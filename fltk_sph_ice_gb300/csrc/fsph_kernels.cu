@@ -32,7 +32,8 @@ namespace fsph {
 __global__ void k_predict_hash(DevParams p, const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                const float4 *__restrict__ acc, float4 *__restrict__ ppos_out,
                                unsigned int *__restrict__ key, unsigned int *__restrict__ rank,
-                               unsigned int *__restrict__ count) {
+                               unsigned int *__restrict__ count, const float4 *__restrict__ dwarm,
+                               float4 *__restrict__ xpred_out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     float3 x = f3(pos[i]);
@@ -41,6 +42,10 @@ __global__ void k_predict_hash(DevParams p, const float4 *__restrict__ pos, cons
     v = v + p.dt * a;
     x = x + p.dt * v;
     x = wall_project(x, p);
+    if (xpred_out) xpred_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
+    /* warm start: the iterations begin from walls(x* + predicted correction);
+     * the grid and lists are then built on that start */
+    if (dwarm) x = wall_project(x + f3(dwarm[i]), p);
     ppos_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
     unsigned int c = cell_index(cell_of(x, p), p);
     key[i] = c;
@@ -201,12 +206,17 @@ __global__ void k_rebuild_gather(int n, const unsigned int *__restrict__ perm, c
                                  const float *__restrict__ dens, float4 *__restrict__ t_pos,
                                  float4 *__restrict__ t_x, unsigned int *__restrict__ t_id,
                                  unsigned int *__restrict__ t_attr, float *__restrict__ t_dens,
-                                 const unsigned int *__restrict__ key, unsigned int *__restrict__ cellb) {
+                                 const unsigned int *__restrict__ key, unsigned int *__restrict__ cellb,
+                                 const float4 *__restrict__ xpred, float4 *__restrict__ t_xpred,
+                                 float *__restrict__ t_lam) {
     int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d >= n) return;
     const float4 *x4 = ctl->parity ? ppos1 : ppos0;
     unsigned int s = perm[d];
     if (cellb) cellb[d] = key[s];
+    if (xpred) t_xpred[d] = xpred[s];
+    /* lambda of the last pass lives in the .w of the other buffer */
+    if (t_lam) t_lam[d] = (ctl->parity ? ppos0 : ppos1)[s].w;
     t_pos[d] = pos[s];
     t_x[d] = x4[s];
     t_id[d] = id[s];
@@ -219,7 +229,9 @@ __global__ void k_rebuild_copy(int n, DevCtl *ctl, const float4 *__restrict__ t_
                                const unsigned int *__restrict__ t_id, const unsigned int *__restrict__ t_attr,
                                const float *__restrict__ t_dens, float4 *__restrict__ pos, float4 *ppos0,
                                float4 *ppos1, float4 *__restrict__ xb, unsigned int *__restrict__ id,
-                               unsigned int *__restrict__ attr, float *__restrict__ dens) {
+                               unsigned int *__restrict__ attr, float *__restrict__ dens,
+                               const float4 *__restrict__ t_xpred, float4 *__restrict__ xpred,
+                               const float *__restrict__ t_lam) {
     int d = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned int par = ctl->parity;
     if (d == 0) {
@@ -227,6 +239,8 @@ __global__ void k_rebuild_copy(int n, DevCtl *ctl, const float4 *__restrict__ t_
         ctl->rebuild = 0u;
     }
     if (d >= n) return;
+    if (xpred) xpred[d] = t_xpred[d];
+    if (t_lam) (par ? ppos0 : ppos1)[d].w = t_lam[d];
     float4 *x4 = par ? ppos1 : ppos0;
     pos[d] = t_pos[d];
     float4 x = t_x[d];
@@ -583,7 +597,8 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
                            const float4 *ppos1, const DevCtl *ctl, const unsigned int *__restrict__ id_b,
                            const unsigned int *__restrict__ attr_b, float4 *__restrict__ pos_a,
                            float4 *__restrict__ vel_a, unsigned int *__restrict__ id_a,
-                           unsigned int *__restrict__ attr_a) {
+                           unsigned int *__restrict__ attr_a, const float4 *__restrict__ xpred,
+                           float4 *__restrict__ dstep) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const float4 *pp = ctl->parity ? ppos1 : ppos0;
@@ -594,6 +609,11 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
     vel_a[i] = make_float4(v.x, v.y, v.z, 0.0f);
     id_a[i] = id_b[i];
     attr_a[i] = attr_b[i];
+    /* total correction of this step, x*_final - x*_predicted */
+    if (dstep) {
+        float3 dd = xs - f3(xpred[i]);
+        dstep[i] = make_float4(dd.x, dd.y, dd.z, 0.0f);
+    }
 }
 
 /* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), and the
@@ -601,12 +621,14 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
 __global__ void k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_start,
                             const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                             const float *__restrict__ dens, float4 *__restrict__ vel_out,
-                            float4 *__restrict__ vort) {
+                            float4 *__restrict__ vort, FeatureOut fo) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     float3 xi = f3(pos[i]), vi = f3(vel[i]);
     int3 c = cell_of(xi, p);
     float3 om = make_float3(0.f, 0.f, 0.f), xs = make_float3(0.f, 0.f, 0.f);
+    float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
+    float div = 0.f, cntf = 1.f; /* self */
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy) {
             unsigned int s, e;
@@ -622,14 +644,40 @@ __global__ void k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_s
                     float3 vij = f3(__ldg(vel + j)) - vi;
                     om = om + cross3(vij, (-g) * d);
                     float q = p.h2 - r2;
-                    float w = p.aw * q * q * q * p.mass / __ldg(dens + j);
+                    float mrho = p.mass / __ldg(dens + j);
+                    float w = p.aw * q * q * q * mrho;
                     xs = xs + w * vij;
+                    if (fo.feat) {
+                        cntf += 1.0f;
+                        off = off - d;
+                        div += mrho * g * dot3(vij, d);
+                        cg = cg + (mrho * g) * d;
+                    }
                 }
             }
         }
     float3 vn = vi + p.xsph_c * xs;
     vel_out[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
     vort[i] = make_float4(om.x, om.y, om.z, 0.0f);
+    if (fo.feat) {
+        /* warm-start features at the end of the step (dimensionless; see kFeatures) */
+        const float inv_h = 1.0f / p.h;
+        const float4 *pl = fo.ctl->parity ? fo.ppos0 : fo.ppos1; /* buffer of the last lambda pass */
+        const float3 dd = f3(fo.dstep[i]);
+        float f[kFeatures];
+        f[0] = dens[i] * p.inv_rest_dens - 1.0f;
+        f[1] = pl[i].w * p.rest_dens * p.h2;
+        f[2] = cntf * (1.0f / 33.0f);
+        f[3] = off.x * inv_h / cntf; f[4] = off.y * inv_h / cntf; f[5] = off.z * inv_h / cntf;
+        f[6] = vi.x * p.dt * inv_h; f[7] = vi.y * p.dt * inv_h; f[8] = vi.z * p.dt * inv_h;
+        f[9] = dd.x * inv_h; f[10] = dd.y * inv_h; f[11] = dd.z * inv_h;
+        f[12] = div * p.dt;
+        f[13] = cg.x * p.h; f[14] = cg.y * p.h; f[15] = cg.z * p.h;
+        float4 *out = reinterpret_cast<float4 *>(fo.feat + (size_t)i * kFeatures);
+#pragma unroll
+        for (int k = 0; k < kFeatures / 4; ++k) out[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+        if (i == 0) *fo.valid = 1u;
+    }
 }
 
 /* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
@@ -831,6 +879,16 @@ __global__ void k_unsort_w(int n, const unsigned int *__restrict__ id, const flo
     if (d >= n) return;
     dst[id[d]] = src[d].w;
 }
+__global__ void k_unsort_rows(int n, const unsigned int *__restrict__ id, const float4 *__restrict__ src,
+                              float4 *__restrict__ dst, int k4) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * k4) return;
+    int d = e / k4, q = e % k4;
+    dst[(size_t)id[d] * k4 + q] = src[e];
+}
+void launch_unsort_rows(int n, const unsigned int *id, const float4 *src, float4 *dst, int k4, cudaStream_t s) {
+    k_unsort_rows<<<blocks_for((long long)n * k4), kBlock, 0, s>>>(n, id, src, dst, k4);
+}
 __global__ void k_iota(int n, unsigned int *dst) {
     int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d < n) dst[d] = (unsigned int)d;
@@ -861,8 +919,9 @@ __global__ void k_pack_w(int n, float4 *dst, const float *w) {
 
 void launch_predict_hash(const DevParams &p, const float4 *pos, const float4 *vel, const float4 *acc,
                          float4 *ppos_out, unsigned int *key, unsigned int *rank, unsigned int *count,
-                         cudaStream_t s) {
-    k_predict_hash<<<blocks_for(p.n), kBlock, 0, s>>>(p, pos, vel, acc, ppos_out, key, rank, count);
+                         const float4 *dwarm, float4 *xpred_out, cudaStream_t s) {
+    k_predict_hash<<<blocks_for(p.n), kBlock, 0, s>>>(p, pos, vel, acc, ppos_out, key, rank, count, dwarm,
+                                                      xpred_out);
 }
 void launch_hash(const DevParams &p, const float4 *x, unsigned int *key, unsigned int *rank, unsigned int *count,
                  cudaStream_t s) {
@@ -890,15 +949,17 @@ void launch_hash_parity(const DevParams &p, const float4 *ppos0, const float4 *p
 void launch_rebuild_gather(int n, const unsigned int *perm, const DevCtl *ctl, const float4 *pos, const float4 *ppos0,
                            const float4 *ppos1, const unsigned int *id, const unsigned int *attr, const float *dens,
                            float4 *t_pos, float4 *t_x, unsigned int *t_id, unsigned int *t_attr, float *t_dens,
-                           const unsigned int *key, unsigned int *cellb, cudaStream_t s) {
+                           const unsigned int *key, unsigned int *cellb, const float4 *xpred, float4 *t_xpred,
+                           float *t_lam, cudaStream_t s) {
     k_rebuild_gather<<<blocks_for(n), kBlock, 0, s>>>(n, perm, ctl, pos, ppos0, ppos1, id, attr, dens, t_pos, t_x,
-                                                      t_id, t_attr, t_dens, key, cellb);
+                                                      t_id, t_attr, t_dens, key, cellb, xpred, t_xpred, t_lam);
 }
 void launch_rebuild_copy(int n, DevCtl *ctl, const float4 *t_pos, const float4 *t_x, const unsigned int *t_id,
                          const unsigned int *t_attr, const float *t_dens, float4 *pos, float4 *ppos0, float4 *ppos1,
-                         float4 *xb, unsigned int *id, unsigned int *attr, float *dens, cudaStream_t s) {
+                         float4 *xb, unsigned int *id, unsigned int *attr, float *dens, const float4 *t_xpred,
+                         float4 *xpred, const float *t_lam, cudaStream_t s) {
     k_rebuild_copy<<<blocks_for(n), kBlock, 0, s>>>(n, ctl, t_pos, t_x, t_id, t_attr, t_dens, pos, ppos0, ppos1, xb,
-                                                    id, attr, dens);
+                                                    id, attr, dens, t_xpred, xpred, t_lam);
 }
 void launch_pbf_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
                         cudaStream_t s) {
@@ -931,13 +992,14 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
 }
 void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
                      const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,
-                     float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, cudaStream_t s) {
+                     float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, const float4 *xpred, float4 *dstep,
+                     cudaStream_t s) {
     k_finalize<<<blocks_for(p.n), kBlock, 0, s>>>(p, pos_b, ppos0, ppos1, ctl, id_b, attr_b, pos_a, vel_a, id_a,
-                                                  attr_a);
+                                                  attr_a, xpred, dstep);
 }
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                      const float *dens, float4 *vel_out, float4 *vort, cudaStream_t s) {
-    k_xsph_vort<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort);
+                      const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, cudaStream_t s) {
+    k_xsph_vort<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort, fo);
 }
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
                        const float *dens, const float4 *vel_in, float4 *vel_out, cudaStream_t s) {

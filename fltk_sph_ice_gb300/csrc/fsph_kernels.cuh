@@ -15,10 +15,12 @@ inline unsigned int blocks_for(long long n, int b = kBlock) { return (unsigned i
 inline unsigned int scan_blocks(unsigned int ncells) { return (ncells + kScanTile - 1) / kScanTile; }
 
 /* ---- grid build: counting sort on the 64-bit key (cell << 32 | previous slot) ---- */
-/* x* = walls(x + dt (v + dt a)), a = gravity when acc == NULL; then key + rank. */
+/* x* = walls(x + dt (v + dt a)), a = gravity when acc == NULL; then key + rank.
+ * xpred_out (optional) keeps that prediction; dwarm (optional) is a warm-start
+ * correction: the iterations then start from walls(x* + dwarm). */
 void launch_predict_hash(const DevParams &p, const float4 *pos, const float4 *vel, const float4 *acc,
                          float4 *ppos_out, unsigned int *key, unsigned int *rank, unsigned int *count,
-                         cudaStream_t s);
+                         const float4 *dwarm, float4 *xpred_out, cudaStream_t s);
 void launch_hash(const DevParams &p, const float4 *x, unsigned int *key, unsigned int *rank, unsigned int *count,
                  cudaStream_t s);
 /* exclusive scan of count[C] into cell_start[C+1]; zeroes count for the next build */
@@ -44,7 +46,8 @@ void launch_hash_parity(const DevParams &p, const float4 *ppos0, const float4 *p
 void launch_rebuild_gather(int n, const unsigned int *perm, const DevCtl *ctl, const float4 *pos, const float4 *ppos0,
                            const float4 *ppos1, const unsigned int *id, const unsigned int *attr, const float *dens,
                            float4 *t_pos, float4 *t_x, unsigned int *t_id, unsigned int *t_attr, float *t_dens,
-                           const unsigned int *key, unsigned int *cellb, cudaStream_t s);
+                           const unsigned int *key, unsigned int *cellb, const float4 *xpred, float4 *t_xpred,
+                           float *t_lam, cudaStream_t s);
 
 /* neighbour lists (see fsph_internal.cuh) */
 struct NbrLists {
@@ -57,7 +60,8 @@ void launch_build_list(const DevParams &p, const unsigned int *cell_start, const
                        cudaStream_t s);
 void launch_rebuild_copy(int n, DevCtl *ctl, const float4 *t_pos, const float4 *t_x, const unsigned int *t_id,
                          const unsigned int *t_attr, const float *t_dens, float4 *pos, float4 *ppos0, float4 *ppos1,
-                         float4 *xb, unsigned int *id, unsigned int *attr, float *dens, cudaStream_t s);
+                         float4 *xb, unsigned int *id, unsigned int *attr, float *dens, const float4 *t_xpred,
+                         float4 *xpred, const float *t_lam, cudaStream_t s);
 
 /* ---- PBF ---- */
 void launch_pbf_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
@@ -73,9 +77,11 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
                        cudaStream_t s);
 void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
                      const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,
-                     float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, cudaStream_t s);
+                     float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, const float4 *xpred, float4 *dstep,
+                     cudaStream_t s);
+/* XSPH + vorticity (omega) pass; with fo.feat also the warm-start features */
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                      const float *dens, float4 *vel_out, float4 *vort, cudaStream_t s);
+                      const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, cudaStream_t s);
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
                        const float *dens, const float4 *vel_in, float4 *vel_out, cudaStream_t s);
 
@@ -99,6 +105,8 @@ void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *ds
 void launch_unsort1(int n, const unsigned int *id, const unsigned int *src, unsigned int *dst, cudaStream_t s);
 void launch_unsort_w(int n, const unsigned int *id, const float4 *src, float *dst, cudaStream_t s);
 void launch_iota(int n, unsigned int *dst, cudaStream_t s);
+/* rows of k4 float4 per slot: dst[id[d]] = src[d] */
+void launch_unsort_rows(int n, const unsigned int *id, const float4 *src, float4 *dst, int k4, cudaStream_t s);
 void launch_pack_w(int n, float4 *dst, const float *w, cudaStream_t s);
 /* *flag |= 1 when any x/y/z of a (or b, if given) is not finite */
 void launch_check_finite(int n, const float4 *a, const float4 *b, unsigned int *flag, cudaStream_t s);

@@ -128,7 +128,9 @@ class rxParticleSystemBase:
     def GetArrayVBO(self, type_: int, d2h: bool = True) -> np.ndarray:
         """GetArrayVBO (rx_ps.h:259): a copy of one array in particle order."""
         n = self.GetNumParticles()
-        if type_ in abi.VECTOR_ARRAYS:
+        if type_ == abi.FSPH_FEATURES:
+            out = np.zeros((n, abi.MLP_FEATURES), dtype=np.float32)
+        elif type_ in abi.VECTOR_ARRAYS:
             out = np.zeros((n, 4), dtype=np.float32)
         elif type_ in (abi.RX_ATTRIBUTE, abi.FSPH_SORTED_ID):
             out = np.zeros(n, dtype=np.int32)

@@ -1,0 +1,213 @@
+"""Learned warm start of the PBF iterations: data collection, training, model files.
+
+The network (fsph_mlp, BF16 tensor-core kernels) maps the 16 end-of-step
+features of a particle (FSPH_FEATURES) to the total position correction its
+next step will need (FSPH_STEP_CORRECTION / h).  The solver then starts the
+constraint iterations from x*_pred + h * network(features) and still
+iterates until the density-error tolerance is met, so the network can only
+change how many iterations a step takes, never the tolerance it reaches.
+
+    python -m fltk_sph_ice_gb300.warmstart --out fltk_sph_ice_gb300/models/warmstart_mlp.npz
+
+collects rollouts of the plain solver on seeded double-dam-break scenes
+(65k-262k particles), trains on the GPU with fsph_mlp_train (Adam) and
+writes the parameter blob plus its training record.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import abi, scenes
+from .abi import FsphError
+
+MODEL_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models")
+DEFAULT_MODEL = os.path.join(MODEL_DIR, "warmstart_mlp.npz")
+
+NI, NH, NO = abi.MLP_FEATURES, abi.MLP_HIDDEN, abi.MLP_OUTPUTS
+O_MU, O_SIG = 0, NI
+O_W1 = 2 * NI
+O_B1 = O_W1 + NI * NH
+O_W2 = O_B1 + NH
+O_B2 = O_W2 + NH * NH
+O_W3 = O_B2 + NH
+O_B3 = O_W3 + NH * NO
+O_SCALE = O_B3 + NO
+assert O_SCALE + 1 == abi.MLP_BLOB_SIZE
+
+
+def init_blob(features: np.ndarray, targets: np.ndarray, seed: int = 0) -> np.ndarray:
+    """Standardisation from the data, output scale = target std, He-initialised weights."""
+    rng = np.random.default_rng(seed)
+    b = np.zeros(abi.MLP_BLOB_SIZE, np.float32)
+    b[O_MU:O_SIG] = features.mean(0)
+    b[O_SIG:O_W1] = np.maximum(features.std(0), 1e-6)
+    b[O_W1:O_B1] = (rng.standard_normal((NI, NH)) * math.sqrt(2.0 / NI)).ravel()
+    b[O_W2:O_B2] = (rng.standard_normal((NH, NH)) * math.sqrt(2.0 / NH)).ravel()
+    b[O_W3:O_B3] = (rng.standard_normal((NH, NO)) * math.sqrt(1.0 / NH)).ravel()
+    b[O_SCALE] = max(float(targets.std()), 1e-6)
+    return b
+
+
+class WarmStartNet:
+    """fsph_mlp: the network and its GPU trainer (device buffers through torch)."""
+
+    def __init__(self, blob: np.ndarray | None = None):
+        self.L = abi.lib()
+        self.h = ctypes.c_void_p()
+        st = self.L.fsph_mlp_create(ctypes.byref(self.h))
+        if st != abi.OK:
+            raise FsphError(st, "fsph_mlp_create")
+        if blob is not None:
+            self.set_blob(blob)
+
+    def close(self):
+        if self.h and self.h.value:
+            self.L.fsph_mlp_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        if st != abi.OK:
+            raise FsphError(st, f"{what}: {self.L.fsph_mlp_last_error(self.h).decode()}")
+
+    def set_blob(self, blob):
+        b = np.ascontiguousarray(blob, dtype=np.float32)
+        assert b.size == abi.MLP_BLOB_SIZE
+        self._check(self.L.fsph_mlp_set_blob(self.h, b.ctypes.data_as(ctypes.c_void_p)), "set_blob")
+
+    def get_blob(self) -> np.ndarray:
+        b = np.zeros(abi.MLP_BLOB_SIZE, np.float32)
+        self._check(self.L.fsph_mlp_get_blob(self.h, b.ctypes.data_as(ctypes.c_void_p)), "get_blob")
+        return b
+
+    def forward(self, x: np.ndarray) -> np.ndarray:
+        import torch
+        xd = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+        yd = torch.empty((x.shape[0], NO), dtype=torch.float32, device="cuda")
+        self._check(self.L.fsph_mlp_forward(self.h, ctypes.c_void_p(xd.data_ptr()), x.shape[0],
+                                            ctypes.c_void_p(yd.data_ptr()), None), "forward")
+        return yd.cpu().numpy()
+
+    def gradient(self, x: np.ndarray, t: np.ndarray):
+        import torch
+        xd = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+        td = torch.from_numpy(np.ascontiguousarray(t, np.float32)).cuda()
+        g = np.zeros(abi.MLP_BLOB_SIZE, np.float32)
+        loss = ctypes.c_float(0)
+        self._check(self.L.fsph_mlp_gradient(self.h, ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(td.data_ptr()),
+                                             x.shape[0], g.ctypes.data_as(ctypes.c_void_p), ctypes.byref(loss)),
+                    "gradient")
+        return g, float(loss.value)
+
+    def train(self, x: np.ndarray, t: np.ndarray, epochs: int, batch: int = 8192, lr: float = 1e-3,
+              seed: int = 0, lr_decay: float = 0.85) -> list[float]:
+        """Adam over shuffled minibatches, one epoch per fsph_mlp_train call;
+        the blob's Adam state persists across epochs, the rate decays per epoch."""
+        import torch
+        xd = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
+        td = torch.from_numpy(np.ascontiguousarray(t, np.float32)).cuda()
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(seed)
+        hist = []
+        for ep in range(epochs):
+            perm = torch.randperm(x.shape[0], device="cuda", generator=gen)
+            xs, ts = xd[perm].contiguous(), td[perm].contiguous()
+            out = np.zeros(1, np.float32)
+            self._check(self.L.fsph_mlp_train(self.h, ctypes.c_void_p(xs.data_ptr()), ctypes.c_void_p(ts.data_ptr()),
+                                              x.shape[0], batch, 1, ctypes.c_float(lr * lr_decay ** ep),
+                                              out.ctypes.data_as(ctypes.c_void_p)), "train")
+            hist.append(float(out[0]))
+        return hist
+
+
+def save_model(path: str, blob: np.ndarray, meta: dict) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    np.savez_compressed(path, blob=np.asarray(blob, np.float32), meta=json.dumps(meta))
+
+
+def load_model(path: str = DEFAULT_MODEL):
+    d = np.load(path)
+    return d["blob"].astype(np.float32), json.loads(str(d["meta"]))
+
+
+def collect_rollout(block, seed: int, steps: int, per_step: int, skip: int = 5, rng=None):
+    """Plain-solver rollout of a double dam break with feature collection:
+    (features before a step, correction / h that step needed) for a random
+    subset of particles of every step after the first `skip`."""
+    from .particles import rxPBDSPH
+    sc = scenes.pbf_double_dam_break(block=block, seed=seed)
+    p = sc.params
+    p.clamp_constraint = 1
+    p.eta = 1e-3
+    p.max_iter = 400
+    p.collect_features = 1
+    ps = rxPBDSPH(p)
+    ps.Set(sc.pos, sc.vel)
+    rng = rng or np.random.default_rng(seed)
+    X, T, iters = [], [], []
+    feats = None
+    for s in range(steps):
+        if s > 0:
+            feats = ps.GetArrayVBO(abi.FSPH_FEATURES).reshape(sc.n, NI)
+        ps.Update(sc.dt)
+        iters.append(ps.last_stats.iterations)
+        if feats is not None and s >= skip:
+            d = ps.GetArrayVBO(abi.RX_STEP_CORRECTION)[:, :3] / p.h
+            idx = rng.choice(sc.n, size=min(per_step, sc.n), replace=False)
+            X.append(feats[idx])
+            T.append(d[idx])
+    ps.close()
+    return np.concatenate(X), np.concatenate(T), iters
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=DEFAULT_MODEL)
+    ap.add_argument("--rollouts", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=160)
+    ap.add_argument("--per-step", type=int, default=256)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--batch", type=int, default=8192)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    args = ap.parse_args()
+    t0 = time.time()
+    rng = np.random.default_rng(12345)
+    X, T = [], []
+    blocks = []
+    for r in range(args.rollouts):
+        # 65k..262k particles: two blocks of bx x bx x 2bx with bx in 20..32
+        bx = int(rng.integers(20, 33))
+        by = int(rng.integers(max(8, bx // 2), bx + 1))
+        blocks.append((bx, by, 2 * bx))
+        x, t, _ = collect_rollout((bx, by, 2 * bx), seed=1000 + r, steps=args.steps, per_step=args.per_step, rng=rng)
+        X.append(x)
+        T.append(t)
+    X = np.concatenate(X).astype(np.float32)
+    T = np.concatenate(T).astype(np.float32)
+    t_collect = time.time() - t0
+    blob = init_blob(X, T)
+    net = WarmStartNet(blob)
+    hist = net.train(X, T, epochs=args.epochs, batch=args.batch, lr=args.lr)
+    blob = net.get_blob()
+    meta = dict(samples=int(X.shape[0]), rollouts=args.rollouts, steps=args.steps, per_step=args.per_step,
+                epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
+                train_s=time.time() - t0 - t_collect, target_var=float((T / blob[O_SCALE]).var() * 3),
+                blocks=blocks[:8])
+    save_model(args.out, blob, meta)
+    print(json.dumps({k: v for k, v in meta.items() if k != "blocks"}))
+
+
+if __name__ == "__main__":
+    main()

@@ -80,8 +80,10 @@ typedef enum fsph_array {
     FSPH_PREDICT_VEL = 9,     /* float4, PBF v* */
     FSPH_SCALING_FACTOR = 10, /* float, PBF lambda */
     FSPH_CORRECTION = 11,     /* float4, PBF delta-p of the last iteration */
+    FSPH_STEP_CORRECTION = 12,/* float4, x*_final - x*_predicted of the last step (warm start / collect) */
     FSPH_VORTICITY = 18,      /* float4, omega of the last finalize pass */
-    FSPH_SORTED_ID = 64       /* int, device order -> particle index (device_ptr only) */
+    FSPH_SORTED_ID = 64,      /* int, device order -> particle index (device_ptr only) */
+    FSPH_FEATURES = 65        /* FSPH_MLP_FEATURES floats per particle: warm-start features for the next step */
 } fsph_array;
 
 /* Solver parameters.  Mirrors rxSPHEnviroment (rx_sph.h:95-182) after the
@@ -115,12 +117,15 @@ typedef struct fsph_params {
                                 inside a step only when a particle moved more than
                                 cell_skin * h since the last build */
     int use_graph;           /* 1: capture the step (with a device-side while loop) in a CUDA graph */
-    int warm_start;          /* 0: plain; 1: learned MLP warm start of the PBF iterations */
+    int warm_start;          /* 0: plain; 1: learned MLP warm start of the PBF iterations
+                                (needs fsph_set_warm_start_model) */
     int clamp_constraint;    /* 0: C = rho/rho0 - 1 as the reference (rx_sph_pbd.cpp:751);
                                 1: unilateral C = max(rho/rho0 - 1, 0) (opt-in, not the reference) */
     int walk_cells;          /* 0: PBF passes read per-particle neighbour lists built with
                                 each grid (radius = cell width); 1: walk the 27 cells every pass */
-    int reserved[5];
+    int collect_features;    /* 1: compute FSPH_FEATURES / FSPH_STEP_CORRECTION every step even
+                                without a warm start (training-data collection) */
+    int reserved[4];
 } fsph_params;
 
 /* Scene description in the reference's own terms (rxSPHEnviroment). */
@@ -249,6 +254,37 @@ int fsph_sph_eval_forces(fsph_ctx *ctx, const float *pos4, const float *vel4, in
  *     host threads) race: order them on one stream or synchronise between them. */
 int fsph_pbf_eval_lambda_noalloc(const fsph_params *params, const float *pos4, int n, float *dens,
                                  float *lambda, void *stream);
+
+/* ---- learned warm start ---- */
+/* The network: FSPH_MLP_FEATURES -> 64 -> 64 -> 3, ReLU, BF16 tensor-core
+ * arithmetic with FP32 accumulation.  Its parameters are one FP32 blob of
+ * FSPH_MLP_BLOB_SIZE floats: mu[16], sigma[16] (input standardisation),
+ * W1[16][64], b1[64], W2[64][64], b2[64], W3[64][3], b3[3], out_scale[1].
+ * Output = (network of (x - mu) / sigma) * out_scale = predicted step
+ * correction / h.  No counterpart in the reference (its PBF loop always
+ * starts from the prediction, rx_sph_pbd.cpp:418-425). */
+#define FSPH_MLP_FEATURES 16
+#define FSPH_MLP_HIDDEN 64
+#define FSPH_MLP_OUTPUTS 3
+#define FSPH_MLP_BLOB_SIZE 5476
+typedef struct fsph_mlp fsph_mlp;
+int fsph_mlp_create(fsph_mlp **out);
+int fsph_mlp_destroy(fsph_mlp *m);
+int fsph_mlp_set_blob(fsph_mlp *m, const float *blob);            /* host blob; resets Adam */
+int fsph_mlp_get_blob(fsph_mlp *m, float *blob);                  /* host blob */
+const char *fsph_mlp_last_error(const fsph_mlp *m);
+/* y[n][3] = network(x[n][16]); device pointers; stream NULL = synchronous */
+int fsph_mlp_forward(fsph_mlp *m, const float *x, int n, float *y, void *stream);
+/* gradient of the mean squared error mean_i sum_k (y_ik - t_ik)^2 w.r.t. the
+ * blob (host, FSPH_MLP_BLOB_SIZE floats; zero for mu, sigma, out_scale);
+ * x, t device pointers; *loss receives the loss. Synchronous. */
+int fsph_mlp_gradient(fsph_mlp *m, const float *x, const float *t, int n, float *grad, float *loss);
+/* Adam (beta 0.9 / 0.999) over `epochs` passes of consecutive minibatches of
+ * `batch` rows of (x, t) (device pointers); loss_per_epoch (host, optional). */
+int fsph_mlp_train(fsph_mlp *m, const float *x, const float *t, int n, int batch, int epochs, float lr,
+                   float *loss_per_epoch);
+/* Install a trained blob (host) as the context's warm-start network. */
+int fsph_set_warm_start_model(fsph_ctx *ctx, const float *blob);
 
 /* ---- measurement ---- */
 typedef enum fsph_pass {

@@ -788,10 +788,15 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
     FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
     FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
     FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    /* the warm-start history (step corrections, features) follows the particles */
+    launch_unsort4(n, c->set[0].id, c->dstep, c->tmp4, 0, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, c->tmp4, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    {
+        float4 *tf = reinterpret_cast<float4 *>(c->nl.list); /* lists are rebuilt by every step */
+        launch_unsort_rows(n, c->set[0].id, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->feat, tf, (size_t)n * kFeatures * 4, cudaMemcpyDeviceToDevice, s));
+    }
     launch_iota(n, c->set[0].id, s);
-    /* the step history of the warm start no longer matches the particles */
-    FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, (size_t)n * 16, s));
-    FSPH_CUDA(c, cudaMemsetAsync(c->warm_valid, 0, sizeof(unsigned int), s));
     cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (type == FSPH_POSITION)
         FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos + start, data, (size_t)count * 16, k, s));

@@ -385,8 +385,9 @@ void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
             fo.ctl = c->ctl;
             fo.valid = c->warm_valid;
         }
-        launch_xsph_vort(p, c->cell_start, c->set[0].pos, c->set[0].vel, c->dens, c->set[1].vel, c->vort, fo, s);
-        launch_vort_apply(p, c->cell_start, c->set[0].pos, c->vort, c->dens, c->set[1].vel, c->set[0].vel, s);
+        launch_xsph_vort(p, c->cell_start, c->set[0].pos, c->set[0].vel, c->dens, c->set[1].vel, c->vort, fo, c->nl,
+                         s);
+        launch_vort_apply(p, c->cell_start, c->set[0].pos, c->vort, c->dens, c->set[1].vel, c->set[0].vel, c->nl, s);
     }
 }
 

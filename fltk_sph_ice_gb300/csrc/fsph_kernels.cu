@@ -271,11 +271,18 @@ __global__ void k_build_list(DevParams p, const unsigned int *__restrict__ cell_
         const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
         const unsigned int s = __ldg(cell_start + base - 1), e = __ldg(cell_start + base + 2);
         if (e - s > 4095u) ovf = true;
-        for (unsigned int j = s; j < e; ++j) {
-            float3 d = xi - f3(__ldg(xb + j));
-            if (dot3(d, d) < p.rl2) {
-                if (k < kListMax) list[(size_t)k * p.n + i] = (unsigned short)((r << 12) | (j - s));
-                ++k;
+        /* four candidates' loads in flight before their tests */
+        for (unsigned int j0 = s; j0 < e; j0 += 4) {
+            float4 xc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xc[u] = __ldg(xb + min(j0 + u, e - 1));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float3 d = xi - f3(xc[u]);
+                if (j0 + u < e && dot3(d, d) < p.rl2) {
+                    if (k < kListMax) list[(size_t)k * p.n + i] = (unsigned short)((r << 12) | (j0 + u - s));
+                    ++k;
+                }
             }
         }
     }
@@ -417,19 +424,17 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned i
         for_each_candidate(
             p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return pp[j]; },
             [&](unsigned int, const float4 &xj4) {
+                /* branch-free: outside h both q and t clamp to zero; the self
+                 * pair (d = 0) adds W(0) to the density and nothing else */
                 const float3 d = xi - f3(xj4);
                 const float r2 = dot3(d, d);
-                if (r2 < p.h2) {
-                    const float q = p.h2 - r2;
-                    wsum += q * q * q;
-                    if (r2 > 0.0f) {
-                        const float inv_r = rsqrtf(r2);
-                        const float t = p.h - r2 * inv_r;
-                        const float g = agr * t * t * inv_r; /* grad W / rho0 = g d */
-                        gs = gs + g * d;
-                        sd += g * g * r2;
-                    }
-                }
+                const float q = fmaxf(p.h2 - r2, 0.0f);
+                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+                const float g = agr * t * t * inv_r; /* grad W / rho0 = g d */
+                wsum += q * q * q;
+                gs = gs + g * d;
+                sd += g * g * r2;
             });
         float rho = p.mass * p.aw * wsum;
         sd += dot3(gs, gs);
@@ -529,21 +534,20 @@ __global__ void __launch_bounds__(kBlock) k_correction(DevParams p, const unsign
         for_each_candidate(
             p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(src + j); },
             [&](unsigned int, const float4 &xj4) {
+                /* branch-free: t = 0 outside h and d = 0 for the self pair */
                 const float3 d = xi - f3(xj4);
                 const float r2 = dot3(d, d);
-                if (r2 < p.h2 && r2 > 0.0f) {
-                    const float inv_r = rsqrtf(r2);
-                    const float t = p.h - r2 * inv_r;
-                    const float g = agr * t * t * inv_r;
-                    float sc = 0.0f;
-                    if (p.use_ap) {
-                        const float q = p.h2 - r2;
-                        const float ww = awq * q * q * q;
-                        const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
-                        sc = k_dt2 * pw;
-                    }
-                    acc = acc + ((li + xj4.w + sc) * g) * d;
+                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+                const float g = agr * t * t * inv_r;
+                float sc = 0.0f;
+                if (p.use_ap) {
+                    const float q = fmaxf(p.h2 - r2, 0.0f);
+                    const float ww = awq * q * q * q;
+                    const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
+                    sc = k_dt2 * pw;
                 }
+                acc = acc + ((li + xj4.w + sc) * g) * d;
             });
         if (dp_out) dp_out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
         float3 xn = wall_project(xi + acc, p);
@@ -618,44 +622,42 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
 
 /* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), and the
  * XSPH update v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij. */
-__global__ void k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_start,
-                            const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-                            const float *__restrict__ dens, float4 *__restrict__ vel_out,
-                            float4 *__restrict__ vort, FeatureOut fo) {
+__global__ void __launch_bounds__(kBlock) k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                      const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                                                      const float *__restrict__ dens, float4 *__restrict__ vel_out,
+                                                      float4 *__restrict__ vort, FeatureOut fo,
+                                                      const unsigned short *__restrict__ list,
+                                                      const unsigned char *__restrict__ cnt,
+                                                      const unsigned int *__restrict__ cellb) {
+    __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    float3 xi = f3(pos[i]), vi = f3(vel[i]);
-    int3 c = cell_of(xi, p);
+    const float3 xi = f3(pos[i]), vi = f3(vel[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), xs = make_float3(0.f, 0.f, 0.f);
     float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
-    float div = 0.f, cntf = 1.f; /* self */
-    for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy) {
-            unsigned int s, e;
-            row_range(cell_start, c, dy, dz, p, s, e);
-            for (unsigned int j = s; j < e; ++j) {
-                if (j == (unsigned int)i) continue;
-                float3 d = xi - f3(__ldg(pos + j));
-                float r2 = dot3(d, d);
-                if (r2 < p.h2 && r2 > 0.0f) {
-                    float r = sqrtf(r2);
-                    float t = p.h - r;
-                    float g = p.ag * t * t / r;
-                    float3 vij = f3(__ldg(vel + j)) - vi;
-                    om = om + cross3(vij, (-g) * d);
-                    float q = p.h2 - r2;
-                    float mrho = p.mass / __ldg(dens + j);
-                    float w = p.aw * q * q * q * mrho;
-                    xs = xs + w * vij;
-                    if (fo.feat) {
-                        cntf += 1.0f;
-                        off = off - d;
-                        div += mrho * g * dot3(vij, d);
-                        cg = cg + (mrho * g) * d;
-                    }
-                }
-            }
-        }
+    float div = 0.f, cntf = 0.f;
+    /* branch-free pair terms: q and t clamp to zero outside h, and the self
+     * pair (d = 0, v_ij = 0) adds only to the neighbour count */
+    for_each_candidate(
+        p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(pos + j); },
+        [&](unsigned int j, const float4 &xj4) {
+            const float3 d = xi - f3(xj4);
+            const float r2 = dot3(d, d);
+            const float inside = r2 < p.h2 ? 1.0f : 0.0f;
+            const float q = fmaxf(p.h2 - r2, 0.0f);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float g = p.ag * t * t * inv_r;
+            const float3 vij = f3(__ldg(vel + j)) - vi;
+            const float mrho = p.mass / __ldg(dens + j);
+            om = om + cross3(vij, (-g) * d);
+            xs = xs + (p.aw * q * q * q * mrho) * vij;
+            cntf += inside;
+            off = off - inside * d;
+            div += mrho * g * dot3(vij, d);
+            cg = cg + (mrho * g) * d;
+        });
+    cntf = fmaxf(cntf, 1.0f);
     float3 vn = vi + p.xsph_c * xs;
     vel_out[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
     vort[i] = make_float4(om.x, om.y, om.z, 0.0f);
@@ -682,37 +684,36 @@ __global__ void k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_s
 
 /* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
  * v_i <- v_i + dt f. */
-__global__ void k_vort_apply(DevParams p, const unsigned int *__restrict__ cell_start,
-                             const float4 *__restrict__ pos, const float4 *__restrict__ vort,
-                             const float *__restrict__ dens, const float4 *__restrict__ vel_in,
-                             float4 *__restrict__ vel_out) {
+__global__ void __launch_bounds__(kBlock) k_vort_apply(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                       const float4 *__restrict__ pos,
+                                                       const float4 *__restrict__ vort,
+                                                       const float *__restrict__ dens,
+                                                       const float4 *__restrict__ vel_in,
+                                                       float4 *__restrict__ vel_out,
+                                                       const unsigned short *__restrict__ list,
+                                                       const unsigned char *__restrict__ cnt,
+                                                       const unsigned int *__restrict__ cellb) {
+    __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     float4 v4 = vel_in[i];
     if (p.vort_eps != 0.0f) {
-        float3 xi = f3(pos[i]);
-        float3 wi = f3(vort[i]);
-        float wmi = sqrtf(dot3(wi, wi));
-        int3 c = cell_of(xi, p);
+        const float3 xi = f3(pos[i]);
+        const float3 wi = f3(vort[i]);
+        const float wmi = sqrtf(dot3(wi, wi));
         float3 eta = make_float3(0.f, 0.f, 0.f);
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy) {
-                unsigned int s, e;
-                row_range(cell_start, c, dy, dz, p, s, e);
-                for (unsigned int j = s; j < e; ++j) {
-                    if (j == (unsigned int)i) continue;
-                    float3 d = xi - f3(__ldg(pos + j));
-                    float r2 = dot3(d, d);
-                    if (r2 < p.h2 && r2 > 0.0f) {
-                        float r = sqrtf(r2);
-                        float t = p.h - r;
-                        float g = p.ag * t * t / r;
-                        float3 wj = f3(__ldg(vort + j));
-                        float k = p.mass / __ldg(dens + j) * (sqrtf(dot3(wj, wj)) - wmi) * g;
-                        eta = eta + k * d;
-                    }
-                }
-            }
+        for_each_candidate(
+            p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(pos + j); },
+            [&](unsigned int j, const float4 &xj4) {
+                const float3 d = xi - f3(xj4);
+                const float r2 = dot3(d, d);
+                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+                const float g = p.ag * t * t * inv_r;
+                const float3 wj = f3(__ldg(vort + j));
+                const float k = p.mass / __ldg(dens + j) * (sqrtf(dot3(wj, wj)) - wmi) * g;
+                eta = eta + k * d;
+            });
         float en = sqrtf(dot3(eta, eta));
         if (en > 1e-30f) {
             float3 N = (1.0f / en) * eta;
@@ -998,12 +999,15 @@ void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos
                                                   attr_a, xpred, dstep);
 }
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                      const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, cudaStream_t s) {
-    k_xsph_vort<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort, fo);
+                      const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, const NbrLists &nl,
+                      cudaStream_t s) {
+    k_xsph_vort<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort, fo,
+                                                   p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
-                       const float *dens, const float4 *vel_in, float4 *vel_out, cudaStream_t s) {
-    k_vort_apply<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vort, dens, vel_in, vel_out);
+                       const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s) {
+    k_vort_apply<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vort, dens, vel_in, vel_out,
+                                                    p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
 void launch_sph_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
                         float *pres, cudaStream_t s) {

@@ -81,9 +81,10 @@ void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos
                      cudaStream_t s);
 /* XSPH + vorticity (omega) pass; with fo.feat also the warm-start features */
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                      const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, cudaStream_t s);
+                      const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, const NbrLists &nl,
+                      cudaStream_t s);
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
-                       const float *dens, const float4 *vel_in, float4 *vel_out, cudaStream_t s);
+                       const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s);
 
 /* ---- WCSPH ---- */
 void launch_sph_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,

@@ -124,7 +124,8 @@ class FsphStepStats(ctypes.Structure):
         ("density_error_two_sided", ctypes.c_float),
         ("density_error_max", ctypes.c_float),
         ("status", ctypes.c_int),
-        ("reserved", ctypes.c_int * 3),
+        ("kernels", ctypes.c_int),
+        ("reserved", ctypes.c_int * 2),
     ]
 
 

@@ -79,6 +79,9 @@ struct fsph_ctx {
     bool graph_valid = false;
     float graph_dt = 0.0f;
     int graph_n = -1;
+    /* kernel nodes of the step graph: outside the loop, per iteration, per grid rebuild */
+    int k_top = 0, k_iter = 0, k_rebuild = 0;
+    bool last_step_graph = false;
     bool stats_pending = false;
     std::string err;
 };
@@ -424,6 +427,20 @@ int add_conditional(fsph_ctx *c, cudaGraph_t g, const cudaGraphNode_t *deps, siz
     return FSPH_OK;
 }
 
+/* kernel nodes directly in g (conditional bodies are separate graphs) */
+int kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return 0;
+    std::vector<cudaGraphNode_t> v(n);
+    if (n && cudaGraphGetNodes(g, v.data(), &n) != cudaSuccess) return 0;
+    int k = 0;
+    for (cudaGraphNode_t nd : v) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}
+
 /* Capture one PBF step into a graph:
  *   pre-pass -> WHILE(h_while){ IF(h_rb){rebuild}; lambda; correction }
  *            -> [IF(h_rb2){rebuild}] -> finalize (+ XSPH / vorticity)      */
@@ -477,6 +494,9 @@ int build_pbf_graph(fsph_ctx *c, const DevParams &p) {
     }
     enqueue_pbf_post(c, p, it, s);
     FSPH_CUDA(c, cudaStreamEndCapture(s, &g));
+    c->k_top = kernel_nodes(g);
+    c->k_iter = kernel_nodes(wbody);
+    c->k_rebuild = kernel_nodes(ibody);
     FSPH_CUDA(c, cudaGraphInstantiate(&c->gexec, g, 0));
     c->graph_valid = true;
     c->graph_dt = p.dt;
@@ -517,6 +537,8 @@ void fill_stats(fsph_ctx *c, fsph_step_stats *st) {
     st->density_error_max = h.errmax;
     st->density_error = c->P.error_mode ? h.err2 : h.err1;
     st->status = FSPH_OK;
+    if (c->last_step_graph) /* every grid build after the first is one run of the rebuild body */
+        st->kernels = c->k_top + (int)h.iter * c->k_iter + ((int)h.builds - 1) * c->k_rebuild;
     if (c->P.solver == FSPH_SOLVER_PBF) {
         if (h.nan_flag) st->status = FSPH_NAN_DETECTED;
         else if (st->density_error > c->P.eta) st->status = FSPH_NOT_CONVERGED;
@@ -826,6 +848,7 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
         return fail(c, FSPH_UNSUPPORTED, "warm_start = 1 needs a network (fsph_set_warm_start_model)");
     DevParams p = make_dev(c->P, c->n, dt);
     c->dp = p;
+    c->last_step_graph = c->P.solver == FSPH_SOLVER_PBF && c->P.use_graph;
     if (c->P.solver == FSPH_SOLVER_WCSPH) {
         FSPH_TRY(sph_step(c, p));
     } else if (c->P.use_graph) {

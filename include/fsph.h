@@ -152,7 +152,8 @@ typedef struct fsph_step_stats {
     float density_error_two_sided;
     float density_error_max;      /* max_i |rho_i - rho0| / rho0 */
     int status;                   /* FSPH_OK, FSPH_NOT_CONVERGED, FSPH_NAN_DETECTED */
-    int reserved[3];
+    int kernels;                  /* kernel launches the step executed (PBF graph mode; 0 = not counted) */
+    int reserved[2];
 } fsph_step_stats;
 
 typedef struct fsph_ctx fsph_ctx;

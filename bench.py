@@ -283,6 +283,25 @@ def run_leg(ctx, warm: bool, blob):
                     "iterations": iters, "kernels": int(sum(kernels))}
 
 
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_lambda_k_correction_pbf_double_dam_break_1M.md")
+
+
+def ncu_traffic(kname: str):
+    """DRAM bytes (read + write) of one launch of kname at 1M particles, from
+    the committed ncu summary's 'traffic per launch' row; None if absent."""
+    import re
+    if not os.path.isfile(TRAFFIC_PROFILE):
+        return None
+    with open(TRAFFIC_PROFILE) as f:
+        for line in f:
+            if line.startswith("| **traffic per launch**"):
+                mb = [float(x) for x in re.findall(r"([0-9.]+) MB", line)]
+                col = {"k_lambda": 0, "k_correction": 1}.get(kname)
+                if col is not None and len(mb) == 2:
+                    return mb[col] * 1e6
+    return None
+
+
 def roofline_of(L, abi, ps, n, mean_iters):
     t_lam, t_cor, t_grid = ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0)
     L.fsph_time_pass(ps.handle, abi.PASS_LAMBDA, 20, ctypes.byref(t_lam))
@@ -294,13 +313,7 @@ def roofline_of(L, abi, ps, n, mean_iters):
         kname, kms, kbytes = "k_lambda", t_lam.value, BYTES_LAMBDA * n
     peak, peak_kind = measured_peaks()
     achieved = kbytes / (kms / 1000.0) / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.isfile(tp):
-        with open(tp) as f:
-            tr = json.load(f)
-        if kname in tr:
-            traffic = tr[kname].get("bytes_per_launch_1M")
+    traffic = ncu_traffic(kname)
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
             "lambda_ms": t_lam.value, "correction_ms": t_cor.value, "grid_build_ms": t_grid.value,
@@ -413,6 +426,108 @@ def gpu_arm(args):
     return 0
 
 
+BATCH_METRIC = "PBF particle-steps/s, 256 batched scenes of 2k-66k particles, 4 constraint iterations"
+BATCH_PREROLL = 10
+BATCH_ITERS = 4
+# compulsory HBM bytes per particle-step of a 4-iteration step, B(I) = 396 + 60 I
+BATCH_BYTES = 396.0 + 60.0 * BATCH_ITERS
+
+
+def batched_arm(args):
+    """The batched-scenes workload: every scene of the seeded 256-scene set
+    steps together (one persistent launch per pass, the step one CUDA graph),
+    launch shape from the library's autotuner.  One JSON line on rank 0."""
+    import torch
+    from fltk_sph_ice_gb300 import PBFBatch, abi, build, scenes
+
+    rank, world, local = rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    build.build()
+    sc = scenes.batched_scenes()
+    for s in sc:
+        s.params.min_iter = BATCH_ITERS
+        s.params.max_iter = BATCH_ITERS
+    pos = np.concatenate([s.pos for s in sc])
+    vel = np.concatenate([s.vel for s in sc])
+    b = PBFBatch([s.params for s in sc], [s.n for s in sc], iterations=BATCH_ITERS)
+    b.set_particles(pos, vel)
+    n, dt = b.n, sc[0].dt
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(BATCH_PREROLL):
+        b.step(dt, sp)
+    cfg, tune_ms = b.autotune(dt, steps=3)
+    for _ in range(max(args.warmup, 3)):
+        b.step(dt, sp)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev[k][0].record(stream)
+            b.step(dt, sp)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    tot_s = sum(a.elapsed_time(c) for a, c in ev) / 1000.0
+    value, tot_s = replica_rate(n, args.steps, tot_s, dist)
+    errs = [b.scene_stats(s) for s in range(b.nscenes)]
+    # e2e: the whole batch host -> device, one step, positions and velocities back
+    x_h = torch.from_numpy(b.get(abi.RX_POSITION)).pin_memory().numpy()
+    v_h = torch.from_numpy(b.get(abi.RX_VELOCITY)).pin_memory().numpy()
+    for _ in range(2):
+        b.set_particles(x_h, v_h)
+        b.step(dt)
+        x_h[:] = b.get(abi.RX_POSITION)
+        v_h[:] = b.get(abi.RX_VELOCITY)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.set_particles(x_h, v_h)
+        b.step(dt)
+        x_h[:] = b.get(abi.RX_POSITION)
+        v_h[:] = b.get(abi.RX_VELOCITY)
+    e2e_value, _ = replica_rate(n, args.steps, time.perf_counter() - t0, dist)
+    peak, peak_kind = measured_peaks()
+    achieved = value * BATCH_BYTES / 1e9
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        small = min(sc, key=lambda s: s.n)
+        secs, kind = cpu_sample(small.pos, small.vel, small.params, BATCH_ITERS)
+        cpu = {"value": small.n / secs, "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": f"one 4-iteration PBF step of the smallest batched scene ({small.n} particles), "
+                         f"1 host thread"}
+    if rank == 0:
+        line = {
+            "metric": BATCH_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattices)",
+            "config": {"workload": "batched_256", "scenes": b.nscenes, "particles": n,
+                       "iterations": BATCH_ITERS, "preroll_steps": BATCH_PREROLL,
+                       "autotuned": {"block": cfg.block, "lanes": cfg.lanes, "cell_skin": round(cfg.cell_skin, 3),
+                                     "ms_per_step_at_tuning": tune_ms},
+                       "mean_error_one_sided": float(np.mean([e.density_error_one_sided for e in errs])),
+                       "l2": "256 MiB flush between timed steps", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "whole step",
+                         "bytes_per_particle_step": BATCH_BYTES, "peak_kind": peak_kind},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n},
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -427,12 +542,16 @@ def main():
                          "which cannot profile kernels inside graphs with conditional nodes)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched_256"],
+                    help="the headline 1M double dam break (default) or the 256-scene batch")
     args = ap.parse_args()
     if args.model is None:
         from fltk_sph_ice_gb300 import warmstart
         args.model = warmstart.DEFAULT_MODEL
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "batched_256":
+        return batched_arm(args)
     return gpu_arm(args)
 
 

@@ -11,6 +11,7 @@ sm_103a CUDA kernels behind a C ABI (include/fsph.h, libfsph.so).
 """
 from . import abi, scenes
 from .abi import FsphError
+from .batch import PBFBatch
 from .particles import rxParticleSystemBase, rxPBDSPH, rxSPH
 
-__all__ = ["abi", "scenes", "FsphError", "rxParticleSystemBase", "rxPBDSPH", "rxSPH"]
+__all__ = ["abi", "scenes", "FsphError", "PBFBatch", "rxParticleSystemBase", "rxPBDSPH", "rxSPH"]

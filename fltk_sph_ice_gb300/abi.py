@@ -21,6 +21,7 @@ SOLVER_WCSPH, SOLVER_PBF = 0, 1
 ERR_ONE_SIDED, ERR_TWO_SIDED = 0, 1
 # fsph_where
 HOST, DEVICE = 0, 1
+BOUNDARY_POSITION, BOUNDARY_VOLUME, BOUNDARY_LAMBDA = 0, 1, 2
 # fsph_array (numbering of rxParticleSystemBase::rxParticleArray, rx_ps.h:68-116)
 RX_POSITION = 0
 RX_VELOCITY = 1
@@ -81,7 +82,8 @@ class FsphParams(ctypes.Structure):
         ("clamp_constraint", ctypes.c_int),
         ("walk_cells", ctypes.c_int),
         ("collect_features", ctypes.c_int),
-        ("reserved", ctypes.c_int * 4),
+        ("compensated_density", ctypes.c_int),
+        ("reserved", ctypes.c_int * 3),
     ]
 
     def to_dict(self) -> dict:
@@ -129,6 +131,15 @@ class FsphStepStats(ctypes.Structure):
     ]
 
 
+class FsphBatchConfig(ctypes.Structure):
+    _fields_ = [
+        ("block", ctypes.c_int),
+        ("lanes", ctypes.c_int),
+        ("cell_skin", ctypes.c_float),
+        ("eager", ctypes.c_int),
+    ]
+
+
 # Every symbol include/fsph.h declares (checked by tests/test_abi.py).
 EXPORTS = [
     "fsph_abi_version", "fsph_status_string", "fsph_last_error", "fsph_params_from_env",
@@ -138,6 +149,10 @@ EXPORTS = [
     "fsph_pbf_eval_correction", "fsph_sph_eval_forces", "fsph_time_pass", "fsph_pbf_eval_lambda_noalloc",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
     "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
+    "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
+    "fsph_batch_create", "fsph_batch_destroy", "fsph_batch_last_error", "fsph_batch_num_particles",
+    "fsph_batch_offsets", "fsph_batch_set_particles", "fsph_batch_step", "fsph_batch_get_array",
+    "fsph_batch_scene_stats", "fsph_batch_set_config", "fsph_batch_get_config", "fsph_batch_autotune",
 ]
 
 # fsph_pass
@@ -185,6 +200,29 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_mlp_gradient.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, P(c_float)]
     L.fsph_mlp_train.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p]
     L.fsph_set_warm_start_model.argtypes = [c_void_p, c_void_p]
+    L.fsph_set_boundary.argtypes = [c_void_p, c_void_p, c_int, c_int]
+    L.fsph_set_boundary.restype = c_int
+    L.fsph_num_boundary.argtypes = [c_void_p]
+    L.fsph_num_boundary.restype = c_int
+    L.fsph_get_boundary.argtypes = [c_void_p, c_int, c_void_p]
+    L.fsph_get_boundary.restype = c_int
+    L.fsph_batch_create.argtypes = [c_void_p, c_void_p, c_int, c_int, P(c_void_p)]
+    L.fsph_batch_destroy.argtypes = [c_void_p]
+    L.fsph_batch_last_error.argtypes = [c_void_p]
+    L.fsph_batch_last_error.restype = c_char_p
+    L.fsph_batch_num_particles.argtypes = [c_void_p]
+    L.fsph_batch_offsets.argtypes = [c_void_p, c_void_p]
+    L.fsph_batch_set_particles.argtypes = [c_void_p, c_void_p, c_void_p, c_int]
+    L.fsph_batch_step.argtypes = [c_void_p, c_float, c_void_p]
+    L.fsph_batch_get_array.argtypes = [c_void_p, c_int, c_void_p, c_int]
+    L.fsph_batch_scene_stats.argtypes = [c_void_p, c_int, P(FsphStepStats)]
+    L.fsph_batch_set_config.argtypes = [c_void_p, P(FsphBatchConfig)]
+    L.fsph_batch_get_config.argtypes = [c_void_p, P(FsphBatchConfig)]
+    L.fsph_batch_autotune.argtypes = [c_void_p, c_float, c_int, P(FsphBatchConfig), P(c_float)]
+    for name in ["fsph_batch_create", "fsph_batch_destroy", "fsph_batch_num_particles", "fsph_batch_offsets",
+                 "fsph_batch_set_particles", "fsph_batch_step", "fsph_batch_get_array", "fsph_batch_scene_stats",
+                 "fsph_batch_set_config", "fsph_batch_get_config", "fsph_batch_autotune"]:
+        getattr(L, name).restype = c_int
     for name in ["fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob",
                  "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
                  "fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",

@@ -81,6 +81,15 @@ struct fsph_ctx {
     int graph_n = -1;
     /* kernel nodes of the step graph: outside the loop, per iteration, per grid rebuild */
     int k_top = 0, k_iter = 0, k_rebuild = 0;
+    /* static boundary particles, sorted by the cells of the fluid grid */
+    int nb = 0;
+    float4 *b_in = nullptr;            /* as given, input order */
+    float4 *b_pos = nullptr;           /* sorted; .w = rho0 psi_b / m */
+    float *b_lam = nullptr, *b_scale = nullptr;
+    float2 *b_stat = nullptr;
+    unsigned int *b_id = nullptr, *b_key = nullptr, *b_rank = nullptr;
+    unsigned int *b_count = nullptr, *b_cell = nullptr;
+    unsigned char *b_near = nullptr;
     bool last_step_graph = false;
     bool stats_pending = false;
     std::string err;
@@ -193,6 +202,7 @@ DevParams make_dev(const fsph_params &p, int n, float dt) {
     d.skin2 = (float)(skin_len * skin_len);
     d.rl2 = (float)(cw * cw);
     d.use_lists = (p.solver == FSPH_SOLVER_PBF && !p.walk_cells) ? 1 : 0;
+    d.compensated = p.compensated_density ? 1 : 0;
     d.dt = dt;
     d.inv_dt = dt != 0.0f ? 1.0f / dt : 0.0f;
     return d;
@@ -230,6 +240,34 @@ void free_grid(fsph_ctx *c) {
     cudaFree(c->count); cudaFree(c->cell_start); cudaFree(c->block_sums);
     c->count = c->cell_start = c->block_sums = nullptr;
     c->ncells = 0;
+}
+
+void free_boundary(fsph_ctx *c) {
+    cudaFree(c->b_in); cudaFree(c->b_pos); cudaFree(c->b_lam); cudaFree(c->b_scale); cudaFree(c->b_stat);
+    cudaFree(c->b_id); cudaFree(c->b_key); cudaFree(c->b_rank); cudaFree(c->b_count); cudaFree(c->b_cell);
+    cudaFree(c->b_near);
+    c->b_in = c->b_pos = nullptr;
+    c->b_lam = c->b_scale = nullptr;
+    c->b_stat = nullptr;
+    c->b_id = c->b_key = c->b_rank = c->b_count = c->b_cell = nullptr;
+    c->b_near = nullptr;
+    c->nb = 0;
+}
+
+/* The boundary's fields of the device parameters (none when nb == 0). */
+void attach_boundary(const fsph_ctx *c, DevParams &p) {
+    p.nb = c->nb;
+    p.bpos = c->b_pos;
+    p.blam = c->b_lam;
+    p.bcell = c->b_cell;
+    p.bnear = c->b_near;
+}
+
+/* device parameters of the context for n particles */
+DevParams dev_for(const fsph_ctx *c, int n, float dt) {
+    DevParams p = make_dev(c->P, n, dt);
+    attach_boundary(c, p);
+    return p;
 }
 
 void drop_graph(fsph_ctx *c) {
@@ -292,6 +330,39 @@ int alloc_grid(fsph_ctx *c) {
     FSPH_CUDA(c, cudaMemsetAsync(c->count, 0, (size_t)nc * sizeof(unsigned int), c->stream));
     c->ncells = nc;
     std::memcpy(c->gdim, g, sizeof(g));
+    return FSPH_OK;
+}
+
+/* Sort the static boundary by the cells of the current grid and derive its
+ * per-cell table, volumes and static lambda_b parts (after every grid
+ * (re)allocation). */
+int boundary_build(fsph_ctx *c) {
+    if (c->nb == 0) return FSPH_OK;
+    cudaStream_t s = c->stream;
+    cudaFree(c->b_count); cudaFree(c->b_cell); cudaFree(c->b_near);
+    c->b_count = c->b_cell = nullptr;
+    c->b_near = nullptr;
+    FSPH_TRY(dalloc(c, &c->b_count, c->ncells));
+    FSPH_TRY(dalloc(c, &c->b_cell, (size_t)c->ncells + 1));
+    FSPH_TRY(dalloc(c, &c->b_near, c->ncells));
+    FSPH_CUDA(c, cudaMemsetAsync(c->b_count, 0, (size_t)c->ncells * sizeof(unsigned int), s));
+    DevParams p = make_dev(c->P, c->nb, 1.0f); /* n = the boundary count */
+    launch_hash(p, c->b_in, c->b_key, c->b_rank, c->b_count, s);
+    launch_scan(c->b_count, c->b_cell, c->block_sums, c->ncells, s);
+    launch_scatter_sort(p, c->b_key, c->b_rank, c->b_cell, c->b_id, c->ncells, s); /* b_id: slot -> input */
+    Gather g{};
+    g.n4 = 1;
+    g.src4[0] = c->b_in;
+    g.dst4[0] = c->b_pos;
+    launch_gather(c->nb, c->b_id, g, nullptr, s);
+    attach_boundary(c, p);
+    launch_boundary_near(p, c->ncells, c->b_near, s);
+    launch_boundary_volume(p, c->b_scale, s);
+    launch_pack_w(c->nb, c->b_pos, c->b_scale, s);
+    launch_boundary_static(p, c->b_stat, s);
+    FSPH_CUDA(c, cudaMemsetAsync(c->b_lam, 0, (size_t)c->nb * sizeof(float), s));
+    FSPH_CUDA(c, cudaGetLastError());
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
     return FSPH_OK;
 }
 
@@ -399,6 +470,7 @@ int pbf_step_eager(fsph_ctx *c, const DevParams &p) {
     int it = enqueue_pbf_pre(c, p, s);
     for (int k = 0;; ++k) {
         launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
+        launch_boundary_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->ctl, c->b_stat, c->b_lam, s);
         launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, 0ull, 0ull, 0,
                           nullptr, c->nl, s);
         FSPH_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, s));
@@ -478,6 +550,7 @@ int build_pbf_graph(fsph_ctx *c, const DevParams &p) {
     if (ext) FSPH_CUDA(c, cudaGraphConditionalHandleCreate(&hrb2, capg, 0, cudaGraphCondAssignDefault));
     FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(c->s2, wbody, &inode, nullptr, 1, cudaStreamCaptureModeRelaxed));
     launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, hw, 1, c->nl, c->s2);
+    launch_boundary_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->ctl, c->b_stat, c->b_lam, c->s2);
     launch_correction(p, c->cell_start, c->ppos[0], c->ppos[1], c->xb, c->ctl, c->dpart, hrb, hrb2, ext ? 3 : 1,
                       nullptr, c->nl, c->s2);
     FSPH_CUDA(c, cudaStreamEndCapture(c->s2, &wbody));
@@ -730,6 +803,7 @@ int fsph_destroy(fsph_ctx *c) {
     drop_graph(c);
     free_particles(c);
     free_grid(c);
+    free_boundary(c);
     cudaFree(c->ctl);
     if (c->ctl_host) cudaFreeHost(c->ctl_host);
     cudaFree(c->flag);
@@ -766,6 +840,7 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
         FSPH_TRY(load_particles(c, (const float *)hp.data(), (const float *)hv.data(), n, FSPH_HOST));
     }
     FSPH_TRY(alloc_grid(c));
+    FSPH_TRY(boundary_build(c)); /* the boundary's cell table follows the grid */
     FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
     return FSPH_OK;
 }
@@ -846,7 +921,7 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
     }
     if (c->P.solver == FSPH_SOLVER_PBF && c->P.warm_start == 1 && !c->model_loaded)
         return fail(c, FSPH_UNSUPPORTED, "warm_start = 1 needs a network (fsph_set_warm_start_model)");
-    DevParams p = make_dev(c->P, c->n, dt);
+    DevParams p = dev_for(c, c->n, dt);
     c->dp = p;
     c->last_step_graph = c->P.solver == FSPH_SOLVER_PBF && c->P.use_graph;
     if (c->P.solver == FSPH_SOLVER_WCSPH) {
@@ -978,7 +1053,7 @@ int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long 
     int n = c->n;
     *total = 0;
     if (n == 0) { offsets[0] = 0; return FSPH_OK; }
-    DevParams p = make_dev(c->P, n, 1.0f);
+    DevParams p = dev_for(c, n, 1.0f);
     cudaStream_t s = c->stream;
     FSPH_TRY(build_on(c, p, c->set[0].pos));
     unsigned int *cnt = c->rank;
@@ -1036,11 +1111,63 @@ int fsph_set_warm_start_model(fsph_ctx *c, const float *blob) {
     return FSPH_OK;
 }
 
+int fsph_set_boundary(fsph_ctx *c, const float *bpos4, int nb, int where) {
+    if (!c || nb < 0 || (nb > 0 && !bpos4)) return FSPH_INVALID_ARG;
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    if (nb > 0 && c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "boundary particles: PBF only");
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    free_boundary(c);
+    drop_graph(c);
+    if (nb == 0) return FSPH_OK;
+    const size_t n = (size_t)nb;
+    FSPH_TRY(dalloc(c, &c->b_in, n)); FSPH_TRY(dalloc(c, &c->b_pos, n));
+    FSPH_TRY(dalloc(c, &c->b_lam, n)); FSPH_TRY(dalloc(c, &c->b_scale, n)); FSPH_TRY(dalloc(c, &c->b_stat, n));
+    FSPH_TRY(dalloc(c, &c->b_id, n)); FSPH_TRY(dalloc(c, &c->b_key, n)); FSPH_TRY(dalloc(c, &c->b_rank, n));
+    cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    FSPH_CUDA(c, cudaMemcpyAsync(c->b_in, bpos4, n * sizeof(float4), k, c->stream));
+    FSPH_CUDA(c, cudaMemsetAsync(c->flag, 0, sizeof(unsigned int), c->stream));
+    launch_check_finite(nb, c->b_in, nullptr, c->flag, c->stream);
+    FSPH_CUDA(c, cudaMemcpyAsync(c->flag_host, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream));
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (*c->flag_host) {
+        free_boundary(c);
+        return fail(c, FSPH_NAN_DETECTED, "non-finite boundary position");
+    }
+    c->nb = nb;
+    return boundary_build(c);
+}
+
+int fsph_get_boundary(fsph_ctx *c, int which, float *dst) {
+    if (!c || !dst) return FSPH_INVALID_ARG;
+    const int nb = c->nb;
+    if (nb == 0) return FSPH_OK;
+    cudaStream_t s = c->stream;
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    if (which == FSPH_BOUNDARY_POSITION) {
+        FSPH_CUDA(c, cudaMemcpyAsync(dst, c->b_in, (size_t)nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+    } else if (which == FSPH_BOUNDARY_VOLUME || which == FSPH_BOUNDARY_LAMBDA) {
+        const float *src = which == FSPH_BOUNDARY_VOLUME ? c->b_scale : c->b_lam;
+        float *t = reinterpret_cast<float *>(c->b_key); /* free after the boundary build */
+        launch_unsort1(nb, c->b_id, reinterpret_cast<const unsigned int *>(src), reinterpret_cast<unsigned int *>(t), s);
+        FSPH_CUDA(c, cudaMemcpyAsync(dst, t, (size_t)nb * sizeof(float), cudaMemcpyDeviceToHost, s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        if (which == FSPH_BOUNDARY_VOLUME) /* rho0 psi_b / m -> psi_b */
+            for (int b = 0; b < nb; ++b) dst[b] = dst[b] * c->P.mass / c->P.rest_dens;
+    } else {
+        return fail(c, FSPH_INVALID_ARG, "which: FSPH_BOUNDARY_POSITION, _VOLUME or _LAMBDA");
+    }
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(check_launch(c));
+    return FSPH_OK;
+}
+
+int fsph_num_boundary(const fsph_ctx *c) { return c ? c->nb : -1; }
+
 int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
     if (!c || !avg_ms || reps <= 0) return FSPH_INVALID_ARG;
     if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     if (c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "pass timing covers the PBF passes");
-    DevParams p = make_dev(c->P, c->n, c->dp.dt > 0.0f ? c->dp.dt : 1e-3f);
+    DevParams p = dev_for(c, c->n, c->dp.dt > 0.0f ? c->dp.dt : 1e-3f);
     cudaStream_t s = c->stream;
     /* the state after a step: x* = x in the home set, already cell-ordered */
     FSPH_TRY(build_on(c, p, c->set[0].pos));
@@ -1085,11 +1212,12 @@ int fsph_pbf_eval_lambda(fsph_ctx *c, const float *pos4, int n, float *dens, flo
     if (!c || !pos4 || !dens || !lambda) return FSPH_INVALID_ARG;
     FSPH_TRY(fsph_set_particles(c, pos4, nullptr, n, FSPH_HOST));
     if (n == 0) return FSPH_OK;
-    DevParams p = make_dev(c->P, n, 1.0f);
+    DevParams p = dev_for(c, n, 1.0f);
     cudaStream_t s = c->stream;
     FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
     FSPH_TRY(build_on(c, p, c->set[0].pos));
     launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
+    launch_boundary_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->ctl, c->b_stat, c->b_lam, s);
     FSPH_TRY(check_launch(c));
     FSPH_TRY(copy_out_scalar(c, c->dens, c->set[1].id, dens, n));
     launch_unsort_w(n, c->set[1].id, c->ppos[0], reinterpret_cast<float *>(c->key), s);
@@ -1102,7 +1230,7 @@ int fsph_pbf_eval_correction(fsph_ctx *c, const float *pos4, const float *lambda
     if (!c || !pos4 || !lambda || !dp4) return FSPH_INVALID_ARG;
     FSPH_TRY(fsph_set_particles(c, pos4, nullptr, n, FSPH_HOST));
     if (n == 0) return FSPH_OK;
-    DevParams p = make_dev(c->P, n, dt);
+    DevParams p = dev_for(c, n, dt);
     cudaStream_t s = c->stream;
     FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
     /* lambda rides in x*.w, in particle order before the sort */
@@ -1125,7 +1253,7 @@ int fsph_sph_eval_forces(fsph_ctx *c, const float *pos4, const float *vel4, int 
     if (!c || !pos4 || !dens || !pres || !acc4) return FSPH_INVALID_ARG;
     FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
     if (n == 0) return FSPH_OK;
-    DevParams p = make_dev(c->P, n, 1.0f);
+    DevParams p = dev_for(c, n, 1.0f);
     cudaStream_t s = c->stream;
     enqueue_sort(c, p, c->set[0].pos, s);
     Gather g{};
@@ -1149,9 +1277,15 @@ int fsph_sph_eval_forces(fsph_ctx *c, const float *pos4, const float *vel4, int 
 
 }  // extern "C"
 
-/* Parameter builders shared with the allocation-free entry point (fsph_noalloc.cu). */
+/* Parameter builders shared with the allocation-free entry point
+ * (fsph_noalloc.cu) and the batched scenes (fsph_batch.cu). */
 namespace fsph {
 DevParams dev_params_for(const fsph_params &p, int n, float dt) { return make_dev(p, n, dt); }
+int validate_params(const fsph_params &p, std::string &why) { return validate(p, why); }
+void grid_dims_for(const fsph_params &p, int g[3]) {
+    double cw, org[3];
+    grid_geometry(p, cw, org, g);
+}
 unsigned long long grid_cells_for(const fsph_params &p) {
     double cw, org[3];
     int g[3];

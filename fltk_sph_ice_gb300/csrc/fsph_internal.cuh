@@ -44,6 +44,14 @@ struct DevParams {
     float rl2;                  /* squared neighbour-list radius (= cell width) */
     int use_lists;              /* 1: lambda / correction passes read the neighbour lists */
     float dt, inv_dt;
+    unsigned int cell_off;      /* first cell of this scene's grid in the cell table (batches; else 0) */
+    int compensated;            /* 1: Kahan-compensated density sums in the lambda pass */
+    /* static boundary particles (nb = 0: none), sorted by the cells of this grid */
+    int nb;
+    const float4 *bpos;         /* x, y, z and w = rho0 psi_b / m */
+    const float *blam;          /* lambda_b of the current lambda pass */
+    const unsigned int *bcell;  /* boundary slots of cell c: [bcell[c], bcell[c + 1]) */
+    const unsigned char *bnear; /* 1 when boundary particles lie in the 27 cells around c */
 };
 
 /* Neighbour lists: up to kListMax entries per particle, transposed
@@ -126,13 +134,15 @@ __device__ inline int3 cell_of(float3 x, const DevParams &p) {
 }
 
 __device__ inline unsigned int cell_index(int3 c, const DevParams &p) {
-    return ((unsigned int)c.z * (unsigned int)p.gy + (unsigned int)c.y) * (unsigned int)p.gx + (unsigned int)c.x;
+    return p.cell_off +
+           ((unsigned int)c.z * (unsigned int)p.gy + (unsigned int)c.y) * (unsigned int)p.gx + (unsigned int)c.x;
 }
 
 /* Slot range [s, e) of the three cells x-1..x+1 in row (y + dy, z + dz). */
 __device__ inline void row_range(const unsigned int *__restrict__ cell_start, int3 c, int dy, int dz,
                                  const DevParams &p, unsigned int &s, unsigned int &e) {
-    unsigned int base = ((unsigned int)(c.z + dz) * (unsigned int)p.gy + (unsigned int)(c.y + dy)) * (unsigned int)p.gx +
+    unsigned int base = p.cell_off +
+                        ((unsigned int)(c.z + dz) * (unsigned int)p.gy + (unsigned int)(c.y + dy)) * (unsigned int)p.gx +
                         (unsigned int)c.x;
     s = __ldg(cell_start + base - 1);
     e = __ldg(cell_start + base + 2);

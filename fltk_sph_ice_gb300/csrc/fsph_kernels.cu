@@ -22,6 +22,7 @@
  *   k_sph_*            rxSPH::calDensity / calForce / integrate (rx_sph_cpu.cpp:495-1077)
  */
 #include "fsph_kernels.cuh"
+#include "fsph_passes.cuh"
 
 namespace fsph {
 
@@ -36,29 +37,14 @@ __global__ void k_predict_hash(DevParams p, const float4 *__restrict__ pos, cons
                                float4 *__restrict__ xpred_out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    float3 x = f3(pos[i]);
-    float3 v = f3(vel[i]);
-    float3 a = acc ? f3(acc[i]) : p.gravity;
-    v = v + p.dt * a;
-    x = x + p.dt * v;
-    x = wall_project(x, p);
-    if (xpred_out) xpred_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
-    /* warm start: the iterations begin from walls(x* + predicted correction);
-     * the grid and lists are then built on that start */
-    if (dwarm) x = wall_project(x + f3(dwarm[i]), p);
-    ppos_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
-    unsigned int c = cell_index(cell_of(x, p), p);
-    key[i] = c;
-    rank[i] = atomicAdd(count + c, 1u);
+    predict_body(p, i, pos, vel, acc, ppos_out, key, rank, count, dwarm, xpred_out);
 }
 
 __global__ void k_hash(DevParams p, const float4 *__restrict__ x4, unsigned int *__restrict__ key,
                        unsigned int *__restrict__ rank, unsigned int *__restrict__ count) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    unsigned int c = cell_index(cell_of(f3(x4[i]), p), p);
-    key[i] = c;
-    rank[i] = atomicAdd(count + c, 1u);
+    hash_body(p, i, f3(x4[i]), key, rank, count);
 }
 
 /* Scan phase 1: each 1024-thread block scans kScanTile = 4096 counts. */
@@ -194,9 +180,7 @@ __global__ void k_hash_parity(DevParams p, const float4 *ppos0, const float4 *pp
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const float4 *x4 = ctl->parity ? ppos1 : ppos0;
-    unsigned int c = cell_index(cell_of(f3(x4[i]), p), p);
-    key[i] = c;
-    rank[i] = atomicAdd(count + c, 1u);
+    hash_body(p, i, f3(x4[i]), key, rank, count);
 }
 
 /* Gather every array carried through the iterations into temporaries. */
@@ -262,81 +246,7 @@ __global__ void k_build_list(DevParams p, const unsigned int *__restrict__ cell_
                              unsigned short *__restrict__ list, unsigned char *__restrict__ cnt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    const float3 xi = f3(xb[i]);
-    const int cb = (int)cellb[i];
-    int k = 0;
-    bool ovf = false;
-#pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-        const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
-        const unsigned int s = __ldg(cell_start + base - 1), e = __ldg(cell_start + base + 2);
-        if (e - s > 4095u) ovf = true;
-        /* four candidates' loads in flight before their tests */
-        for (unsigned int j0 = s; j0 < e; j0 += 4) {
-            float4 xc[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) xc[u] = __ldg(xb + min(j0 + u, e - 1));
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const float3 d = xi - f3(xc[u]);
-                if (j0 + u < e && dot3(d, d) < p.rl2) {
-                    if (k < kListMax) list[(size_t)k * p.n + i] = (unsigned short)((r << 12) | (j0 + u - s));
-                    ++k;
-                }
-            }
-        }
-    }
-    cnt[i] = (ovf || k > kListMax) ? kListOverflow : (unsigned char)k;
-}
-
-/* Calls f(j, x[j]) for every candidate slot j of slot i: its list entries,
- * or -- for an overflowed list or when lists are off -- every slot of the 27
- * cells around the current position.  List entries are taken kBatch at a
- * time: their indices are decoded and their positions loaded before any is
- * used, so each thread keeps kBatch independent loads in flight (the passes
- * are bound by load latency, not by arithmetic).  rs: this thread's 9 row
- * starts in shared memory, strided by the block size.  Load selects the
- * load flavour for x. */
-constexpr int kBatch = 4;
-
-template <class Load, class F>
-__device__ __forceinline__ void for_each_candidate(const DevParams &p, const unsigned int *__restrict__ cell_start,
-                                                   const unsigned short *__restrict__ list,
-                                                   const unsigned char *__restrict__ cnt,
-                                                   const unsigned int *__restrict__ cellb, int i, float3 xi,
-                                                   unsigned int *rs, Load &&load, F &&f) {
-    const int k = list ? (int)cnt[i] : (int)kListOverflow;
-    if (k != (int)kListOverflow) {
-        const int cb = (int)cellb[i];
-#pragma unroll
-        for (int r = 0; r < 9; ++r) {
-            const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
-            rs[r * blockDim.x] = __ldg(cell_start + base - 1);
-        }
-        for (int t0 = 0; t0 < k; t0 += kBatch) {
-            unsigned int j[kBatch];
-            float4 xj[kBatch];
-#pragma unroll
-            for (int u = 0; u < kBatch; ++u) {
-                const int t = t0 + u < k ? t0 + u : k - 1;
-                const unsigned int e = __ldg(list + (size_t)t * p.n + i);
-                j[u] = rs[(e >> 12) * blockDim.x] + (e & 0xfffu);
-            }
-#pragma unroll
-            for (int u = 0; u < kBatch; ++u) xj[u] = load(j[u]);
-#pragma unroll
-            for (int u = 0; u < kBatch; ++u)
-                if (t0 + u < k) f(j[u], xj[u]);
-        }
-    } else {
-        const int3 c = cell_of(xi, p);
-        for (int dz = -1; dz <= 1; ++dz)
-            for (int dy = -1; dy <= 1; ++dy) {
-                unsigned int s, e;
-                row_range(cell_start, c, dy, dz, p, s, e);
-                for (unsigned int j = s; j < e; ++j) f(j, load(j));
-            }
-    }
+    build_list_body(p, i, cell_start, xb, cellb, list, cnt);
 }
 
 /* ======================================================================== */
@@ -364,7 +274,17 @@ __global__ void k_pbf_density(DevParams p, const unsigned int *__restrict__ cell
                 }
             }
         }
-    dens[i] = p.mass * p.aw * acc;
+    float rho = p.mass * p.aw * acc;
+    if (p.nb) { /* + sum_b rho0 psi_b W (rx_sph_pbd.cpp:624-644) */
+        float bw = 0.f;
+        for_each_boundary(p, xi, [&](unsigned int, const float4 &b4) {
+            const float3 d = xi - f3(b4);
+            const float q = fmaxf(p.h2 - dot3(d, d), 0.0f);
+            bw += b4.w * q * q * q;
+        });
+        rho += p.mass * p.aw * bw;
+    }
+    dens[i] = rho;
 }
 
 /* a_i = mu sum_{j != i} m (v_j - v_i) / rho_i lapW + g (rx_sph_pbd.cpp:651-689). */
@@ -400,6 +320,7 @@ __global__ void k_pbf_visc(DevParams p, const unsigned int *__restrict__ cell_st
  * into x*.w, block partial errors; the last block reduces the errors in a
  * fixed order, advances the iteration counter and decides whether the
  * device-side loop continues. */
+template <bool KAHAN>
 __global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens,
                                                    DevCtl *ctl, ErrPartial *part,
@@ -407,99 +328,19 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned i
                                                    const unsigned short *__restrict__ list,
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb) {
-    __shared__ float sh1[kBlock / 32], sh2[kBlock / 32], shm[kBlock / 32];
     __shared__ unsigned int s_rs[9 * kBlock];
-    __shared__ int s_last;
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     float4 *pp = par ? ppos1 : ppos0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float e1 = 0.f, e2 = 0.f, em = 0.f;
     if (i < p.n) {
-        const float3 xi = f3(pp[i]);
-        float wsum = 0.f, sd = 0.f;
-        float3 gs = make_float3(0.f, 0.f, 0.f);
-        const float agr = p.ag * p.inv_rest_dens;
-        /* plain (L1-cached) loads: only the .w words of pp are written by this
-         * kernel, and the neighbour loop reads x, y, z */
-        for_each_candidate(
-            p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return pp[j]; },
-            [&](unsigned int, const float4 &xj4) {
-                /* branch-free: outside h both q and t clamp to zero; the self
-                 * pair (d = 0) adds W(0) to the density and nothing else */
-                const float3 d = xi - f3(xj4);
-                const float r2 = dot3(d, d);
-                const float q = fmaxf(p.h2 - r2, 0.0f);
-                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
-                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
-                const float g = agr * t * t * inv_r; /* grad W / rho0 = g d */
-                wsum += q * q * q;
-                gs = gs + g * d;
-                sd += g * g * r2;
-            });
-        float rho = p.mass * p.aw * wsum;
-        sd += dot3(gs, gs);
-        float C = rho * p.inv_rest_dens - 1.0f;
-        float Cc = (p.clamp_constraint && C < 0.0f) ? 0.0f : C;
-        float lam = -Cc / (sd + p.epsilon);
-        reinterpret_cast<float *>(pp + i)[3] = lam;
-        dens[i] = rho;
+        const float C =
+            lambda_body<1, KAHAN>(p, cell_start, pp, dens, ctl, list, cnt, cellb, s_rs + threadIdx.x, i, 0, true);
         e1 = C > 0.0f ? C : 0.0f;
         e2 = fabsf(C);
         em = e2;
-        if (!(rho == rho)) ctl->nan_flag = 1u;
     }
-    e1 = warp_sum(e1);
-    e2 = warp_sum(e2);
-    em = warp_max(em);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { sh1[warp] = e1; sh2[warp] = e2; shm[warp] = em; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float a = 0.f, b = 0.f, m = 0.f;
-        for (int w = 0; w < kBlock / 32; ++w) { a += sh1[w]; b += sh2[w]; m = fmaxf(m, shm[w]); }
-        part[blockIdx.x] = ErrPartial{a, b, m, 0.f};
-        __threadfence();
-        unsigned int t = atomicAdd(&ctl->ticket, 1u);
-        s_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    /* fixed-order reduction of the block partials (double) */
-    __shared__ double r1[kBlock], r2s[kBlock];
-    __shared__ float rm[kBlock];
-    double a = 0.0, b = 0.0;
-    float m = 0.f;
-    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
-        float4 v = __ldcg(reinterpret_cast<const float4 *>(part) + k);
-        a += v.x; b += v.y; m = fmaxf(m, v.z);
-    }
-    r1[threadIdx.x] = a; r2s[threadIdx.x] = b; rm[threadIdx.x] = m;
-    __syncthreads();
-    for (int o = kBlock / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            r1[threadIdx.x] += r1[threadIdx.x + o];
-            r2s[threadIdx.x] += r2s[threadIdx.x + o];
-            rm[threadIdx.x] = fmaxf(rm[threadIdx.x], rm[threadIdx.x + o]);
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        float err1 = (float)(r1[0] / (double)p.n);
-        float err2 = (float)(r2s[0] / (double)p.n);
-        ctl->err1 = err1;
-        ctl->err2 = err2;
-        ctl->errmax = rm[0];
-        unsigned int it = ctl->iter + 1u;
-        ctl->iter = it;
-        float err = p.error_mode ? err2 : err1;
-        int minit = p.min_iter > 1 ? p.min_iter : 1;
-        int cont = ((int)it < p.max_iter) && !(err <= p.eta && (int)it >= minit);
-        if (ctl->nan_flag) cont = 0;
-        ctl->done = cont ? 0u : 1u;
-        ctl->ticket = 0u;
-        if (use_graph & 1) cudaGraphSetConditional(hwhile, cont ? 1u : 0u);
-    }
+    lambda_tail(p, ctl, part, e1, e2, em, hwhile, use_graph);
 }
 
 /* correction pass: dp_i = sum_j (lambda_i + lambda_j + s_corr) grad W_ij / rho0,
@@ -515,84 +356,16 @@ __global__ void __launch_bounds__(kBlock) k_correction(DevParams p, const unsign
                                                        const unsigned short *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
                                                        const unsigned int *__restrict__ cellb) {
-    __shared__ float shm[kBlock / 32];
     __shared__ unsigned int s_rs[9 * kBlock];
-    __shared__ int s_last;
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     const float4 *__restrict__ src = par ? ppos1 : ppos0;
     float4 *__restrict__ dst = par ? ppos0 : ppos1;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float disp2 = 0.f;
-    if (i < p.n) {
-        const float4 xi4 = src[i];
-        const float3 xi = f3(xi4);
-        const float li = xi4.w;
-        float3 acc = make_float3(0.f, 0.f, 0.f);
-        const float k_dt2 = -p.ap_k * p.dt * p.dt;
-        const float agr = p.ag * p.inv_rest_dens;
-        const float awq = p.aw * p.inv_wq;
-        for_each_candidate(
-            p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(src + j); },
-            [&](unsigned int, const float4 &xj4) {
-                /* branch-free: t = 0 outside h and d = 0 for the self pair */
-                const float3 d = xi - f3(xj4);
-                const float r2 = dot3(d, d);
-                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
-                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
-                const float g = agr * t * t * inv_r;
-                float sc = 0.0f;
-                if (p.use_ap) {
-                    const float q = fmaxf(p.h2 - r2, 0.0f);
-                    const float ww = awq * q * q * q;
-                    const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
-                    sc = k_dt2 * pw;
-                }
-                acc = acc + ((li + xj4.w + sc) * g) * d;
-            });
-        if (dp_out) dp_out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
-        float3 xn = wall_project(xi + acc, p);
-        dst[i] = make_float4(xn.x, xn.y, xn.z, 0.0f);
-        float3 dd = xn - f3(xb[i]);
-        disp2 = dot3(dd, dd);
-        if (!(xn.x == xn.x && xn.y == xn.y && xn.z == xn.z)) ctl->nan_flag = 1u;
-    }
-    disp2 = warp_max(disp2);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) shm[warp] = disp2;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float m = 0.f;
-        for (int w = 0; w < kBlock / 32; ++w) m = fmaxf(m, shm[w]);
-        part[blockIdx.x] = m;
-        __threadfence();
-        unsigned int t = atomicAdd(&ctl->ticket2, 1u);
-        s_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    __shared__ float rm[kBlock];
-    float m = 0.f;
-    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) m = fmaxf(m, __ldcg(part + k));
-    rm[threadIdx.x] = m;
-    __syncthreads();
-    for (int o = kBlock / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) rm[threadIdx.x] = fmaxf(rm[threadIdx.x], rm[threadIdx.x + o]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        float md = rm[0];
-        ctl->disp2_bits = __float_as_uint(md);
-        unsigned int rb = (md > p.skin2 || !(md == md)) ? 1u : 0u;
-        ctl->rebuild = rb;
-        ctl->parity = 1u - par;
-        ctl->ticket2 = 0u;
-        if (use_graph & 1) {
-            unsigned int more = ctl->done ? 0u : 1u;
-            cudaGraphSetConditional(hif, rb & more);
-            if (use_graph & 2) cudaGraphSetConditional(hif2, rb);
-        }
-    }
+    if (i < p.n)
+        disp2 = correction_body<1>(p, cell_start, src, dst, xb, ctl, dp_out, list, cnt, cellb, s_rs + threadIdx.x, i,
+                                   0, true);
+    correction_tail(p, ctl, part, disp2, par, hif, hif2, use_graph);
 }
 
 /* v = (x* - x) / dt, x = x* (rx_sph_pbd.cpp:464-471); also brings id / attr
@@ -632,54 +405,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph_vort(DevParams p, const unsigne
     __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    const float3 xi = f3(pos[i]), vi = f3(vel[i]);
-    float3 om = make_float3(0.f, 0.f, 0.f), xs = make_float3(0.f, 0.f, 0.f);
-    float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
-    float div = 0.f, cntf = 0.f;
-    /* branch-free pair terms: q and t clamp to zero outside h, and the self
-     * pair (d = 0, v_ij = 0) adds only to the neighbour count */
-    for_each_candidate(
-        p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(pos + j); },
-        [&](unsigned int j, const float4 &xj4) {
-            const float3 d = xi - f3(xj4);
-            const float r2 = dot3(d, d);
-            const float inside = r2 < p.h2 ? 1.0f : 0.0f;
-            const float q = fmaxf(p.h2 - r2, 0.0f);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
-            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
-            const float g = p.ag * t * t * inv_r;
-            const float3 vij = f3(__ldg(vel + j)) - vi;
-            const float mrho = p.mass / __ldg(dens + j);
-            om = om + cross3(vij, (-g) * d);
-            xs = xs + (p.aw * q * q * q * mrho) * vij;
-            cntf += inside;
-            off = off - inside * d;
-            div += mrho * g * dot3(vij, d);
-            cg = cg + (mrho * g) * d;
-        });
-    cntf = fmaxf(cntf, 1.0f);
-    float3 vn = vi + p.xsph_c * xs;
-    vel_out[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
-    vort[i] = make_float4(om.x, om.y, om.z, 0.0f);
-    if (fo.feat) {
-        /* warm-start features at the end of the step (dimensionless; see kFeatures) */
-        const float inv_h = 1.0f / p.h;
-        const float4 *pl = fo.ctl->parity ? fo.ppos0 : fo.ppos1; /* buffer of the last lambda pass */
-        const float3 dd = f3(fo.dstep[i]);
-        float f[kFeatures];
-        f[0] = dens[i] * p.inv_rest_dens - 1.0f;
-        f[1] = pl[i].w * p.rest_dens * p.h2;
-        f[2] = cntf * (1.0f / 33.0f);
-        f[3] = off.x * inv_h / cntf; f[4] = off.y * inv_h / cntf; f[5] = off.z * inv_h / cntf;
-        f[6] = vi.x * p.dt * inv_h; f[7] = vi.y * p.dt * inv_h; f[8] = vi.z * p.dt * inv_h;
-        f[9] = dd.x * inv_h; f[10] = dd.y * inv_h; f[11] = dd.z * inv_h;
-        f[12] = div * p.dt;
-        f[13] = cg.x * p.h; f[14] = cg.y * p.h; f[15] = cg.z * p.h;
-        float4 *out = reinterpret_cast<float4 *>(fo.feat + (size_t)i * kFeatures);
-#pragma unroll
-        for (int k = 0; k < kFeatures / 4; ++k) out[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
-        if (i == 0) *fo.valid = 1u;
-    }
+    xsph_vort_body(p, i, cell_start, pos, vel, dens, vel_out, vort, fo, list, cnt, cellb, s_rs + threadIdx.x);
 }
 
 /* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
@@ -696,34 +422,111 @@ __global__ void __launch_bounds__(kBlock) k_vort_apply(DevParams p, const unsign
     __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    float4 v4 = vel_in[i];
-    if (p.vort_eps != 0.0f) {
-        const float3 xi = f3(pos[i]);
-        const float3 wi = f3(vort[i]);
-        const float wmi = sqrtf(dot3(wi, wi));
-        float3 eta = make_float3(0.f, 0.f, 0.f);
-        for_each_candidate(
-            p, cell_start, list, cnt, cellb, i, xi, s_rs + threadIdx.x, [&](unsigned int j) { return __ldg(pos + j); },
-            [&](unsigned int j, const float4 &xj4) {
-                const float3 d = xi - f3(xj4);
-                const float r2 = dot3(d, d);
-                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
-                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
-                const float g = p.ag * t * t * inv_r;
-                const float3 wj = f3(__ldg(vort + j));
-                const float k = p.mass / __ldg(dens + j) * (sqrtf(dot3(wj, wj)) - wmi) * g;
-                eta = eta + k * d;
-            });
-        float en = sqrtf(dot3(eta, eta));
-        if (en > 1e-30f) {
-            float3 N = (1.0f / en) * eta;
-            float3 f = p.vort_eps * cross3(N, wi);
-            v4.x += p.dt * f.x;
-            v4.y += p.dt * f.y;
-            v4.z += p.dt * f.z;
-        }
+    vort_apply_body(p, i, cell_start, pos, vort, dens, vel_in, vel_out, list, cnt, cellb, s_rs + threadIdx.x);
+}
+
+/* ======================================================================== */
+/* static boundary particles                                                */
+/* ======================================================================== */
+/* p.n = the boundary count in these kernels; p.bpos etc. the sorted boundary */
+
+/* psi_b = m / sum_b' m W(r_bb') (rx_sph_pbd.cpp:1061-1090); bscale[b] = rho0 psi_b / m */
+__global__ void k_boundary_volume(DevParams p, float *__restrict__ bscale) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= p.n) return;
+    const float3 xb = f3(__ldg(p.bpos + b));
+    float wsum = 0.f;
+    for_each_boundary(p, xb, [&](unsigned int, const float4 &c4) {
+        const float3 d = xb - f3(c4);
+        const float q = fmaxf(p.h2 - dot3(d, d), 0.0f);
+        wsum += q * q * q;
+    });
+    const float mw = p.mass * p.aw * wsum; /* sum_b' m W, self included */
+    bscale[b] = p.rest_dens / mw;          /* rho0 psi_b / m = rho0 / (sum m W) */
+}
+
+/* The boundary-boundary parts of lambda_b, fixed for a static boundary. */
+__global__ void k_boundary_static(DevParams p, float2 *__restrict__ bstat) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= p.n) return;
+    const float3 xb = f3(__ldg(p.bpos + b));
+    const float agr = p.ag * p.inv_rest_dens;
+    float bw = 0.f, sd = 0.f;
+    for_each_boundary(p, xb, [&](unsigned int, const float4 &c4) {
+        const float3 d = xb - f3(c4);
+        const float r2 = dot3(d, d);
+        const float q = fmaxf(p.h2 - r2, 0.0f);
+        const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+        const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+        const float gb = c4.w * agr * t * t * inv_r;
+        bw += c4.w * q * q * q;
+        sd += gb * gb * r2;
+    });
+    bstat[b] = make_float2(p.mass * p.aw * bw, sd);
+}
+
+__global__ void k_boundary_near(DevParams p, unsigned int ncells, unsigned char *__restrict__ bnear) {
+    unsigned int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const int x = (int)(c % (unsigned int)p.gx), y = (int)((c / (unsigned int)p.gx) % (unsigned int)p.gy),
+              z = (int)(c / ((unsigned int)p.gx * (unsigned int)p.gy));
+    unsigned char any = 0;
+    if (x >= 1 && y >= 1 && z >= 1 && x <= p.gx - 2 && y <= p.gy - 2 && z <= p.gz - 2) {
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy) {
+                const unsigned int base = c + (unsigned int)((dz * p.gy + dy) * p.gx);
+                if (p.bcell[base + 2] > p.bcell[base - 1]) any = 1;
+            }
     }
-    vel_out[i] = v4;
+    bnear[c] = any;
+}
+
+/* lambda_b = -C_b / (sd_b + eps): rho_b and sd_b from the fluid x* of the
+ * current parity plus the static boundary parts (rx_sph_pbd.cpp:825-913,
+ * fluid neighbours on the current positions as rx_pbdsph_kernel.cu:666-735). */
+__global__ void __launch_bounds__(kBlock) k_boundary_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                            const float4 *ppos0, const float4 *ppos1,
+                                                            const DevCtl *ctl, const float2 *__restrict__ bstat,
+                                                            float *__restrict__ blam) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= p.nb) return;
+    const float4 *pp = ctl->parity ? ppos1 : ppos0;
+    const float3 xb = f3(__ldg(p.bpos + b));
+    const float agr = p.ag * p.inv_rest_dens;
+    float wsum = 0.f, sd = 0.f;
+    for_each_candidate<1>(
+        p, cell_start, nullptr, nullptr, nullptr, 0, xb, nullptr, 0, [&](unsigned int j) { return pp[j]; },
+        [&](unsigned int, const float4 &xj4) {
+            const float3 d = xb - f3(xj4);
+            const float r2 = dot3(d, d);
+            const float q = fmaxf(p.h2 - r2, 0.0f);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float g = agr * t * t * inv_r;
+            wsum += q * q * q;
+            sd += g * g * r2;
+        });
+    const float2 st = bstat[b];
+    const float rho = p.mass * p.aw * wsum + st.x;
+    sd += st.y;
+    float C = rho * p.inv_rest_dens - 1.0f;
+    if (p.clamp_constraint && C < 0.0f) C = 0.0f;
+    blam[b] = -C / (sd + p.epsilon);
+}
+
+void launch_boundary_volume(const DevParams &p, float *bscale, cudaStream_t s) {
+    k_boundary_volume<<<blocks_for(p.n), kBlock, 0, s>>>(p, bscale);
+}
+void launch_boundary_static(const DevParams &p, float2 *bstat, cudaStream_t s) {
+    k_boundary_static<<<blocks_for(p.n), kBlock, 0, s>>>(p, bstat);
+}
+void launch_boundary_near(const DevParams &p, unsigned int ncells, unsigned char *bnear, cudaStream_t s) {
+    k_boundary_near<<<blocks_for(ncells), kBlock, 0, s>>>(p, ncells, bnear);
+}
+void launch_boundary_lambda(const DevParams &p, const unsigned int *cell_start, const float4 *ppos0,
+                            const float4 *ppos1, const DevCtl *ctl, const float2 *bstat, float *blam, cudaStream_t s) {
+    if (p.nb <= 0) return;
+    k_boundary_lambda<<<blocks_for(p.nb), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, ctl, bstat, blam);
 }
 
 /* ======================================================================== */
@@ -973,9 +776,10 @@ void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const f
 void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1, float *dens,
                    DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
                    const NbrLists &nl, cudaStream_t s) {
-    k_lambda<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
-                                                (cudaGraphConditionalHandle)while_handle, use_graph,
-                                                p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
+    auto k = p.compensated ? k_lambda<true> : k_lambda<false>;
+    k<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
+                                         (cudaGraphConditionalHandle)while_handle, use_graph,
+                                         p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
 void launch_build_list(const DevParams &p, const unsigned int *cell_start, const float4 *xb, const NbrLists &nl,
                        cudaStream_t s) {

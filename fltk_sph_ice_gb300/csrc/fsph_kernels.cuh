@@ -9,6 +9,7 @@
 namespace fsph {
 
 constexpr int kBlock = 256;
+constexpr int kBlockMax = 512;  /* largest block of the batched persistent kernels */
 constexpr int kScanTile = 4096; /* cells per block of the first scan phase */
 
 inline unsigned int blocks_for(long long n, int b = kBlock) { return (unsigned int)((n + b - 1) / b); }
@@ -85,6 +86,18 @@ void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const 
                       cudaStream_t s);
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
                        const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s);
+
+/* ---- static boundary particles (p.bpos / p.bcell / p.bnear of the sorted boundary) ---- */
+/* bscale[b] = rho0 psi_b / m with psi_b = m / sum_b' m W(r_bb') (rx_sph_pbd.cpp:1061-1090) */
+void launch_boundary_volume(const DevParams &p, float *bscale, cudaStream_t s);
+/* bstat[b] = (sum_b' rho0 psi_b' W, sum_b' |(rho0 psi_b' / m) grad W / rho0|^2): the static
+ * boundary-boundary parts of lambda_b */
+void launch_boundary_static(const DevParams &p, float2 *bstat, cudaStream_t s);
+/* bnear[c] = 1 when any boundary slot lies in the 27 cells around cell c */
+void launch_boundary_near(const DevParams &p, unsigned int ncells, unsigned char *bnear, cudaStream_t s);
+/* lambda_b of every boundary particle from the fluid x* of the current parity (rx_sph_pbd.cpp:825-913) */
+void launch_boundary_lambda(const DevParams &p, const unsigned int *cell_start, const float4 *ppos0,
+                            const float4 *ppos1, const DevCtl *ctl, const float2 *bstat, float *blam, cudaStream_t s);
 
 /* ---- WCSPH ---- */
 void launch_sph_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,

@@ -1,0 +1,516 @@
+/*
+ * fsph_passes.cuh -- per-particle bodies of the PBF passes, shared by the
+ * single-scene kernels (fsph_kernels.cu, one thread per particle) and the
+ * batched persistent kernels (fsph_batch.cu, tiles of one scene per block).
+ *
+ * A body computes one particle i (a slot in device order) with the constants
+ * of its scene, p.  `valid` is false for the padding lanes of a tile: they
+ * run the loops on a clamped slot (so warp-wide shuffles stay convergent)
+ * and write nothing.  LPP > 1 lets LPP adjacent lanes share one particle's
+ * candidates (lane `sub` takes entries sub, sub + LPP, ...); their partial
+ * sums are combined with shuffles, and lane 0 of the group writes.
+ */
+#pragma once
+#include "fsph_kernels.cuh"
+
+namespace fsph {
+
+/* ---------------- candidate loop ---------------- */
+
+/* Calls f(j, x[j]) for every candidate slot j of slot i handled by lane
+ * `sub` of its LPP-lane group: the list entries sub, sub + LPP, ... or -- for
+ * an overflowed list or when lists are off -- every LPP-th slot of the 27
+ * cells around the current position.  List entries are taken kBatch at a
+ * time: their indices are decoded and their positions loaded before any is
+ * used, so each thread keeps kBatch independent loads in flight (the passes
+ * are bound by load latency, not by arithmetic).  rs: this thread's 9 row
+ * starts in shared memory, strided by the block size.  Load selects the
+ * load flavour for x. */
+constexpr int kBatch = 4;
+
+template <int LPP, class Load, class F>
+__device__ __forceinline__ void for_each_candidate(const DevParams &p, const unsigned int *__restrict__ cell_start,
+                                                   const unsigned short *__restrict__ list,
+                                                   const unsigned char *__restrict__ cnt,
+                                                   const unsigned int *__restrict__ cellb, int i, float3 xi,
+                                                   unsigned int *rs, int sub, Load &&load, F &&f) {
+    const int k = list ? (int)cnt[i] : (int)kListOverflow;
+    if (k != (int)kListOverflow) {
+        const int cb = (int)cellb[i];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
+            rs[r * blockDim.x] = __ldg(cell_start + base - 1);
+        }
+        for (int t0 = sub; t0 < k; t0 += kBatch * LPP) {
+            unsigned int j[kBatch];
+            float4 xj[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int t = t0 + u * LPP < k ? t0 + u * LPP : k - 1;
+                const unsigned int e = __ldg(list + (size_t)t * p.n + i);
+                j[u] = rs[(e >> 12) * blockDim.x] + (e & 0xfffu);
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) xj[u] = load(j[u]);
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u)
+                if (t0 + u * LPP < k) f(j[u], xj[u]);
+        }
+    } else {
+        const int3 c = cell_of(xi, p);
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy) {
+                unsigned int s, e;
+                row_range(cell_start, c, dy, dz, p, s, e);
+                for (unsigned int j = s + (unsigned int)sub; j < e; j += LPP) f(j, load(j));
+            }
+    }
+}
+
+/* Calls f(b, bpos[b]) for every boundary slot b in the 27 cells around the
+ * cell of x (nothing when no boundary particle is near that cell).  The
+ * boundary is static and sorted by the same cells as the fluid, so a
+ * boundary particle within h of x lies in those cells. */
+template <class F>
+__device__ __forceinline__ void for_each_boundary(const DevParams &p, float3 x, F &&f) {
+    const int3 c = cell_of(x, p);
+    const unsigned int ci = cell_index(c, p);
+    if (!p.bnear[ci]) return;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy) {
+            const unsigned int base = ci + (unsigned int)((dz * p.gy + dy) * p.gx);
+            const unsigned int s = __ldg(p.bcell + base - 1), e = __ldg(p.bcell + base + 2);
+            for (unsigned int j = s; j < e; ++j) f(j, __ldg(p.bpos + j));
+        }
+}
+
+/* sum over the LPP lanes of a group (every lane of the warp must call it) */
+template <int LPP>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = LPP / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+/* ---------------- grid build ---------------- */
+
+/* x* = walls(x + dt (v + dt a)), a = gravity when acc == NULL, then the
+ * cell key and the slot's rank within the cell. */
+__device__ __forceinline__ void predict_body(const DevParams &p, int i, const float4 *__restrict__ pos,
+                                             const float4 *__restrict__ vel, const float4 *__restrict__ acc,
+                                             float4 *__restrict__ ppos_out, unsigned int *__restrict__ key,
+                                             unsigned int *__restrict__ rank, unsigned int *__restrict__ count,
+                                             const float4 *__restrict__ dwarm, float4 *__restrict__ xpred_out) {
+    float3 x = f3(pos[i]);
+    float3 v = f3(vel[i]);
+    float3 a = acc ? f3(acc[i]) : p.gravity;
+    v = v + p.dt * a;
+    x = x + p.dt * v;
+    x = wall_project(x, p);
+    if (xpred_out) xpred_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
+    /* warm start: the iterations begin from walls(x* + predicted correction);
+     * the grid and lists are then built on that start */
+    if (dwarm) x = wall_project(x + f3(dwarm[i]), p);
+    ppos_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
+    unsigned int c = cell_index(cell_of(x, p), p);
+    key[i] = c;
+    rank[i] = atomicAdd(count + c, 1u);
+}
+
+__device__ __forceinline__ void hash_body(const DevParams &p, int i, float3 x, unsigned int *__restrict__ key,
+                                          unsigned int *__restrict__ rank, unsigned int *__restrict__ count) {
+    unsigned int c = cell_index(cell_of(x, p), p);
+    key[i] = c;
+    rank[i] = atomicAdd(count + c, 1u);
+}
+
+/* Every slot j within the list radius (= the cell width) of slot i at the
+ * build positions xb, self included, as (row << 12) | (j - row_start). */
+__device__ __forceinline__ void build_list_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
+                                                const float4 *__restrict__ xb, const unsigned int *__restrict__ cellb,
+                                                unsigned short *__restrict__ list, unsigned char *__restrict__ cnt) {
+    const float3 xi = f3(xb[i]);
+    const int cb = (int)cellb[i];
+    int k = 0;
+    bool ovf = false;
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
+        const unsigned int s = __ldg(cell_start + base - 1), e = __ldg(cell_start + base + 2);
+        if (e - s > 4095u) ovf = true;
+        /* four candidates' loads in flight before their tests */
+        for (unsigned int j0 = s; j0 < e; j0 += 4) {
+            float4 xc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xc[u] = __ldg(xb + min(j0 + u, e - 1));
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float3 d = xi - f3(xc[u]);
+                if (j0 + u < e && dot3(d, d) < p.rl2) {
+                    if (k < kListMax) list[(size_t)k * p.n + i] = (unsigned short)((r << 12) | (j0 + u - s));
+                    ++k;
+                }
+            }
+        }
+    }
+    cnt[i] = (ovf || k > kListMax) ? kListOverflow : (unsigned char)k;
+}
+
+/* ---------------- constraint iterations ---------------- */
+
+/* lambda pass of one particle: density, C, sum |grad C|^2 (with the k = i
+ * term), lambda into x*.w and rho into dens (lane 0 of a valid group).
+ * Returns C (the caller turns it into the error terms). */
+template <int LPP, bool KAHAN = false>
+__device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned int *__restrict__ cell_start,
+                                             float4 *pp, float *__restrict__ dens, DevCtl *ctl,
+                                             const unsigned short *__restrict__ list,
+                                             const unsigned char *__restrict__ cnt,
+                                             const unsigned int *__restrict__ cellb, unsigned int *rs, int i, int sub,
+                                             bool valid) {
+    const float3 xi = f3(pp[i]);
+    float wsum = 0.f, wc = 0.f, sd = 0.f;
+    float3 gs = make_float3(0.f, 0.f, 0.f);
+    const float agr = p.ag * p.inv_rest_dens;
+    /* plain (L1-cached) loads: only the .w words of pp are written by this
+     * pass, and the neighbour loop reads x, y, z */
+    for_each_candidate<LPP>(
+        p, cell_start, list, cnt, cellb, i, xi, rs, sub, [&](unsigned int j) { return pp[j]; },
+        [&](unsigned int, const float4 &xj4) {
+            /* branch-free: outside h both q and t clamp to zero; the self
+             * pair (d = 0) adds W(0) to the density and nothing else */
+            const float3 d = xi - f3(xj4);
+            const float r2 = dot3(d, d);
+            const float q = fmaxf(p.h2 - r2, 0.0f);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float g = agr * t * t * inv_r; /* grad W / rho0 = g d */
+            if (KAHAN) { /* compensated sum of the density terms */
+                const float y = q * q * q - wc;
+                const float s = wsum + y;
+                wc = (s - wsum) - y;
+                wsum = s;
+            } else {
+                wsum += q * q * q;
+            }
+            gs = gs + g * d;
+            sd += g * g * r2;
+        });
+    if (LPP > 1) {
+        wsum = group_sum<LPP>(wsum);
+        sd = group_sum<LPP>(sd);
+        gs.x = group_sum<LPP>(gs.x);
+        gs.y = group_sum<LPP>(gs.y);
+        gs.z = group_sum<LPP>(gs.z);
+    }
+    float rho = p.mass * p.aw * wsum;
+    sd += dot3(gs, gs);
+    if (p.nb) {
+        /* boundary particles (rx_sph_pbd.cpp:728-748, 795-818): density
+         * rho0 psi_b W and |grad C|^2 terms of (rho0 psi_b / m) grad W / rho0,
+         * each boundary neighbour counted once (rx_pbdsph_kernel.cu:577-664);
+         * every lane of a group sums them (they are few) */
+        float bw = 0.f;
+        for_each_boundary(p, xi, [&](unsigned int, const float4 &b4) {
+            const float3 d = xi - f3(b4);
+            const float r2 = dot3(d, d);
+            const float q = fmaxf(p.h2 - r2, 0.0f);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float gb = b4.w * agr * t * t * inv_r;
+            bw += b4.w * q * q * q;
+            sd += gb * gb * r2;
+        });
+        rho += p.mass * p.aw * bw;
+    }
+    float C = rho * p.inv_rest_dens - 1.0f;
+    float Cc = (p.clamp_constraint && C < 0.0f) ? 0.0f : C;
+    float lam = -Cc / (sd + p.epsilon);
+    if (valid && sub == 0) {
+        reinterpret_cast<float *>(pp + i)[3] = lam;
+        dens[i] = rho;
+        if (!(rho == rho)) ctl->nan_flag = 1u;
+    }
+    return C;
+}
+
+/* End of the lambda pass: block partial errors; the last block reduces them
+ * in a fixed order, advances the iteration counter and decides whether the
+ * device-side loop continues (lp: the loop constants).  Every thread of the
+ * block calls it. */
+__device__ __forceinline__ void lambda_tail(const DevParams &lp, DevCtl *ctl, ErrPartial *part, float e1, float e2,
+                                            float em, cudaGraphConditionalHandle hwhile, int use_graph) {
+    __shared__ float sh1[32], sh2[32], shm[32];
+    __shared__ double d1[32], d2[32];
+    __shared__ int s_last;
+    e1 = warp_sum(e1);
+    e2 = warp_sum(e2);
+    em = warp_max(em);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) { sh1[warp] = e1; sh2[warp] = e2; shm[warp] = em; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.f, b = 0.f, m = 0.f;
+        for (int w = 0; w < nw; ++w) { a += sh1[w]; b += sh2[w]; m = fmaxf(m, shm[w]); }
+        part[blockIdx.x] = ErrPartial{a, b, m, 0.f};
+        __threadfence();
+        unsigned int t = atomicAdd(&ctl->ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    /* fixed-order reduction of the block partials (double): strided per
+     * thread, a shuffle tree per warp, then the warps in order */
+    double a = 0.0, b = 0.0;
+    float m = 0.f;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+        float4 v = __ldcg(reinterpret_cast<const float4 *>(part) + k);
+        a += v.x; b += v.y; m = fmaxf(m, v.z);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    }
+    if (lane == 0) { d1[warp] = a; d2[warp] = b; shm[warp] = m; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = 0.0; b = 0.0; m = 0.f;
+        for (int w = 0; w < nw; ++w) { a += d1[w]; b += d2[w]; m = fmaxf(m, shm[w]); }
+        float err1 = (float)(a / (double)lp.n);
+        float err2 = (float)(b / (double)lp.n);
+        ctl->err1 = err1;
+        ctl->err2 = err2;
+        ctl->errmax = m;
+        unsigned int it = ctl->iter + 1u;
+        ctl->iter = it;
+        float err = lp.error_mode ? err2 : err1;
+        int minit = lp.min_iter > 1 ? lp.min_iter : 1;
+        int cont = ((int)it < lp.max_iter) && !(err <= lp.eta && (int)it >= minit);
+        if (ctl->nan_flag) cont = 0;
+        ctl->done = cont ? 0u : 1u;
+        ctl->ticket = 0u;
+        if (use_graph & 1) cudaGraphSetConditional(hwhile, cont ? 1u : 0u);
+    }
+}
+
+/* correction pass of one particle: dp_i = sum_j (lambda_i + lambda_j + s_corr)
+ * grad W_ij / rho0, x*_i <- walls(x*_i + dp_i) into dst (lane 0 of a valid
+ * group).  Returns |x*_i - xb_i|^2 (0 for the other lanes). */
+template <int LPP>
+__device__ __forceinline__ float correction_body(const DevParams &p, const unsigned int *__restrict__ cell_start,
+                                                 const float4 *__restrict__ src, float4 *__restrict__ dst,
+                                                 const float4 *__restrict__ xb, DevCtl *ctl,
+                                                 float4 *__restrict__ dp_out, const unsigned short *__restrict__ list,
+                                                 const unsigned char *__restrict__ cnt,
+                                                 const unsigned int *__restrict__ cellb, unsigned int *rs, int i,
+                                                 int sub, bool valid) {
+    const float4 xi4 = src[i];
+    const float3 xi = f3(xi4);
+    const float li = xi4.w;
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const float k_dt2 = -p.ap_k * p.dt * p.dt;
+    const float agr = p.ag * p.inv_rest_dens;
+    const float awq = p.aw * p.inv_wq;
+    for_each_candidate<LPP>(
+        p, cell_start, list, cnt, cellb, i, xi, rs, sub, [&](unsigned int j) { return __ldg(src + j); },
+        [&](unsigned int, const float4 &xj4) {
+            /* branch-free: t = 0 outside h and d = 0 for the self pair */
+            const float3 d = xi - f3(xj4);
+            const float r2 = dot3(d, d);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float g = agr * t * t * inv_r;
+            float sc = 0.0f;
+            if (p.use_ap) {
+                const float q = fmaxf(p.h2 - r2, 0.0f);
+                const float ww = awq * q * q * q;
+                const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
+                sc = k_dt2 * pw;
+            }
+            acc = acc + ((li + xj4.w + sc) * g) * d;
+        });
+    if (LPP > 1) {
+        acc.x = group_sum<LPP>(acc.x);
+        acc.y = group_sum<LPP>(acc.y);
+        acc.z = group_sum<LPP>(acc.z);
+    }
+    if (p.nb) {
+        /* boundary terms (rx_sph_pbd.cpp:977-1019): lambda_b, and s_corr of
+         * the (rho0 psi_b / m)-scaled W */
+        float3 accb = make_float3(0.f, 0.f, 0.f);
+        for_each_boundary(p, xi, [&](unsigned int b, const float4 &b4) {
+            const float3 d = xi - f3(b4);
+            const float r2 = dot3(d, d);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float g = agr * t * t * inv_r;
+            float sc = 0.0f;
+            if (p.use_ap) {
+                const float q = fmaxf(p.h2 - r2, 0.0f);
+                const float ww = b4.w * awq * q * q * q;
+                const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
+                sc = k_dt2 * pw;
+            }
+            accb = accb + ((li + __ldg(p.blam + b) + sc) * g) * d;
+        });
+        acc = acc + accb;
+    }
+    if (!valid || sub != 0) return 0.0f;
+    if (dp_out) dp_out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+    float3 xn = wall_project(xi + acc, p);
+    dst[i] = make_float4(xn.x, xn.y, xn.z, 0.0f);
+    float3 dd = xn - f3(xb[i]);
+    if (!(xn.x == xn.x && xn.y == xn.y && xn.z == xn.z)) ctl->nan_flag = 1u;
+    return dot3(dd, dd);
+}
+
+/* End of the correction pass: the largest displacement measure of the block;
+ * the last block compares the maximum with lp.skin2 (a rebuild is due above
+ * it), flips the x* parity and sets the graph's rebuild conditions.  Every
+ * thread of the block calls it. */
+__device__ __forceinline__ void correction_tail(const DevParams &lp, DevCtl *ctl, float *part, float disp2,
+                                                unsigned int par, cudaGraphConditionalHandle hif,
+                                                cudaGraphConditionalHandle hif2, int use_graph) {
+    __shared__ float shm[32];
+    __shared__ int s_last;
+    disp2 = warp_max(disp2);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) shm[warp] = disp2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.f;
+        for (int w = 0; w < nw; ++w) m = fmaxf(m, shm[w]);
+        part[blockIdx.x] = m;
+        __threadfence();
+        unsigned int t = atomicAdd(&ctl->ticket2, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    float m = 0.f;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) m = fmaxf(m, __ldcg(part + k));
+    m = warp_max(m);
+    __syncthreads(); /* every warp has read its shm entry above */
+    if (lane == 0) shm[warp] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float md = 0.f;
+        for (int w = 0; w < nw; ++w) md = fmaxf(md, shm[w]);
+        ctl->disp2_bits = __float_as_uint(md);
+        unsigned int rb = (md > lp.skin2 || !(md == md)) ? 1u : 0u;
+        ctl->rebuild = rb;
+        ctl->parity = 1u - par;
+        ctl->ticket2 = 0u;
+        if (use_graph & 1) {
+            unsigned int more = ctl->done ? 0u : 1u;
+            cudaGraphSetConditional(hif, rb & more);
+            if (use_graph & 2) cudaGraphSetConditional(hif2, rb);
+        }
+    }
+}
+
+/* ---------------- end of step ---------------- */
+
+/* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), the XSPH
+ * update v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij, and (fo.feat) the
+ * warm-start features of the particle. */
+__device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
+                                               const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                                               const float *__restrict__ dens, float4 *__restrict__ vel_out,
+                                               float4 *__restrict__ vort, const FeatureOut &fo,
+                                               const unsigned short *__restrict__ list,
+                                               const unsigned char *__restrict__ cnt,
+                                               const unsigned int *__restrict__ cellb, unsigned int *rs) {
+    const float3 xi = f3(pos[i]), vi = f3(vel[i]);
+    float3 om = make_float3(0.f, 0.f, 0.f), xs = make_float3(0.f, 0.f, 0.f);
+    float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
+    float div = 0.f, cntf = 0.f;
+    /* branch-free pair terms: q and t clamp to zero outside h, and the self
+     * pair (d = 0, v_ij = 0) adds only to the neighbour count */
+    for_each_candidate<1>(
+        p, cell_start, list, cnt, cellb, i, xi, rs, 0, [&](unsigned int j) { return __ldg(pos + j); },
+        [&](unsigned int j, const float4 &xj4) {
+            const float3 d = xi - f3(xj4);
+            const float r2 = dot3(d, d);
+            const float inside = r2 < p.h2 ? 1.0f : 0.0f;
+            const float q = fmaxf(p.h2 - r2, 0.0f);
+            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+            const float g = p.ag * t * t * inv_r;
+            const float3 vij = f3(__ldg(vel + j)) - vi;
+            const float mrho = p.mass / __ldg(dens + j);
+            om = om + cross3(vij, (-g) * d);
+            xs = xs + (p.aw * q * q * q * mrho) * vij;
+            cntf += inside;
+            off = off - inside * d;
+            div += mrho * g * dot3(vij, d);
+            cg = cg + (mrho * g) * d;
+        });
+    cntf = fmaxf(cntf, 1.0f);
+    float3 vn = vi + p.xsph_c * xs;
+    vel_out[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
+    vort[i] = make_float4(om.x, om.y, om.z, 0.0f);
+    if (fo.feat) {
+        /* warm-start features at the end of the step (dimensionless; see kFeatures) */
+        const float inv_h = 1.0f / p.h;
+        const float4 *pl = fo.ctl->parity ? fo.ppos0 : fo.ppos1; /* buffer of the last lambda pass */
+        const float3 dd = f3(fo.dstep[i]);
+        float f[kFeatures];
+        f[0] = dens[i] * p.inv_rest_dens - 1.0f;
+        f[1] = pl[i].w * p.rest_dens * p.h2;
+        f[2] = cntf * (1.0f / 33.0f);
+        f[3] = off.x * inv_h / cntf; f[4] = off.y * inv_h / cntf; f[5] = off.z * inv_h / cntf;
+        f[6] = vi.x * p.dt * inv_h; f[7] = vi.y * p.dt * inv_h; f[8] = vi.z * p.dt * inv_h;
+        f[9] = dd.x * inv_h; f[10] = dd.y * inv_h; f[11] = dd.z * inv_h;
+        f[12] = div * p.dt;
+        f[13] = cg.x * p.h; f[14] = cg.y * p.h; f[15] = cg.z * p.h;
+        float4 *out = reinterpret_cast<float4 *>(fo.feat + (size_t)i * kFeatures);
+#pragma unroll
+        for (int k = 0; k < kFeatures / 4; ++k) out[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+        if (i == 0) *fo.valid = 1u;
+    }
+}
+
+/* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
+ * v_i <- v_i + dt f. */
+__device__ __forceinline__ void vort_apply_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
+                                                const float4 *__restrict__ pos, const float4 *__restrict__ vort,
+                                                const float *__restrict__ dens, const float4 *__restrict__ vel_in,
+                                                float4 *__restrict__ vel_out, const unsigned short *__restrict__ list,
+                                                const unsigned char *__restrict__ cnt,
+                                                const unsigned int *__restrict__ cellb, unsigned int *rs) {
+    float4 v4 = vel_in[i];
+    if (p.vort_eps != 0.0f) {
+        const float3 xi = f3(pos[i]);
+        const float3 wi = f3(vort[i]);
+        const float wmi = sqrtf(dot3(wi, wi));
+        float3 eta = make_float3(0.f, 0.f, 0.f);
+        for_each_candidate<1>(
+            p, cell_start, list, cnt, cellb, i, xi, rs, 0, [&](unsigned int j) { return __ldg(pos + j); },
+            [&](unsigned int j, const float4 &xj4) {
+                const float3 d = xi - f3(xj4);
+                const float r2 = dot3(d, d);
+                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+                const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
+                const float g = p.ag * t * t * inv_r;
+                const float3 wj = f3(__ldg(vort + j));
+                const float k = p.mass / __ldg(dens + j) * (sqrtf(dot3(wj, wj)) - wmi) * g;
+                eta = eta + k * d;
+            });
+        float en = sqrtf(dot3(eta, eta));
+        if (en > 1e-30f) {
+            float3 N = (1.0f / en) * eta;
+            float3 f = p.vort_eps * cross3(N, wi);
+            v4.x += p.dt * f.x;
+            v4.y += p.dt * f.y;
+            v4.z += p.dt * f.z;
+        }
+    }
+    vel_out[i] = v4;
+}
+
+}  // namespace fsph

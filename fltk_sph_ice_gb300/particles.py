@@ -199,6 +199,24 @@ class rxPBDSPH(rxParticleSystemBase):
 
     solver = abi.SOLVER_PBF
 
+    def SetBoundary(self, bpos):
+        """Static boundary particles (the boundary set-up of rxPBDSPH::Initialize,
+        rx_sph_pbd.cpp:280-297); bpos (NB,3) or (NB,4); an empty array removes them."""
+        b4 = _as4(bpos) if len(bpos) else np.zeros((0, 4), np.float32)
+        self._check(self.L.fsph_set_boundary(self._ctx, _ptr(b4) if b4.shape[0] else None, b4.shape[0], abi.HOST),
+                    "fsph_set_boundary")
+
+    def GetNumBoundaryParticles(self) -> int:
+        return int(self.L.fsph_num_boundary(self._ctx))
+
+    def GetBoundary(self, which: int) -> np.ndarray:
+        """abi.BOUNDARY_POSITION (NB,4), BOUNDARY_VOLUME psi_b (NB,) or BOUNDARY_LAMBDA (NB,)."""
+        nb = self.GetNumBoundaryParticles()
+        out = np.zeros((nb, 4) if which == abi.BOUNDARY_POSITION else (nb,), np.float32)
+        if nb:
+            self._check(self.L.fsph_get_boundary(self._ctx, which, _ptr(out)), "fsph_get_boundary")
+        return out
+
     def EvalScalingFactor(self, pos):
         """calScalingFactor on the given predicted positions (rx_sph_pbd.cpp:699-914)."""
         pos4 = _as4(pos)

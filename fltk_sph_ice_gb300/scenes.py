@@ -101,6 +101,7 @@ class Scene:
     dt: float
     steps: int
     fixed_iters: int = 0     # > 0: run exactly this many PBF iterations per step
+    boundary: np.ndarray | None = None   # (NB, 4) float32 static boundary particles
 
     @property
     def n(self) -> int:
@@ -198,26 +199,68 @@ def pbf_double_dam_break(block=(64, 64, 128), h: float = H_DEFAULT, seed: int = 
     return Scene("pbf_double_dam_break", pos, np.zeros_like(pos), p, 0.0016, 500)
 
 
-def batched_scenes(count: int = 256, seed: int = 4, n_lo: int = 2048, n_hi: int = 65536) -> list[Scene]:
-    """Independent PBF scenes: N_s log-uniform in [n_lo, n_hi], box side
-    uniform in [0.3, 1.0]^3, fill fraction uniform in [0.2, 0.5]; spacing
-    (fill V / N_s)^(1/3) and h = 2 spacing, so every scene keeps ~33 neighbours."""
+def batched_scenes(count: int = 256, seed: int = 4, n_lo: int = 2048, n_hi: int = 65536,
+                   h: float = H_DEFAULT) -> list[Scene]:
+    """Independent PBF scenes: N_s log-uniform in [n_lo, n_hi], box sides
+    uniform in [0.3, 1.0] (the box's proportions), fill fraction uniform in
+    [0.2, 0.5].  As in the other workloads h and the constants stay fixed
+    (spacing h/2, ~33 neighbours) and the box is scaled so that the N_s-
+    particle block fills the stated fraction of it: with the stated 0.3-1.0
+    sides themselves h would have to shrink per scene, and at the fixed
+    dt = 0.0016 the reference's dt^2-scaled s_corr term then dominates lambda
+    in the small-h scenes and the step diverges (seen on the CPU oracle)."""
     idx = np.arange(count, dtype=np.int64)
     un = uniform(seed, 100, idx)
     ub = [uniform(seed, 101 + a, idx) for a in range(3)]
     uf = uniform(seed, 104, idx)
+    sp = 0.5 * h
     out = []
     for s_i in range(count):
         n_target = int(round(math.exp(math.log(n_lo) + un[s_i] * (math.log(n_hi) - math.log(n_lo)))))
-        L = [0.3 + 0.7 * ub[a][s_i] for a in range(3)]
+        shape = [0.3 + 0.7 * ub[a][s_i] for a in range(3)]
         fill = 0.2 + 0.3 * uf[s_i]
-        vol = fill * L[0] * L[1] * L[2]
-        sp = (vol / n_target) ** (1.0 / 3.0)
+        scale = (n_target * sp ** 3 / (fill * shape[0] * shape[1] * shape[2])) ** (1.0 / 3.0)
+        L = [scale * shape[a] for a in range(3)]
         ext = [L[a] * fill ** (1.0 / 3.0) for a in range(3)]
         dims = [max(2, int(round(e / sp))) for e in ext]
-        h = 2.0 * sp
         box_max = [max(L[a], dims[a] * sp + 0.05 * h) for a in range(3)]
         pos = lattice_block(_block_origin([0, 0, 0], h), dims, sp, 0.01 * h, seed + 1000 + s_i, 0)
         p = pbf_params(h, [0, 0, 0], box_max, pos.shape[0])
         out.append(Scene(f"batched_{s_i}", pos, np.zeros_like(pos), p, 0.0016, 500, fixed_iters=4))
     return out
+
+
+def box_surface(lo, side: float, spacing: float) -> np.ndarray:
+    """Particles on the surface of the axis-aligned cube [lo, lo + side]^3: the
+    lattice points of an m^3 grid (m = side / spacing, rounded) that lie on
+    the cube's faces, each once -- the role of rxSolid::GenerateParticlesOnSurf
+    for a box (rx_sph_pbd.cpp:180, spacing 1.2 r there)."""
+    m = max(1, int(round(side / spacing)))
+    s = side / m
+    g = np.arange(m + 1)
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    on = (x == 0) | (x == m) | (y == 0) | (y == m) | (z == 0) | (z == m)
+    pts = np.stack([x[on], y[on], z[on]], axis=1).astype(np.float64) * s + np.asarray(lo, np.float64)
+    out = np.zeros((pts.shape[0], 4), np.float32)
+    out[:, :3] = pts
+    return out
+
+
+def pbf_obstacle_drop(n_side: int = 256, h: float = H_DEFAULT, seed: int = 5) -> Scene:
+    """An n_side^3 jittered block (spacing h/2) dropped onto a static box
+    obstacle made of boundary particles (the 16,777,216-particle configuration
+    at n_side = 256).  The stated 2 x 2 x 2 box and 0.3 obstacle keep their
+    proportions, scaled so the block fits at the stated h: box L^3 with L =
+    2.6 block sides, obstacle side 0.15 L at the centre, block centred in x and
+    z above it.  Obstacle surface particles at spacing 1.2 r (r = h / 4), as
+    the reference samples solids."""
+    s = 0.5 * h
+    B = n_side * s
+    L = 2.6 * B
+    ob_side = 0.15 * L
+    ob_lo = [0.5 * (L - ob_side)] * 3
+    bnd = box_surface(ob_lo, ob_side, 1.2 * 0.25 * h)
+    o = [0.5 * (L - B) + 0.5 * s, L - B + 0.5 * s, 0.5 * (L - B) + 0.5 * s]
+    pos = lattice_block(o, (n_side, n_side, n_side), s, 0.01 * h, seed, 0)
+    p = pbf_params(h, [0, 0, 0], [L, L, L], pos.shape[0])
+    return Scene("pbf_obstacle_drop", pos, np.zeros_like(pos), p, 0.0016, 100, boundary=bnd)

@@ -115,7 +115,7 @@ typedef struct fsph_params {
     /* GPU grid */
     float cell_skin;         /* cell width = h (1 + cell_skin); the grid is rebuilt
                                 inside a step only when a particle moved more than
-                                cell_skin * h since the last build */
+                                half the skin, cell_skin * h / 2, since the last build */
     int use_graph;           /* 1: capture the step (with a device-side while loop) in a CUDA graph */
     int warm_start;          /* 0: plain; 1: learned MLP warm start of the PBF iterations
                                 (needs fsph_set_warm_start_model) */
@@ -125,7 +125,8 @@ typedef struct fsph_params {
                                 each grid (radius = cell width); 1: walk the 27 cells every pass */
     int collect_features;    /* 1: compute FSPH_FEATURES / FSPH_STEP_CORRECTION every step even
                                 without a warm start (training-data collection) */
-    int reserved[4];
+    int compensated_density; /* 1: Kahan-compensated FP32 density sums in the lambda pass */
+    int reserved[3];
 } fsph_params;
 
 /* Scene description in the reference's own terms (rxSPHEnviroment). */
@@ -256,6 +257,28 @@ int fsph_sph_eval_forces(fsph_ctx *ctx, const float *pos4, const float *vel4, in
 int fsph_pbf_eval_lambda_noalloc(const fsph_params *params, const float *pos4, int n, float *dens,
                                  float *lambda, void *stream);
 
+/* ---- static boundary particles (PBF) ---- */
+/* Replaces the boundary set-up of rxPBDSPH::Initialize (rx_sph_pbd.cpp:180,
+ * 280-297: particles sampled on a solid's surface, then calBoundaryVolumes,
+ * rx_sph_pbd.cpp:1061-1090) and rxPBDSPH_GPU::InitBoundary
+ * (rx_sph_pbd_gpu.cpp:654-754).  The caller gives the boundary particles'
+ * float4 positions (the sampling of a solid is the caller's, e.g. the
+ * surface of a box at spacing 1.2 r as rxSolid::GenerateParticlesOnSurf).
+ * Each then has a volume psi_b = m / sum_b' m W(r_bb'), adds
+ * rho0 psi_b W to the density of fluid neighbours, gets its own lambda_b
+ * every pass and enters the position correction (rx_sph_pbd.cpp:624-644,
+ * 728-818, 824-913, 977-1019; compiled in by RX_USE_BOUNDARY_PARTICLE).
+ * nb = 0 removes the boundary.  The boundary stays fixed. */
+typedef enum fsph_boundary_array {
+    FSPH_BOUNDARY_POSITION = 0,  /* float4 per boundary particle, as given */
+    FSPH_BOUNDARY_VOLUME = 1,    /* psi_b */
+    FSPH_BOUNDARY_LAMBDA = 2     /* lambda_b of the last lambda pass */
+} fsph_boundary_array;
+int fsph_set_boundary(fsph_ctx *ctx, const float *bpos4, int nb, int where);
+int fsph_num_boundary(const fsph_ctx *ctx);
+/* host dst, the given order of the boundary particles */
+int fsph_get_boundary(fsph_ctx *ctx, int which, float *dst);
+
 /* ---- learned warm start ---- */
 /* The network: FSPH_MLP_FEATURES -> 64 -> 64 -> 3, ReLU, BF16 tensor-core
  * arithmetic with FP32 accumulation.  Its parameters are one FP32 blob of
@@ -300,6 +323,48 @@ typedef enum fsph_pass {
  * No counterpart in the reference (its timing was the GUI's RXTIMER splits,
  * rx_sph.h:40-58). */
 int fsph_time_pass(fsph_ctx *ctx, int pass, int reps, float *avg_ms);
+
+/* ---- batched scenes ---- */
+/* Many independent PBF scenes of uneven sizes advanced together: every pass
+ * of the step is one persistent launch over all scenes (tiles of one scene
+ * per block), and the whole step -- a fixed number of constraint
+ * iterations -- is one CUDA graph.  Each scene behaves as its own
+ * rxPBDSPH::Update (rx_sph_pbd.cpp:377-484) with its own fsph_params (h,
+ * mass, box, ...), run for exactly `iterations` iterations; the reference has
+ * no batched form (one rxPBDSPH object per scene, one Update call each).
+ * Arrays cross this interface scene after scene, each scene in its own
+ * particle order; fsph_batch_offsets gives where each scene starts. */
+typedef struct fsph_batch fsph_batch;
+typedef struct fsph_batch_config {
+    int block;         /* threads per block of the persistent launches: 128, 256 or 512 */
+    int lanes;         /* lanes sharing one particle in the constraint passes: 1, 2 or 4 */
+    float cell_skin;   /* cell width = h (1 + cell_skin), in [0.02, 0.5] */
+    int eager;         /* 1: host-driven iteration loop instead of the CUDA graph (same kernels; profilers) */
+} fsph_batch_config;
+/* params[s] (PBF) and counts[s] particles for each of the nscenes scenes. */
+int fsph_batch_create(const fsph_params *params, const int *counts, int nscenes, int iterations,
+                      fsph_batch **out);
+int fsph_batch_destroy(fsph_batch *b);
+const char *fsph_batch_last_error(const fsph_batch *b);
+int fsph_batch_num_particles(const fsph_batch *b);
+/* offsets[nscenes + 1]: first particle of each scene in the batched arrays */
+int fsph_batch_offsets(const fsph_batch *b, int *offsets);
+/* all scenes' float4 positions (and velocities; NULL = zero) back to back */
+int fsph_batch_set_particles(fsph_batch *b, const float *pos4, const float *vel4, int where);
+/* one step of every scene; stream NULL = the batch's own stream */
+int fsph_batch_step(fsph_batch *b, float dt, void *stream);
+/* FSPH_POSITION, FSPH_VELOCITY (float4) or FSPH_DENSITY (float), all scenes */
+int fsph_batch_get_array(fsph_batch *b, int type, void *dst, int where);
+/* the last step's iterations, grid builds and density errors of scene s */
+int fsph_batch_scene_stats(fsph_batch *b, int scene, fsph_step_stats *stats);
+int fsph_batch_set_config(fsph_batch *b, const fsph_batch_config *cfg);
+int fsph_batch_get_config(const fsph_batch *b, fsph_batch_config *cfg);
+/* Autotuner: times `steps` steps of dt under every candidate configuration
+ * (block x lanes x cell skin) from the current state, restores that state,
+ * installs the fastest configuration and returns it with its time per step.
+ * The winner is cached per scene-set signature (counts and parameters) for
+ * the life of the process, and reused without timing. */
+int fsph_batch_autotune(fsph_batch *b, float dt, int steps, fsph_batch_config *best, float *best_ms_per_step);
 
 #ifdef __cplusplus
 }

@@ -58,6 +58,8 @@ def orc_lib() -> ctypes.CDLL:
         L.fsph_orc_destroy.argtypes = [vp]
         L.fsph_orc_set.argtypes = [vp, vp, vp]
         L.fsph_orc_get.argtypes = [vp, ci, vp]
+        L.fsph_orc_set_boundary.argtypes = [vp, vp, ci]
+        L.fsph_orc_get_boundary.argtypes = [vp, ci, vp]
         L.fsph_orc_pbf_step.argtypes = [vp, cf, ci, vp]
         L.fsph_orc_pbf_step.restype = ci
         L.fsph_orc_sph_step.argtypes = [vp, cf]
@@ -104,6 +106,17 @@ class Oracle:
         vec = which in ("pos", "vel", "dp", "ppos", "force", "vort")
         out = np.zeros((self.n, 4) if vec else (self.n,), dtype=np.float32)
         self.L.fsph_orc_get(self.h, code, _vp(out))
+        return out
+
+    def set_boundary(self, bpos4):
+        """Static boundary particles (float4 positions); computes psi_b."""
+        b = np.ascontiguousarray(bpos4, dtype=np.float32).reshape(-1, 4)
+        self.nb = b.shape[0]
+        self.L.fsph_orc_set_boundary(self.h, _vp(b), self.nb)
+
+    def get_boundary(self, which: str) -> np.ndarray:
+        out = np.zeros(getattr(self, "nb", 0), dtype=np.float32)
+        self.L.fsph_orc_get_boundary(self.h, {"vol": 0, "lambda": 1}[which], _vp(out))
         return out
 
     def pbf_step(self, dt: float, fixed_iters: int = 0):

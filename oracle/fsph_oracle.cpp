@@ -99,6 +99,11 @@ struct Solver {
     int n = 0;
     std::vector<T> pos, vel, ppos, pvel, frc, dens, pres, lam, dp, vort;
     std::vector<int> noff, nidx; /* neighbour CSR */
+    /* static boundary particles: positions, volumes psi_b, lambda_b, and the
+     * boundary-boundary, fluid-boundary and boundary-fluid neighbour CSRs */
+    int nb = 0;
+    std::vector<T> bpos, bvol, blam;
+    std::vector<int> bb_off, bb_idx, fb_off, fb_idx, bf_off, bf_idx;
     Kern K;
     int last_iters = 0;
     double last_err1 = 0, last_err2 = 0, last_errmax = 0;
@@ -178,6 +183,107 @@ struct Solver {
         for (int i = 0; i < n; ++i) std::copy(lists[i].begin(), lists[i].end(), nidx.begin() + noff[i]);
     }
 
+    /* For every point i of a (na points): the points j of b (nbp points)
+     * with fl(|a_i - b_j|^2) <= fl(h*h), ascending j -- the criterion of
+     * rxNNGrid::GetNN(pos, ...) (rx_nnsearch.h:454-515) between two sets. */
+    void cross_sets(const std::vector<T> &a, int na, const std::vector<T> &b, int nbp, std::vector<int> &off,
+               std::vector<int> &idx) const {
+        const T hT = (T)P.h;
+        const T h2 = hT * hT;
+        off.assign(na + 1, 0);
+        idx.clear();
+        if (nbp == 0 || na == 0) return;
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int j = 0; j < nbp; ++j)
+            for (int k = 0; k < 3; ++k) {
+                double v = (double)b[4 * (size_t)j + k];
+                lo[k] = std::min(lo[k], v); hi[k] = std::max(hi[k], v);
+            }
+        const double cw = (double)P.h * 1.0001;
+        int g[3];
+        for (int k = 0; k < 3; ++k) g[k] = std::max(1, (int)std::floor((hi[k] - lo[k]) / cw) + 1);
+        const size_t C = (size_t)g[0] * g[1] * g[2];
+        std::vector<int> cnt(C + 1, 0), cellOf(nbp), order(nbp);
+        for (int j = 0; j < nbp; ++j) {
+            int c[3];
+            for (int k = 0; k < 3; ++k)
+                c[k] = std::min(std::max((int)std::floor(((double)b[4 * (size_t)j + k] - lo[k]) / cw), 0), g[k] - 1);
+            cellOf[j] = (int)(((size_t)c[2] * g[1] + c[1]) * g[0] + c[0]);
+            cnt[cellOf[j] + 1]++;
+        }
+        for (size_t c = 0; c < C; ++c) cnt[c + 1] += cnt[c];
+        {
+            std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+            for (int j = 0; j < nbp; ++j) order[fill[cellOf[j]]++] = j;
+        }
+        std::vector<std::vector<int>> lists(na);
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int i = 0; i < na; ++i) {
+            V3 xi = v3((double)a[4 * (size_t)i], (double)a[4 * (size_t)i + 1], (double)a[4 * (size_t)i + 2]);
+            long long c0[3];
+            double xs[3] = {xi.x, xi.y, xi.z};
+            for (int k = 0; k < 3; ++k) c0[k] = (long long)std::floor((xs[k] - lo[k]) / cw);
+            std::vector<int> &L = lists[i];
+            for (long long z = c0[2] - 1; z <= c0[2] + 1; ++z)
+                for (long long y = c0[1] - 1; y <= c0[1] + 1; ++y)
+                    for (long long x = c0[0] - 1; x <= c0[0] + 1; ++x) {
+                        if (x < 0 || y < 0 || z < 0 || x >= g[0] || y >= g[1] || z >= g[2]) continue;
+                        size_t cc = ((size_t)z * g[1] + y) * g[0] + x;
+                        for (int s = cnt[cc]; s < cnt[cc + 1]; ++s) {
+                            int j = order[s];
+                            V3 d = xi - v3((double)b[4 * (size_t)j], (double)b[4 * (size_t)j + 1],
+                                           (double)b[4 * (size_t)j + 2]);
+                            T d2 = (T)dot(d, d);
+                            if (d2 <= h2) L.push_back(j);
+                        }
+                    }
+            std::sort(L.begin(), L.end());
+        }
+        for (int i = 0; i < na; ++i) off[i + 1] = off[i] + (int)lists[i].size();
+        idx.resize(off[na]);
+        for (int i = 0; i < na; ++i) std::copy(lists[i].begin(), lists[i].end(), idx.begin() + off[i]);
+    }
+
+    V3 bat(int b) const { return at(bpos, b); }
+
+    /* Static boundary particles and their volumes psi_b = m / sum_b' m W(r_bb')
+     * (rxPBDSPH::calBoundaryVolumes, rx_sph_pbd.cpp:1061-1090), float
+     * accumulation of the double kernel values as in the reference. */
+    void set_boundary(const float *b4, int count) {
+        nb = count;
+        bpos.assign(4 * (size_t)nb, 0);
+        for (size_t k = 0; k < 4 * (size_t)nb; ++k) bpos[k] = (T)b4[k];
+        bvol.assign(nb, 0);
+        blam.assign(nb, 0);
+        cross_sets(bpos, nb, bpos, nb, bb_off, bb_idx);
+        const T m = (T)P.mass;
+        for (int i = 0; i < nb; ++i) {
+            T mw = 0;
+            for (int s = bb_off[i]; s < bb_off[i + 1]; ++s) {
+                V3 d = bat(bb_idx[s]) - bat(i);
+                T r = (T)std::sqrt(dot(d, d));
+                acc_add(mw, (double)m * K.W((double)r));
+            }
+            bvol[i] = m / mw;
+        }
+    }
+
+    /* rho0 psi_b / m of boundary particle b, in float as the reference forms it */
+    T bscale(int b) const { return (T)P.rest_dens * bvol[b] / (T)P.mass; }
+
+    /* sum_b rho0 psi_b W(|x_i - x_b|) over the boundary neighbours of fluid i
+     * (rx_sph_pbd.cpp:624-644) */
+    T boundary_density(const V3 &xi, int i) const {
+        T brho = 0;
+        for (int s = fb_off[i]; s < fb_off[i + 1]; ++s) {
+            int b = fb_idx[s];
+            V3 d = bat(b) - xi;
+            T r = (T)std::sqrt(dot(d, d));
+            acc_add(brho, (double)((T)P.rest_dens * bvol[b]) * K.W((double)r));
+        }
+        return brho;
+    }
+
     /* Box-wall projection keeping the particle radius from every face
      * (rxSolidBox::GetDistanceR -> AABB_point_dist with sgn = 1, contact =
      * pos + n |d|).  Velocity is left unchanged: the reflection is commented
@@ -234,6 +340,7 @@ struct Solver {
 
     /* rho_i = sum_j m W(r_ij), self included. */
     void density(const std::vector<T> &p, std::vector<T> &rho) {
+        if (nb) cross_sets(p, n, bpos, nb, fb_off, fb_idx);
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; ++i) {
             V3 xi = at(p, i);
@@ -243,6 +350,7 @@ struct Solver {
                 T r = (T)std::sqrt(dot(d, d));
                 acc_add(acc, (double)(T)P.mass * K.W((double)r));
             }
+            if (nb) acc = acc + boundary_density(xi, i);
             rho[i] = acc;
         }
     }
@@ -273,6 +381,7 @@ struct Solver {
      * with the k = i term |sum_j grad W_ij / rho0|^2 (rx_sph_pbd.cpp:699-914). */
     void lambda_pass(const std::vector<T> &p) {
         const double r0 = (double)(T)P.rest_dens;
+        if (nb) cross_sets(p, n, bpos, nb, fb_off, fb_idx);
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; ++i) {
             V3 xi = at(p, i);
@@ -289,10 +398,66 @@ struct Solver {
                 if (j != i) acc_add(sd, dot(g, g));
             }
             acc_add(sd, dot(gsum, gsum));
+            if (nb) {
+                /* boundary density and |grad C|^2 terms (rx_sph_pbd.cpp:728-748,
+                 * 795-818), each boundary neighbour counted once as in
+                 * rx_pbdsph_kernel.cu:577-664 */
+                rho = rho + boundary_density(xi, i);
+                for (int s = fb_off[i]; s < fb_off[i + 1]; ++s) {
+                    int b = fb_idx[s];
+                    V3 d = xi - bat(b);
+                    T r = (T)std::sqrt(dot(d, d));
+                    V3 g = ((double)bscale(b) * K.G((double)r) * d) / r0;
+                    acc_add(sd, dot(g, g));
+                }
+            }
             T C = (T)((double)rho / r0) - (T)1;
             if (P.clamp_constraint && C < (T)0) C = (T)0;
             dens[i] = rho;
             lam[i] = (T)(-(double)C / ((double)sd + (double)(T)P.epsilon));
+        }
+        if (nb) boundary_lambda(p);
+    }
+
+    /* lambda_b of every boundary particle from its fluid neighbours at the
+     * current positions and its boundary neighbours (rx_sph_pbd.cpp:825-913;
+     * fluid neighbours found on the current positions as in
+     * rx_pbdsph_kernel.cu:666-735). */
+    void boundary_lambda(const std::vector<T> &p) {
+        const double r0 = (double)(T)P.rest_dens;
+        cross_sets(bpos, nb, p, n, bf_off, bf_idx);
+#pragma omp parallel for schedule(static)
+        for (int b = 0; b < nb; ++b) {
+            V3 xb = bat(b);
+            T brho = 0;
+            for (int s = bf_off[b]; s < bf_off[b + 1]; ++s) {
+                V3 d = at(p, bf_idx[s]) - xb;
+                T r = (T)std::sqrt(dot(d, d));
+                acc_add(brho, (double)(T)P.mass * K.W((double)r));
+            }
+            for (int s = bb_off[b]; s < bb_off[b + 1]; ++s) {
+                int c = bb_idx[s];
+                V3 d = bat(c) - xb;
+                T r = (T)std::sqrt(dot(d, d));
+                acc_add(brho, (double)((T)P.rest_dens * bvol[c]) * K.W((double)r));
+            }
+            T C = (T)((double)brho / r0) - (T)1;
+            if (P.clamp_constraint && C < (T)0) C = (T)0;
+            T sd = 0;
+            for (int s = bf_off[b]; s < bf_off[b + 1]; ++s) {
+                V3 d = xb - at(p, bf_idx[s]);
+                T r = (T)std::sqrt(dot(d, d));
+                V3 g = (K.G((double)r) * d) / r0;
+                acc_add(sd, dot(g, g));
+            }
+            for (int s = bb_off[b]; s < bb_off[b + 1]; ++s) {
+                int c = bb_idx[s];
+                V3 d = xb - bat(c);
+                T r = (T)std::sqrt(dot(d, d));
+                V3 g = ((double)bscale(c) * K.G((double)r) * d) / r0;
+                acc_add(sd, dot(g, g));
+            }
+            blam[b] = (T)(-(double)C / ((double)sd + (double)(T)P.epsilon));
         }
     }
 
@@ -302,6 +467,7 @@ struct Solver {
         const double r0 = (double)(T)P.rest_dens;
         const T dq = (T)P.ap_q * (T)P.h;
         const T wq = (T)K.W((double)dq);
+        if (nb) cross_sets(p, n, bpos, nb, fb_off, fb_idx);
 #pragma omp parallel for schedule(static)
         for (int i = 0; i < n; ++i) {
             V3 xi = at(p, i);
@@ -318,6 +484,25 @@ struct Solver {
                 }
                 T coef = lam[i] + lam[j] + sc;
                 acc = acc + ((double)coef * K.G((double)r) / r0) * d;
+            }
+            if (nb) {
+                /* boundary terms (rx_sph_pbd.cpp:977-1019): lambda_b, and s_corr
+                 * of rho0 psi_b / m scaled W */
+                V3 accb = v3(0, 0, 0);
+                for (int s = fb_off[i]; s < fb_off[i + 1]; ++s) {
+                    int bj = fb_idx[s];
+                    V3 d = xi - bat(bj);
+                    T r = (T)std::sqrt(dot(d, d));
+                    if ((double)r > (double)(T)P.h) continue;
+                    T sc = 0;
+                    if (P.use_ap) {
+                        T ww = (T)((double)bscale(bj) * K.W((double)r) / (double)wq);
+                        sc = (T)(-(double)(T)P.ap_k * std::pow((double)ww, (double)(T)P.ap_n)) * dt * dt;
+                    }
+                    T coef = lam[i] + blam[bj] + sc;
+                    accb = accb + ((double)coef * K.G((double)r) / r0) * d;
+                }
+                acc = acc + accb;
             }
             size_t b = 4 * (size_t)i;
             dp[b] = (T)acc.x; dp[b + 1] = (T)acc.y; dp[b + 2] = (T)acc.z; dp[b + 3] = 0;
@@ -527,6 +712,19 @@ void fsph_orc_destroy(fsph_orc *o) {
 
 void fsph_orc_set(fsph_orc *o, const float *pos4, const float *vel4) {
     ORC_DISPATCH(o, { load4(S->pos, pos4, S->n); load4(S->vel, vel4, S->n); });
+}
+
+/* Static boundary particles (float4 positions); computes their volumes. */
+void fsph_orc_set_boundary(fsph_orc *o, const float *bpos4, int nb) {
+    ORC_DISPATCH(o, S->set_boundary(bpos4, nb));
+}
+
+/* which: 0 volume psi_b, 1 lambda_b of the last lambda pass (nb floats) */
+void fsph_orc_get_boundary(fsph_orc *o, int which, float *out) {
+    ORC_DISPATCH(o, {
+        if (which == 0) store(out, S->bvol);
+        else store(out, S->blam);
+    });
 }
 
 /* which: 0 pos, 1 vel, 2 dens, 3 lambda, 4 dp, 5 predicted pos, 6 force, 7 pressure, 8 vorticity */

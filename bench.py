@@ -528,6 +528,130 @@ def batched_arm(args):
     return 0
 
 
+LARGE_METRIC = ("PBF particle-steps/s at 16.8M particles with a boundary obstacle, learned warm start, "
+                "0.1% density error")
+LARGE_PREROLL = 10
+LARGE_REPLICA = 16       # lattice side of the replica the FP64 oracle follows step by step
+LARGE_REPLICA_STEPS = 20
+LARGE_REPLICA_ITERS = 10
+
+
+def fp64_error_per_step(abi, rxPBDSPH, scenes):
+    """FP32 GPU (compensated density) against the FP64 oracle, step by step,
+    on a small replica of the obstacle scene, both with a fixed iteration
+    count: max |x_gpu - x_fp64| / h per step."""
+    import oracle
+    sc = scenes.pbf_obstacle_drop(n_side=LARGE_REPLICA)
+    p = sc.params
+    p.min_iter = p.max_iter = LARGE_REPLICA_ITERS
+    p.compensated_density = 1
+    ps = rxPBDSPH(p)
+    ps.Set(sc.pos, sc.vel)
+    ps.SetBoundary(sc.boundary)
+    o = oracle.Oracle(p, sc.n, precision="double", threads=host_cores())
+    o.set(sc.pos, sc.vel)
+    o.set_boundary(sc.boundary)
+    out = []
+    for _ in range(LARGE_REPLICA_STEPS):
+        ps.Update(sc.dt)
+        o.pbf_step(sc.dt, fixed_iters=LARGE_REPLICA_ITERS)
+        d = ps.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64) - o.get("pos")[:, :3]
+        out.append(float(np.abs(d).max() / p.h))
+    ps.close()
+    return {"replica_particles": sc.n, "replica_boundary": int(sc.boundary.shape[0]),
+            "iterations": LARGE_REPLICA_ITERS, "max_abs_position_error_over_h": out}
+
+
+def large_arm(args):
+    """The 16.8M-particle obstacle drop (a 256^3 block onto a box of boundary
+    particles), compensated density sums, learned warm start iterating to the
+    0.1 % criterion; plain form beside it; FP64 error per step on a replica."""
+    import torch
+    from fltk_sph_ice_gb300 import abi, build, rxPBDSPH, scenes, warmstart
+
+    rank, world, local = rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    build.build()
+    L = abi.lib()
+    blob, meta = warmstart.load_model(args.model)
+    sc = scenes.pbf_obstacle_drop(n_side=256)
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def leg(warm: bool):
+        p = abi.FsphParams.from_buffer_copy(sc.params)
+        p.eta, p.error_mode, p.clamp_constraint = 1e-3, abi.ERR_ONE_SIDED, 1
+        p.min_iter, p.max_iter, p.use_graph = 2, 400, 1
+        p.compensated_density = 1
+        p.warm_start = 1 if warm else 0
+        ps = rxPBDSPH(p)
+        if warm and L.fsph_set_warm_start_model(ps.handle, blob.ctypes.data_as(ctypes.c_void_p)) != abi.OK:
+            raise RuntimeError("fsph_set_warm_start_model")
+        ps.Set(sc.pos, sc.vel)
+        ps.SetBoundary(sc.boundary)
+        stats = abi.FsphStepStats()
+        for _ in range(LARGE_PREROLL + max(args.warmup, 3)):
+            if L.fsph_step(ps.handle, ctypes.c_float(sc.dt), sp, None) != abi.OK:
+                raise RuntimeError(L.fsph_last_error(ps.handle).decode())
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        iters, errs, kern = [], [], 0
+        if dist:
+            dist.barrier()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev[k][0].record(stream)
+            L.fsph_step(ps.handle, ctypes.c_float(sc.dt), sp, None)
+            ev[k][1].record(stream)
+            stream.synchronize()
+            L.fsph_last_stats(ps.handle, ctypes.byref(stats))
+            iters.append(stats.iterations)
+            errs.append(stats.density_error_one_sided)
+            kern += stats.kernels
+        tot_s = sum(a.elapsed_time(c) for a, c in ev) / 1000.0
+        value, tot_s = replica_rate(sc.n, args.steps, tot_s, dist)
+        ps.close()
+        return {"value": value, "ms_per_step": 1000.0 * tot_s / args.steps, "mean_iterations": float(np.mean(iters)),
+                "max_error": float(np.max(errs)), "kernels": kern}
+
+    with ClockSampler(local) as clk:
+        plain = leg(False) if not args.no_plain else None
+        warm = leg(True)
+    fp64 = fp64_error_per_step(abi, rxPBDSPH, scenes) if rank == 0 and not args.no_cpu else None
+    peak, peak_kind = measured_peaks()
+    bytes_ps = 396.0 + 60.0 * warm["mean_iterations"]
+    if rank == 0:
+        cfg = {"workload": "pbf_obstacle_drop_16M", "particles": sc.n, "boundary_particles": int(sc.boundary.shape[0]),
+               "block": [256, 256, 256], "dt": sc.dt, "eta_one_sided": 1e-3, "compensated_density": True,
+               "constraint": "unilateral (clamped C >= 0)", "method": "learned warm start (BF16 MLP 16-64-64-3)",
+               "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
+               "preroll_steps": LARGE_PREROLL, "l2": "256 MiB flush between timed steps",
+               "parallelism": f"replicas x{world}", "fp64_error_per_step": fp64}
+        if plain:
+            cfg["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "mean_iterations", "max_error")}
+            cfg["speedup_vs_plain"] = warm["value"] / plain["value"]
+        line = {
+            "metric": LARGE_METRIC, "value": warm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": warm["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+            "config": cfg,
+            "roofline": {"bound": "hbm", "achieved": warm["value"] * bytes_ps / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": warm["value"] * bytes_ps / 1e9 / peak, "traffic": None, "kernel": "whole step",
+                         "bytes_per_particle_step": bytes_ps, "peak_kind": peak_kind},
+            "cpu_baseline": None, "e2e": None, "clocks": clk.summary(), "gpu_launches": warm["kernels"],
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -542,8 +666,9 @@ def main():
                          "which cannot profile kernels inside graphs with conditional nodes)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched_256"],
-                    help="the headline 1M double dam break (default) or the 256-scene batch")
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched_256", "pbf_obstacle_drop_16M"],
+                    help="the headline 1M double dam break (default), the 256-scene batch, or the 16.8M "
+                         "obstacle drop with boundary particles")
     args = ap.parse_args()
     if args.model is None:
         from fltk_sph_ice_gb300 import warmstart
@@ -552,6 +677,8 @@ def main():
         return reference_arm(args)
     if args.workload == "batched_256":
         return batched_arm(args)
+    if args.workload == "pbf_obstacle_drop_16M":
+        return large_arm(args)
     return gpu_arm(args)
 
 

@@ -320,8 +320,13 @@ __global__ void k_pbf_visc(DevParams p, const unsigned int *__restrict__ cell_st
  * into x*.w, block partial errors; the last block reduces the errors in a
  * fixed order, advances the iteration counter and decides whether the
  * device-side loop continues. */
+/* resident blocks per SM the constraint passes are compiled for */
+#ifndef FSPH_PASS_MINB
+#define FSPH_PASS_MINB 1
+#endif
+
 template <bool KAHAN>
-__global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
+__global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens,
                                                    DevCtl *ctl, ErrPartial *part,
                                                    cudaGraphConditionalHandle hwhile, int use_graph,
@@ -347,7 +352,7 @@ __global__ void __launch_bounds__(kBlock) k_lambda(DevParams p, const unsigned i
  * x*_i <- walls(x*_i + dp_i) into the other ping-pong buffer; the largest
  * displacement since the last grid build decides whether the grid must be
  * rebuilt before the next pass. */
-__global__ void __launch_bounds__(kBlock) k_correction(DevParams p, const unsigned int *__restrict__ cell_start,
+__global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_correction(DevParams p, const unsigned int *__restrict__ cell_start,
                                                        float4 *ppos0, float4 *ppos1,
                                                        const float4 *__restrict__ xb, DevCtl *ctl, float *part,
                                                        cudaGraphConditionalHandle hif,

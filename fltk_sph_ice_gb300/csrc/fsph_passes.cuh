@@ -26,7 +26,10 @@ namespace fsph {
  * are bound by load latency, not by arithmetic).  rs: this thread's 9 row
  * starts in shared memory, strided by the block size.  Load selects the
  * load flavour for x. */
-constexpr int kBatch = 4;
+#ifndef FSPH_KBATCH
+#define FSPH_KBATCH 4
+#endif
+constexpr int kBatch = FSPH_KBATCH;
 
 template <int LPP, class Load, class F>
 __device__ __forceinline__ void for_each_candidate(const DevParams &p, const unsigned int *__restrict__ cell_start,

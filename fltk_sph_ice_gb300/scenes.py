@@ -252,15 +252,16 @@ def pbf_obstacle_drop(n_side: int = 256, h: float = H_DEFAULT, seed: int = 5) ->
     at n_side = 256).  The stated 2 x 2 x 2 box and 0.3 obstacle keep their
     proportions, scaled so the block fits at the stated h: box L^3 with L =
     2.6 block sides, obstacle side 0.15 L at the centre, block centred in x and
-    z above it.  Obstacle surface particles at spacing 1.2 r (r = h / 4), as
-    the reference samples solids."""
+    z one h above it (so the impact starts within a few steps).  Obstacle
+    surface particles at spacing 1.2 r (r = h / 4), as the reference samples
+    solids."""
     s = 0.5 * h
     B = n_side * s
     L = 2.6 * B
     ob_side = 0.15 * L
     ob_lo = [0.5 * (L - ob_side)] * 3
     bnd = box_surface(ob_lo, ob_side, 1.2 * 0.25 * h)
-    o = [0.5 * (L - B) + 0.5 * s, L - B + 0.5 * s, 0.5 * (L - B) + 0.5 * s]
+    o = [0.5 * (L - B) + 0.5 * s, ob_lo[1] + ob_side + h + 0.5 * s, 0.5 * (L - B) + 0.5 * s]
     pos = lattice_block(o, (n_side, n_side, n_side), s, 0.01 * h, seed, 0)
     p = pbf_params(h, [0, 0, 0], [L, L, L], pos.shape[0])
     return Scene("pbf_obstacle_drop", pos, np.zeros_like(pos), p, 0.0016, 100, boundary=bnd)

@@ -461,7 +461,12 @@ def batched_arm(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     for _ in range(BATCH_PREROLL):
         b.step(dt, sp)
-    cfg, tune_ms = b.autotune(dt, steps=3)
+    if args.no_tune:  # the default configuration (256 threads, 1 lane, skin 0.05)
+        cfg, tune_ms = b.config, None
+    else:
+        cfg, tune_ms = b.autotune(dt, steps=3)
+    if args.eager:  # the same kernels with the loop on the host (profilers)
+        b.set_config(cfg.block, cfg.lanes, cfg.cell_skin, eager=True)
     for _ in range(max(args.warmup, 3)):
         b.step(dt, sp)
     torch.cuda.synchronize()
@@ -666,6 +671,7 @@ def main():
                          "which cannot profile kernels inside graphs with conditional nodes)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="batched_256: skip the autotuner, default launch shape")
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched_256", "pbf_obstacle_drop_16M"],
                     help="the headline 1M double dam break (default), the 256-scene batch, or the 16.8M "
                          "obstacle drop with boundary particles")

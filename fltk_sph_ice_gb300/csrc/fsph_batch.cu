@@ -94,7 +94,7 @@ template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_build_list(BatchArgs b, const unsigned int *__restrict__ cell_start,
                                                        const float4 *__restrict__ xb,
                                                        const unsigned int *__restrict__ cellb,
-                                                       unsigned short *__restrict__ list,
+                                                       ListEntry *__restrict__ list,
                                                        unsigned char *__restrict__ cnt) {
     __shared__ DevParams s_p;
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
@@ -107,10 +107,11 @@ __global__ void __launch_bounds__(BLOCK) kb_build_list(BatchArgs b, const unsign
 /* lambda pass over all scenes; lp holds the loop constants (n = all
  * particles, min_iter = max_iter = the fixed iteration count). */
 template <int BLOCK, int LPP>
-__global__ void __launch_bounds__(BLOCK) kb_lambda(BatchArgs b, DevParams lp, const unsigned int *__restrict__ cell_start,
+__global__ void __launch_bounds__(BLOCK, FSPH_PASS_MINB * 256 / BLOCK)
+    kb_lambda(BatchArgs b, DevParams lp, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens, DevCtl *ctl,
                                                    ErrPartial *part, cudaGraphConditionalHandle hwhile, int use_graph,
-                                                   const unsigned short *__restrict__ list,
+                                                   const ListEntry *__restrict__ list,
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb) {
     __shared__ DevParams s_p;
@@ -138,12 +139,12 @@ __global__ void __launch_bounds__(BLOCK) kb_lambda(BatchArgs b, DevParams lp, co
 /* correction pass over all scenes; the rebuild measure is the largest
  * |x* - xb|^2 / skin2 of the particle's own scene (lp.skin2 = 1). */
 template <int BLOCK, int LPP>
-__global__ void __launch_bounds__(BLOCK) kb_correction(BatchArgs b, DevParams lp,
+__global__ void __launch_bounds__(BLOCK, FSPH_PASS_MINB * 256 / BLOCK) kb_correction(BatchArgs b, DevParams lp,
                                                        const unsigned int *__restrict__ cell_start, float4 *ppos0,
                                                        float4 *ppos1, const float4 *__restrict__ xb, DevCtl *ctl,
                                                        float *part, cudaGraphConditionalHandle hif,
                                                        cudaGraphConditionalHandle hif2, int use_graph,
-                                                       const unsigned short *__restrict__ list,
+                                                       const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
                                                        const unsigned int *__restrict__ cellb) {
     __shared__ DevParams s_p;
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(BLOCK) kb_xsph_vort(BatchArgs b, const unsigne
                                                       const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                       const float *__restrict__ dens, float4 *__restrict__ vel_out,
                                                       float4 *__restrict__ vort,
-                                                      const unsigned short *__restrict__ list,
+                                                      const ListEntry *__restrict__ list,
                                                       const unsigned char *__restrict__ cnt,
                                                       const unsigned int *__restrict__ cellb) {
     __shared__ DevParams s_p;
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(BLOCK) kb_vort_apply(BatchArgs b, const unsign
                                                        const float4 *__restrict__ pos, const float4 *__restrict__ vort,
                                                        const float *__restrict__ dens,
                                                        const float4 *__restrict__ vel_in, float4 *__restrict__ vel_out,
-                                                       const unsigned short *__restrict__ list,
+                                                       const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
                                                        const unsigned int *__restrict__ cellb) {
     __shared__ DevParams s_p;
@@ -732,7 +733,7 @@ int fsph_batch_create(const fsph_params *params, const int *counts, int nscenes,
         if (counts[s] < 0) return FSPH_INVALID_ARG;
         total += counts[s];
     }
-    /* 16-bit list offsets and 32-bit slots: keep the batch below 2^31 particles */
+    /* 32-bit slots and list entries: keep the batch well below 2^31 particles */
     if (total > (1ll << 30)) return FSPH_INVALID_ARG;
     fsph_batch *b = new (std::nothrow) fsph_batch();
     if (!b) return FSPH_OOM;

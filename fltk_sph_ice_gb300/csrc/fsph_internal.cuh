@@ -56,11 +56,23 @@ struct DevParams {
 
 /* Neighbour lists: up to kListMax entries per particle, transposed
  * (entry k of slot i at [k * n + i]) so a warp's lanes read consecutive
- * 16-bit words; an entry is (row << 12) | (j - row_start), row = the
+ * words.  An entry is the candidate's slot (32 bits).  Built with
+ * FSPH_LIST16 it is (row << 12) | (j - row_start) in 16 bits, row = the
  * (dz, dy) index 0..8 of the 27-cell neighbourhood of the particle's build
- * cell.  A count of kListOverflow sends the particle to the cell walk. */
+ * cell: half the list bytes, but every candidate then pays a shared-memory
+ * row-start lookup, and the passes are bound by instruction issue (the
+ * 32-bit form measured 14 % faster per step).  A count of kListOverflow
+ * sends the particle to the cell walk. */
 constexpr int kListMax = 64;
 constexpr unsigned char kListOverflow = 255;
+#ifndef FSPH_LIST16
+#define FSPH_LIST32
+#endif
+#ifdef FSPH_LIST32
+typedef unsigned int ListEntry;   /* the candidate's slot itself */
+#else
+typedef unsigned short ListEntry; /* (row << 12) | (slot - row start) */
+#endif
 
 /* Warm-start features of a particle at the end of a step, all dimensionless:
  *   0 rho/rho0 - 1 of the last lambda pass     1 lambda rho0 h^2

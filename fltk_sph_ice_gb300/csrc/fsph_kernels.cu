@@ -243,7 +243,7 @@ __global__ void k_rebuild_copy(int n, DevCtl *ctl, const float4 *__restrict__ t_
  * build positions xb, self included, as (row << 12) | (j - row_start). */
 __global__ void k_build_list(DevParams p, const unsigned int *__restrict__ cell_start,
                              const float4 *__restrict__ xb, const unsigned int *__restrict__ cellb,
-                             unsigned short *__restrict__ list, unsigned char *__restrict__ cnt) {
+                             ListEntry *__restrict__ list, unsigned char *__restrict__ cnt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     build_list_body(p, i, cell_start, xb, cellb, list, cnt);
@@ -320,17 +320,12 @@ __global__ void k_pbf_visc(DevParams p, const unsigned int *__restrict__ cell_st
  * into x*.w, block partial errors; the last block reduces the errors in a
  * fixed order, advances the iteration counter and decides whether the
  * device-side loop continues. */
-/* resident blocks per SM the constraint passes are compiled for */
-#ifndef FSPH_PASS_MINB
-#define FSPH_PASS_MINB 1
-#endif
-
 template <bool KAHAN>
 __global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens,
                                                    DevCtl *ctl, ErrPartial *part,
                                                    cudaGraphConditionalHandle hwhile, int use_graph,
-                                                   const unsigned short *__restrict__ list,
+                                                   const ListEntry *__restrict__ list,
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb) {
     __shared__ unsigned int s_rs[9 * kBlock];
@@ -358,7 +353,7 @@ __global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_correction(DevParams
                                                        cudaGraphConditionalHandle hif,
                                                        cudaGraphConditionalHandle hif2, int use_graph,
                                                        float4 *__restrict__ dp_out,
-                                                       const unsigned short *__restrict__ list,
+                                                       const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
                                                        const unsigned int *__restrict__ cellb) {
     __shared__ unsigned int s_rs[9 * kBlock];
@@ -404,7 +399,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph_vort(DevParams p, const unsigne
                                                       const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                       const float *__restrict__ dens, float4 *__restrict__ vel_out,
                                                       float4 *__restrict__ vort, FeatureOut fo,
-                                                      const unsigned short *__restrict__ list,
+                                                      const ListEntry *__restrict__ list,
                                                       const unsigned char *__restrict__ cnt,
                                                       const unsigned int *__restrict__ cellb) {
     __shared__ unsigned int s_rs[9 * kBlock];
@@ -421,7 +416,7 @@ __global__ void __launch_bounds__(kBlock) k_vort_apply(DevParams p, const unsign
                                                        const float *__restrict__ dens,
                                                        const float4 *__restrict__ vel_in,
                                                        float4 *__restrict__ vel_out,
-                                                       const unsigned short *__restrict__ list,
+                                                       const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
                                                        const unsigned int *__restrict__ cellb) {
     __shared__ unsigned int s_rs[9 * kBlock];

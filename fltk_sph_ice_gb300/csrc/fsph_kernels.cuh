@@ -52,7 +52,7 @@ void launch_rebuild_gather(int n, const unsigned int *perm, const DevCtl *ctl, c
 
 /* neighbour lists (see fsph_internal.cuh) */
 struct NbrLists {
-    unsigned short *list = nullptr;  /* [kListMax][n] */
+    ListEntry *list = nullptr;       /* [kListMax][n] */
     unsigned char *cnt = nullptr;    /* [n], kListOverflow = use the cell walk */
     unsigned int *cellb = nullptr;   /* [n] build cell of each slot */
 };

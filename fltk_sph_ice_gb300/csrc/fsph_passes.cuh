@@ -29,30 +29,42 @@ namespace fsph {
 #ifndef FSPH_KBATCH
 #define FSPH_KBATCH 4
 #endif
+
+/* resident 256-thread blocks per SM the constraint passes are compiled for:
+ * 6 caps them at 42 registers, 48 warps per SM (measured best) */
+#ifndef FSPH_PASS_MINB
+#define FSPH_PASS_MINB 6
+#endif
 constexpr int kBatch = FSPH_KBATCH;
 
 template <int LPP, class Load, class F>
 __device__ __forceinline__ void for_each_candidate(const DevParams &p, const unsigned int *__restrict__ cell_start,
-                                                   const unsigned short *__restrict__ list,
+                                                   const ListEntry *__restrict__ list,
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb, int i, float3 xi,
                                                    unsigned int *rs, int sub, Load &&load, F &&f) {
     const int k = list ? (int)cnt[i] : (int)kListOverflow;
     if (k != (int)kListOverflow) {
+#ifndef FSPH_LIST32
         const int cb = (int)cellb[i];
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
             const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
             rs[r * blockDim.x] = __ldg(cell_start + base - 1);
         }
+#endif
         for (int t0 = sub; t0 < k; t0 += kBatch * LPP) {
             unsigned int j[kBatch];
             float4 xj[kBatch];
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) {
                 const int t = t0 + u * LPP < k ? t0 + u * LPP : k - 1;
+#ifdef FSPH_LIST32
+                j[u] = __ldg(list + (size_t)t * p.n + i);
+#else
                 const unsigned int e = __ldg(list + (size_t)t * p.n + i);
                 j[u] = rs[(e >> 12) * blockDim.x] + (e & 0xfffu);
+#endif
             }
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) xj[u] = load(j[u]);
@@ -132,7 +144,7 @@ __device__ __forceinline__ void hash_body(const DevParams &p, int i, float3 x, u
  * build positions xb, self included, as (row << 12) | (j - row_start). */
 __device__ __forceinline__ void build_list_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
                                                 const float4 *__restrict__ xb, const unsigned int *__restrict__ cellb,
-                                                unsigned short *__restrict__ list, unsigned char *__restrict__ cnt) {
+                                                ListEntry *__restrict__ list, unsigned char *__restrict__ cnt) {
     const float3 xi = f3(xb[i]);
     const int cb = (int)cellb[i];
     int k = 0;
@@ -151,7 +163,11 @@ __device__ __forceinline__ void build_list_body(const DevParams &p, int i, const
             for (int u = 0; u < 4; ++u) {
                 const float3 d = xi - f3(xc[u]);
                 if (j0 + u < e && dot3(d, d) < p.rl2) {
-                    if (k < kListMax) list[(size_t)k * p.n + i] = (unsigned short)((r << 12) | (j0 + u - s));
+#ifdef FSPH_LIST32
+                    if (k < kListMax) list[(size_t)k * p.n + i] = j0 + u;
+#else
+                    if (k < kListMax) list[(size_t)k * p.n + i] = (ListEntry)((r << 12) | (j0 + u - s));
+#endif
                     ++k;
                 }
             }
@@ -168,7 +184,7 @@ __device__ __forceinline__ void build_list_body(const DevParams &p, int i, const
 template <int LPP, bool KAHAN = false>
 __device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned int *__restrict__ cell_start,
                                              float4 *pp, float *__restrict__ dens, DevCtl *ctl,
-                                             const unsigned short *__restrict__ list,
+                                             const ListEntry *__restrict__ list,
                                              const unsigned char *__restrict__ cnt,
                                              const unsigned int *__restrict__ cellb, unsigned int *rs, int i, int sub,
                                              bool valid) {
@@ -306,7 +322,7 @@ template <int LPP>
 __device__ __forceinline__ float correction_body(const DevParams &p, const unsigned int *__restrict__ cell_start,
                                                  const float4 *__restrict__ src, float4 *__restrict__ dst,
                                                  const float4 *__restrict__ xb, DevCtl *ctl,
-                                                 float4 *__restrict__ dp_out, const unsigned short *__restrict__ list,
+                                                 float4 *__restrict__ dp_out, const ListEntry *__restrict__ list,
                                                  const unsigned char *__restrict__ cnt,
                                                  const unsigned int *__restrict__ cellb, unsigned int *rs, int i,
                                                  int sub, bool valid) {
@@ -425,7 +441,7 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
                                                const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                const float *__restrict__ dens, float4 *__restrict__ vel_out,
                                                float4 *__restrict__ vort, const FeatureOut &fo,
-                                               const unsigned short *__restrict__ list,
+                                               const ListEntry *__restrict__ list,
                                                const unsigned char *__restrict__ cnt,
                                                const unsigned int *__restrict__ cellb, unsigned int *rs) {
     const float3 xi = f3(pos[i]), vi = f3(vel[i]);
@@ -483,7 +499,7 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
 __device__ __forceinline__ void vort_apply_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
                                                 const float4 *__restrict__ pos, const float4 *__restrict__ vort,
                                                 const float *__restrict__ dens, const float4 *__restrict__ vel_in,
-                                                float4 *__restrict__ vel_out, const unsigned short *__restrict__ list,
+                                                float4 *__restrict__ vel_out, const ListEntry *__restrict__ list,
                                                 const unsigned char *__restrict__ cnt,
                                                 const unsigned int *__restrict__ cellb, unsigned int *rs) {
     float4 v4 = vel_in[i];

@@ -258,7 +258,7 @@ def run_leg(ctx, warm: bool, blob):
         step()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    iters, errs, kernels = [], [], []
+    iters, errs, kernels, builds = [], [], [], []
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -273,6 +273,7 @@ def run_leg(ctx, warm: bool, blob):
         iters.append(stats.iterations)
         errs.append(stats.density_error_one_sided)
         kernels.append(stats.kernels)
+        builds.append(stats.grid_builds)
     torch.cuda.synchronize()
     tot_ms = sum(a.elapsed_time(b) for a, b in ev)
     n = sc.n
@@ -280,7 +281,7 @@ def run_leg(ctx, warm: bool, blob):
     tot_ms = secs * 1000.0
     return ps, sc, {"value": value, "ms_per_step": tot_ms / args.steps,
                     "mean_iterations": float(np.mean(iters)), "max_error": float(np.max(errs)),
-                    "iterations": iters, "kernels": int(sum(kernels))}
+                    "iterations": iters, "kernels": int(sum(kernels)), "grid_builds": float(np.mean(builds))}
 
 
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_lambda_k_correction_pbf_double_dam_break_1M.md")
@@ -407,11 +408,14 @@ def gpu_arm(args):
         cfg = {"workload": WORKLOAD, "particles": n, "block": list(BLOCK), "dt": sc.dt, "eta_one_sided": 1e-3,
                "constraint": "unilateral (clamped C >= 0)", "method": "learned warm start (BF16 MLP 16-64-64-3)",
                "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
-               "model": {"samples": meta.get("samples"), "rollouts": meta.get("rollouts")},
+               "grid_builds_per_step": warm["grid_builds"],
+               "model": {"samples": meta.get("samples"), "rollouts": meta.get("rollouts"),
+                         "output_damping": meta.get("output_damping")},
                "preroll_steps": args.preroll, "l2": "256 MiB flush between timed steps",
                "parallelism": f"replicas x{world}"}
         if plain:
-            cfg["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "mean_iterations", "max_error")}
+            cfg["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "mean_iterations", "max_error",
+                                                  "grid_builds")}
             cfg["speedup_vs_plain"] = warm["value"] / plain["value"]
         line = {
             "metric": METRIC, "value": warm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -484,21 +488,23 @@ def batched_arm(args):
     tot_s = sum(a.elapsed_time(c) for a, c in ev) / 1000.0
     value, tot_s = replica_rate(n, args.steps, tot_s, dist)
     errs = [b.scene_stats(s) for s in range(b.nscenes)]
-    # e2e: the whole batch host -> device, one step, positions and velocities back
-    x_h = torch.from_numpy(b.get(abi.RX_POSITION)).pin_memory().numpy()
-    v_h = torch.from_numpy(b.get(abi.RX_VELOCITY)).pin_memory().numpy()
-    for _ in range(2):
-        b.set_particles(x_h, v_h)
-        b.step(dt)
-        x_h[:] = b.get(abi.RX_POSITION)
-        v_h[:] = b.get(abi.RX_VELOCITY)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        b.set_particles(x_h, v_h)
-        b.step(dt)
-        x_h[:] = b.get(abi.RX_POSITION)
-        v_h[:] = b.get(abi.RX_VELOCITY)
-    e2e_value, _ = replica_rate(n, args.steps, time.perf_counter() - t0, dist)
+    e2e_value = None
+    if not args.no_e2e:
+        # e2e: the whole batch host -> device, one step, positions and velocities back
+        x_h = torch.from_numpy(b.get(abi.RX_POSITION)).pin_memory().numpy()
+        v_h = torch.from_numpy(b.get(abi.RX_VELOCITY)).pin_memory().numpy()
+        for _ in range(2):
+            b.set_particles(x_h, v_h)
+            b.step(dt)
+            x_h[:] = b.get(abi.RX_POSITION)
+            v_h[:] = b.get(abi.RX_VELOCITY)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b.set_particles(x_h, v_h)
+            b.step(dt)
+            x_h[:] = b.get(abi.RX_POSITION)
+            v_h[:] = b.get(abi.RX_VELOCITY)
+        e2e_value, _ = replica_rate(n, args.steps, time.perf_counter() - t0, dist)
     peak, peak_kind = measured_peaks()
     achieved = value * BATCH_BYTES / 1e9
     cpu = None
@@ -523,7 +529,8 @@ def batched_arm(args):
                          "frac": achieved / peak, "traffic": None, "kernel": "whole step",
                          "bytes_per_particle_step": BATCH_BYTES, "peak_kind": peak_kind},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n},
+            "e2e": None if e2e_value is None else {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n,
+                                                   "d2h_bytes_per_step": 32 * n},
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)

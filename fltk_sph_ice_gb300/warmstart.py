@@ -172,9 +172,49 @@ def collect_rollout(block, seed: int, steps: int, per_step: int, skip: int = 5, 
     return np.concatenate(X), np.concatenate(T), iters
 
 
+CALIB_SCENES = (((28, 24, 56), 501), ((24, 16, 48), 502), ((32, 20, 64), 503))
+
+
+def mean_iterations(blob, block, seed: int, steps: int = 60, skip: int = 30) -> float:
+    """Mean constraint iterations per step of a warm-started double dam break
+    (steps skip..steps-1) with the given network."""
+    from .particles import rxPBDSPH
+    L = abi.lib()
+    sc = scenes.pbf_double_dam_break(block=block, seed=seed)
+    p = sc.params
+    p.clamp_constraint, p.eta, p.max_iter, p.warm_start = 1, 1e-3, 400, 1
+    ps = rxPBDSPH(p)
+    st = L.fsph_set_warm_start_model(ps.handle, np.ascontiguousarray(blob, np.float32).ctypes.data_as(ctypes.c_void_p))
+    if st != abi.OK:
+        raise FsphError(st, "fsph_set_warm_start_model")
+    ps.Set(sc.pos, sc.vel)
+    its = []
+    for s in range(steps):
+        ps.Update(sc.dt)
+        if s >= skip:
+            its.append(ps.last_stats.iterations)
+    ps.close()
+    return float(np.mean(its))
+
+
+def calibrate_damping(blob, alphas=(0.6, 0.7, 0.8, 0.9, 1.0)):
+    """The output damping alpha (network output x alpha) that minimises the
+    mean iterations on held-out scenes of the training distribution (seeds
+    not used in training); returns (alpha, {alpha: mean iterations})."""
+    table = {}
+    for a in alphas:
+        b = np.array(blob, np.float32)
+        b[O_SCALE] *= a
+        table[a] = float(np.mean([mean_iterations(b, blk, seed) for blk, seed in CALIB_SCENES]))
+    best = min(table, key=table.get)
+    return best, table
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=DEFAULT_MODEL)
+    ap.add_argument("--calibrate", default=None, metavar="MODEL",
+                    help="only calibrate the output damping of an existing model file, writing --out")
     ap.add_argument("--rollouts", type=int, default=256)
     ap.add_argument("--steps", type=int, default=160)
     ap.add_argument("--per-step", type=int, default=256)
@@ -182,6 +222,17 @@ def main():
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
     args = ap.parse_args()
+    if args.calibrate:
+        blob, meta = load_model(args.calibrate)
+        if "output_damping" in meta:  # undo an earlier calibration first
+            blob[O_SCALE] /= meta["output_damping"]
+        alpha, table = calibrate_damping(blob)
+        blob[O_SCALE] *= alpha
+        meta["output_damping"] = alpha
+        meta["damping_table"] = {str(k): v for k, v in table.items()}
+        save_model(args.out, blob, meta)
+        print(json.dumps({"output_damping": alpha, "mean_iterations": meta["damping_table"]}))
+        return
     t0 = time.time()
     rng = np.random.default_rng(12345)
     X, T = [], []
@@ -205,6 +256,10 @@ def main():
                 epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
                 train_s=time.time() - t0 - t_collect, target_var=float((T / blob[O_SCALE]).var() * 3),
                 blocks=blocks[:8])
+    alpha, table = calibrate_damping(blob)
+    blob[O_SCALE] *= alpha
+    meta["output_damping"] = alpha
+    meta["damping_table"] = {str(k): v for k, v in table.items()}
     save_model(args.out, blob, meta)
     print(json.dumps({k: v for k, v in meta.items() if k != "blocks"}))
 

@@ -113,6 +113,34 @@ def test_autotune_restores_state_and_caches(gpu):
     assert_rel(b.get(abi.RX_POSITION)[:, :3], ref.get(abi.RX_POSITION)[:, :3], 1e-5, "tuned vs default")
 
 
+def test_empty_and_single_scenes(gpu):
+    """Scenes without particles take no tiles and report zero error; a
+    one-scene batch steps like the single-scene path."""
+    sc = small_set(count=2, seed=15)
+    empty = scenes.batched_scenes(count=1, seed=16, n_lo=512, n_hi=600)[0]
+    params = [empty.params, sc[0].params, empty.params, sc[1].params]
+    counts = [0, sc[0].n, 0, sc[1].n]
+    for p in params:
+        p.min_iter = p.max_iter = ITERS
+    b = PBFBatch(params, counts, iterations=ITERS)
+    b.set_particles(np.concatenate([sc[0].pos, sc[1].pos]), np.concatenate([sc[0].vel, sc[1].vel]))
+    b.step(sc[0].dt)
+    assert b.scene_stats(0).density_error_one_sided == 0.0 and b.scene_stats(2).density_error_max == 0.0
+    x = b.get(abi.RX_POSITION)
+    for k, s in ((1, sc[0]), (3, sc[1])):
+        ps = rxPBDSPH(s.params)
+        ps.Set(s.pos, s.vel)
+        ps.Update(s.dt)
+        assert_rel(b.scene(x, k)[:, :3], ps.GetArrayVBO(abi.RX_POSITION)[:, :3], 1e-5, f"scene {k}")
+        ps.close()
+    one = make_batch(sc[:1])
+    one.step(sc[0].dt)
+    ps = rxPBDSPH(sc[0].params)
+    ps.Set(sc[0].pos, sc[0].vel)
+    ps.Update(sc[0].dt)
+    assert_rel(one.get(abi.RX_POSITION)[:, :3], ps.GetArrayVBO(abi.RX_POSITION)[:, :3], 1e-5, "one-scene batch")
+
+
 def test_invalid_arguments(gpu):
     sc = small_set(count=2)
     with pytest.raises(FsphError):

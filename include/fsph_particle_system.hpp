@@ -194,6 +194,20 @@ public:
 class rxPBDSPH : public rxParticleSystemBase {
 public:
     explicit rxPBDSPH(const fsph_params &p) : rxParticleSystemBase(p, FSPH_SOLVER_PBF) {}
+    /* Static boundary particles, 4 floats each (the boundary set-up of
+     * rxPBDSPH::Initialize, rx_sph_pbd.cpp:280-297); an empty vector removes them. */
+    bool SetBoundary(const std::vector<float> &bpos4) {
+        const int nb = (int)(bpos4.size() / 4);
+        m_status = fsph_set_boundary(m_ctx, nb ? bpos4.data() : nullptr, nb, FSPH_HOST);
+        return m_status == FSPH_OK;
+    }
+    int GetNumBoundaryParticles() const { return m_ctx ? fsph_num_boundary(m_ctx) : 0; }
+    /* positions (4 floats each), psi_b or lambda_b, in the given order */
+    std::vector<float> GetBoundary(int which) {
+        std::vector<float> out((size_t)GetNumBoundaryParticles() * (which == FSPH_BOUNDARY_POSITION ? 4 : 1));
+        if (!out.empty()) m_status = fsph_get_boundary(m_ctx, which, out.data());
+        return out;
+    }
     /* Initialize(env) derivation (rx_sph_pbd.cpp:102-201) */
     static fsph_params ParamsFromEnv(const fsph_env &env) {
         fsph_params p;

@@ -61,6 +61,47 @@ def test_step_correction_and_features(gpu):
     np.testing.assert_allclose(x_after[inside, :3], pred[inside] + d[inside], rtol=0, atol=2e-6)
 
 
+def features_numpy(x, v, dens, lam, dstep, p, dt):
+    """The 16 end-of-step features restated by brute force over all pairs (FP64)."""
+    h, r0, m = float(p.h), float(p.rest_dens), float(p.mass)
+    ag = -45.0 / (np.pi * h ** 6)
+    X, V = x[:, :3].astype(np.float64), v[:, :3].astype(np.float64)
+    d = X[:, None, :] - X[None, :, :]                     # x_i - x_j
+    r = np.sqrt((d * d).sum(-1))
+    inside = r * r < h * h
+    cnt = np.maximum(inside.sum(1), 1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        g = np.where((r > 0) & (r < h), ag * (h - r) ** 2 / r, 0.0)   # grad W = g d
+    mrho = m / dens.astype(np.float64)[None, :]
+    vij = V[None, :, :] - V[:, None, :]                   # v_j - v_i
+    f = np.zeros((x.shape[0], 16))
+    f[:, 0] = dens / r0 - 1.0
+    f[:, 1] = lam * r0 * h * h
+    f[:, 2] = inside.sum(1) / 33.0
+    f[:, 3:6] = -(inside[..., None] * d).sum(1) / h / cnt[:, None]
+    f[:, 6:9] = V * dt / h
+    f[:, 9:12] = dstep[:, :3] / h
+    f[:, 12] = (mrho * g * (vij * d).sum(-1)).sum(1) * dt
+    f[:, 13:16] = ((mrho * g)[..., None] * d).sum(1) * h
+    return f
+
+
+def test_features_match_numpy(gpu):
+    """Every feature against a brute-force restatement, on a state where the
+    velocity is the one the feature pass saw (XSPH and vorticity off)."""
+    sc, p = make(block=(10, 8, 20), collect=1, seed=5)
+    p.xsph_c, p.vort_eps = 0.0, 0.0
+    ps, _, _ = run(sc, p, 25)
+    f = ps.GetArrayVBO(abi.FSPH_FEATURES).reshape(sc.n, 16)
+    ref = features_numpy(ps.GetArrayVBO(abi.RX_POSITION), ps.GetArrayVBO(abi.RX_VELOCITY),
+                         ps.GetArrayVBO(abi.RX_DENSITY), ps.GetArrayVBO(abi.RX_SCALING_FACTOR),
+                         ps.GetArrayVBO(abi.RX_STEP_CORRECTION), p, sc.dt)
+    for k in range(16):
+        scale = max(np.abs(ref[:, k]).max(), 1e-3)
+        err = np.abs(f[:, k] - ref[:, k]).max() / scale
+        assert err < 2e-3, (k, err)
+
+
 def test_unknown_warm_start_mode_rejected(gpu):
     sc, p = make(mode=2)
     with pytest.raises(abi.FsphError) as e:

@@ -289,7 +289,8 @@ TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_lambda_k_correction_pbf_doub
 
 def ncu_traffic(kname: str):
     """DRAM bytes (read + write) of one launch of kname at 1M particles, from
-    the committed ncu summary's 'traffic per launch' row; None if absent."""
+    the committed ncu summary's 'traffic per launch' row (its first two
+    columns are the current kernels); None if absent."""
     import re
     if not os.path.isfile(TRAFFIC_PROFILE):
         return None
@@ -298,7 +299,7 @@ def ncu_traffic(kname: str):
             if line.startswith("| **traffic per launch**"):
                 mb = [float(x) for x in re.findall(r"([0-9.]+) MB", line)]
                 col = {"k_lambda": 0, "k_correction": 1}.get(kname)
-                if col is not None and len(mb) == 2:
+                if col is not None and len(mb) >= 2:
                     return mb[col] * 1e6
     return None
 

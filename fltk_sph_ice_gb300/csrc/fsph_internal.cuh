@@ -54,8 +54,8 @@ struct DevParams {
     const unsigned char *bnear; /* 1 when boundary particles lie in the 27 cells around c */
 };
 
-/* Neighbour lists: up to kListMax entries per particle, transposed
- * (entry k of slot i at [k * n + i]) so a warp's lanes read consecutive
+/* Neighbour lists: up to kListMax entries per particle, transposed (entry
+ * k of slot i at list_at(k, i, n)) so a warp's lanes read consecutive
  * words.  An entry is the candidate's slot (32 bits).  Built with
  * FSPH_LIST16 it is (row << 12) | (j - row_start) in 16 bits, row = the
  * (dz, dy) index 0..8 of the 27-cell neighbourhood of the particle's build
@@ -73,6 +73,20 @@ typedef unsigned int ListEntry;   /* the candidate's slot itself */
 #else
 typedef unsigned short ListEntry; /* (row << 12) | (slot - row start) */
 #endif
+/* 32-bit entries are stored in groups of four: group g of slot i is the
+ * 16-byte word [g * n + i], so a warp reads four entries of its 32 slots
+ * with one coalesced 512-byte load; a list's last group is padded with its
+ * last entry.  FSPH_LIST_SCALAR keeps one entry per word ([t * n + i]). */
+#if defined(FSPH_LIST32) && !defined(FSPH_LIST_SCALAR)
+#define FSPH_LIST_GROUPED 1
+#endif
+__host__ __device__ inline size_t list_at(int t, int i, int n) {
+#ifdef FSPH_LIST_GROUPED
+    return ((size_t)(t >> 2) * (size_t)n + (size_t)i) * 4 + (size_t)(t & 3);
+#else
+    return (size_t)t * (size_t)n + (size_t)i;
+#endif
+}
 
 /* Warm-start features of a particle at the end of a step, all dimensionless:
  *   0 rho/rho0 - 1 of the last lambda pass     1 lambda rho0 h^2

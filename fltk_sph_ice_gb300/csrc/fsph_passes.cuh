@@ -44,6 +44,23 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
                                                    const unsigned int *__restrict__ cellb, int i, float3 xi,
                                                    unsigned int *rs, int sub, Load &&load, F &&f) {
     const int k = list ? (int)cnt[i] : (int)kListOverflow;
+#ifdef FSPH_LIST_GROUPED
+    if (LPP == 1 && kBatch == 4 && k != (int)kListOverflow) {
+        /* one 16-byte load brings the next four entries (the tail group is
+         * padded with a valid slot, so every load stays in bounds) */
+        const uint4 *lg = reinterpret_cast<const uint4 *>(list) + i;
+        for (int t0 = 0; t0 < k; t0 += 4) {
+            const uint4 e = __ldg(lg + (size_t)(t0 >> 2) * (size_t)p.n);
+            const unsigned int j[4] = {e.x, e.y, e.z, e.w};
+            float4 xj[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xj[u] = load(j[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (t0 + u < k) f(j[u], xj[u]);
+        }
+    } else
+#endif
     if (k != (int)kListOverflow) {
 #ifndef FSPH_LIST32
         const int cb = (int)cellb[i];
@@ -60,9 +77,9 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
             for (int u = 0; u < kBatch; ++u) {
                 const int t = t0 + u * LPP < k ? t0 + u * LPP : k - 1;
 #ifdef FSPH_LIST32
-                j[u] = __ldg(list + (size_t)t * p.n + i);
+                j[u] = __ldg(list + list_at(t, i, p.n));
 #else
-                const unsigned int e = __ldg(list + (size_t)t * p.n + i);
+                const unsigned int e = __ldg(list + list_at(t, i, p.n));
                 j[u] = rs[(e >> 12) * blockDim.x] + (e & 0xfffu);
 #endif
             }
@@ -149,6 +166,7 @@ __device__ __forceinline__ void build_list_body(const DevParams &p, int i, const
     const int cb = (int)cellb[i];
     int k = 0;
     bool ovf = false;
+    ListEntry last = 0;
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
         const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
@@ -164,16 +182,22 @@ __device__ __forceinline__ void build_list_body(const DevParams &p, int i, const
                 const float3 d = xi - f3(xc[u]);
                 if (j0 + u < e && dot3(d, d) < p.rl2) {
 #ifdef FSPH_LIST32
-                    if (k < kListMax) list[(size_t)k * p.n + i] = j0 + u;
+                    last = j0 + u;
 #else
-                    if (k < kListMax) list[(size_t)k * p.n + i] = (ListEntry)((r << 12) | (j0 + u - s));
+                    last = (ListEntry)((r << 12) | (j0 + u - s));
 #endif
+                    if (k < kListMax) list[list_at(k, i, p.n)] = last;
                     ++k;
                 }
             }
         }
     }
-    cnt[i] = (ovf || k > kListMax) ? kListOverflow : (unsigned char)k;
+    const bool overflow = ovf || k > kListMax;
+#ifdef FSPH_LIST_GROUPED
+    if (!overflow) /* pad the last group (k >= 1: the slot itself is always listed) */
+        for (int t = k; (t & 3) != 0; ++t) list[list_at(t, i, p.n)] = last;
+#endif
+    cnt[i] = overflow ? kListOverflow : (unsigned char)k;
 }
 
 /* ---------------- constraint iterations ---------------- */

@@ -124,6 +124,9 @@ class WarmStartNet:
         for ep in range(epochs):
             perm = torch.randperm(x.shape[0], device="cuda", generator=gen)
             xs, ts = xd[perm].contiguous(), td[perm].contiguous()
+            # the trainer runs on the library's own stream: the shuffled copies
+            # must be complete before it reads them
+            torch.cuda.current_stream().synchronize()
             out = np.zeros(1, np.float32)
             self._check(self.L.fsph_mlp_train(self.h, ctypes.c_void_p(xs.data_ptr()), ctypes.c_void_p(ts.data_ptr()),
                                               x.shape[0], batch, 1, ctypes.c_float(lr * lr_decay ** ep),

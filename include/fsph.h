@@ -297,7 +297,10 @@ int fsph_mlp_destroy(fsph_mlp *m);
 int fsph_mlp_set_blob(fsph_mlp *m, const float *blob);            /* host blob; resets Adam */
 int fsph_mlp_get_blob(fsph_mlp *m, float *blob);                  /* host blob */
 const char *fsph_mlp_last_error(const fsph_mlp *m);
-/* y[n][3] = network(x[n][16]); device pointers; stream NULL = synchronous */
+/* The network's calls run on its own stream (or the given one): device
+ * inputs written by other streams must be complete before a call (for
+ * gradient / train, which take no stream, synchronise the producing stream).
+ * y[n][3] = network(x[n][16]); device pointers; stream NULL = synchronous */
 int fsph_mlp_forward(fsph_mlp *m, const float *x, int n, float *y, void *stream);
 /* gradient of the mean squared error mean_i sum_k (y_ik - t_ik)^2 w.r.t. the
  * blob (host, FSPH_MLP_BLOB_SIZE floats; zero for mu, sigma, out_scale);

@@ -92,7 +92,9 @@ __host__ __device__ inline size_t list_at(int t, int i, int n) {
  *   0 rho/rho0 - 1 of the last lambda pass     1 lambda rho0 h^2
  *   2 neighbour count / 33                     3-5 mean offset to neighbours / h
  *   6-8 v dt / h                               9-11 step correction (x*_final - x*_pred) / h
- *   12 SPH velocity divergence * dt            13-15 colour-field gradient * h
+ *   12 C' = rho'/rho0 - 1 and 13-15 h grad_i C' at the next step's predicted
+ *      relative positions x_ij + dt (v_i - v_j) (the constraint the coming
+ *      iterations will have to remove, from the same neighbour loop)
  * Row-major, kFeatures floats per particle. */
 constexpr int kFeatures = 16;
 struct DevCtl;

@@ -471,7 +471,8 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
     const float3 xi = f3(pos[i]), vi = f3(vel[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), xs = make_float3(0.f, 0.f, 0.f);
     float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
-    float div = 0.f, cntf = 0.f;
+    float cntf = 0.f;
+    float wpred = 0.f; /* sum q^3 at the next step's predicted relative positions */
     /* branch-free pair terms: q and t clamp to zero outside h, and the self
      * pair (d = 0, v_ij = 0) adds only to the neighbour count */
     for_each_candidate<1>(
@@ -490,20 +491,17 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
             xs = xs + (p.aw * q * q * q * mrho) * vij;
             cntf += inside;
             off = off - inside * d;
-#ifdef FSPH_FEAT_PRED
-            if (fo.feat) { /* the pair at the next step's prediction, x + dt v */
+            if (fo.feat) {
+                /* the pair at the next step's prediction x + dt v (gravity cancels
+                 * in relative positions): poly6 and its spiky gradient there */
                 const float3 ds = d - p.dt * vij;
                 const float r2s = dot3(ds, ds);
                 const float qs = fmaxf(p.h2 - r2s, 0.0f);
                 const float inv_rs = rsqrtf(fmaxf(r2s, 1e-20f));
                 const float ts = fmaxf(p.h - r2s * inv_rs, 0.0f);
-                div += qs * qs * qs;
+                wpred += qs * qs * qs;
                 cg = cg + (p.ag * ts * ts * inv_rs) * ds;
             }
-#else
-            div += mrho * g * dot3(vij, d);
-            cg = cg + (mrho * g) * d;
-#endif
         });
     cntf = fmaxf(cntf, 1.0f);
     float3 vn = vi + p.xsph_c * xs;
@@ -521,14 +519,10 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
         f[3] = off.x * inv_h / cntf; f[4] = off.y * inv_h / cntf; f[5] = off.z * inv_h / cntf;
         f[6] = vi.x * p.dt * inv_h; f[7] = vi.y * p.dt * inv_h; f[8] = vi.z * p.dt * inv_h;
         f[9] = dd.x * inv_h; f[10] = dd.y * inv_h; f[11] = dd.z * inv_h;
-#ifdef FSPH_FEAT_PRED
-        const float mr0 = p.mass * p.inv_rest_dens; /* C' and h grad C' at the prediction */
-        f[12] = mr0 * p.aw * div - 1.0f;
+        /* predicted constraint C' = rho' / rho0 - 1 and h grad_i C' at the next prediction */
+        const float mr0 = p.mass * p.inv_rest_dens;
+        f[12] = mr0 * p.aw * wpred - 1.0f;
         f[13] = mr0 * cg.x * p.h; f[14] = mr0 * cg.y * p.h; f[15] = mr0 * cg.z * p.h;
-#else
-        f[12] = div * p.dt;
-        f[13] = cg.x * p.h; f[14] = cg.y * p.h; f[15] = cg.z * p.h;
-#endif
         float4 *out = reinterpret_cast<float4 *>(fo.feat + (size_t)i * kFeatures);
 #pragma unroll
         for (int k = 0; k < kFeatures / 4; ++k) out[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);

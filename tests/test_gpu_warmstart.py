@@ -64,16 +64,18 @@ def test_step_correction_and_features(gpu):
 def features_numpy(x, v, dens, lam, dstep, p, dt):
     """The 16 end-of-step features restated by brute force over all pairs (FP64)."""
     h, r0, m = float(p.h), float(p.rest_dens), float(p.mass)
+    aw = 315.0 / (64.0 * np.pi * h ** 9)
     ag = -45.0 / (np.pi * h ** 6)
     X, V = x[:, :3].astype(np.float64), v[:, :3].astype(np.float64)
     d = X[:, None, :] - X[None, :, :]                     # x_i - x_j
     r = np.sqrt((d * d).sum(-1))
     inside = r * r < h * h
     cnt = np.maximum(inside.sum(1), 1)
+    ds = d - dt * (V[None, :, :] - V[:, None, :])        # x_ij + dt (v_i - v_j)
+    rs = np.sqrt((ds * ds).sum(-1))
+    qs = np.maximum(h * h - rs * rs, 0.0)
     with np.errstate(divide="ignore", invalid="ignore"):
-        g = np.where((r > 0) & (r < h), ag * (h - r) ** 2 / r, 0.0)   # grad W = g d
-    mrho = m / dens.astype(np.float64)[None, :]
-    vij = V[None, :, :] - V[:, None, :]                   # v_j - v_i
+        gs = np.where((rs > 0) & (rs < h), ag * (h - rs) ** 2 / rs, 0.0)
     f = np.zeros((x.shape[0], 16))
     f[:, 0] = dens / r0 - 1.0
     f[:, 1] = lam * r0 * h * h
@@ -81,8 +83,8 @@ def features_numpy(x, v, dens, lam, dstep, p, dt):
     f[:, 3:6] = -(inside[..., None] * d).sum(1) / h / cnt[:, None]
     f[:, 6:9] = V * dt / h
     f[:, 9:12] = dstep[:, :3] / h
-    f[:, 12] = (mrho * g * (vij * d).sum(-1)).sum(1) * dt
-    f[:, 13:16] = ((mrho * g)[..., None] * d).sum(1) * h
+    f[:, 12] = m / r0 * aw * (qs ** 3).sum(1) - 1.0
+    f[:, 13:16] = m / r0 * h * (gs[..., None] * ds).sum(1)
     return f
 
 

@@ -182,14 +182,15 @@ def pbf_double_dam_break(block=(64, 64, 128), h: float = H_DEFAULT, seed: int = 
                          eta: float = 1e-3) -> Scene:
     """Two water columns at opposite ends of a long box collapsing toward each
     other; with the default 64x64x128 blocks, 1,048,576 particles.  The box is
-    L x L/4 x L/2 with L = 4.1 block widths (blocks need by <= bx, bz <= 2 bx)."""
+    L x L/4 x L/2 with L = 4.1 block widths (blocks with by <= bx, bz <= 2 bx);
+    columns taller than wide (bx < by <= 2 bx) get a box L/2 high."""
     s = 0.5 * h
     bx, by, bz = block
-    if by > bx or bz > 2 * bx:
-        raise ValueError("block must satisfy by <= bx and bz <= 2 bx")
+    if by > 2 * bx or bz > 2 * bx:
+        raise ValueError("block must satisfy by <= 2 bx and bz <= 2 bx")
     L = 4.1 * bx * s
     box_min = [0.0, 0.0, 0.0]
-    box_max = [L, 0.25 * L, 0.5 * L]
+    box_max = [L, (0.25 if by <= bx else 0.5) * L, 0.5 * L]
     o = _block_origin(box_min, h)
     a = lattice_block(o, block, s, 0.01 * h, seed, 0)
     o2 = [box_max[0] - o[0] - (bx - 1) * s, o[1], o[2]]

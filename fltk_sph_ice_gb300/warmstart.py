@@ -224,6 +224,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--sizes", default="small", choices=["small", "large"],
+                    help="training scenes of 16k-131k particles (small) or 65k-262k with taller columns (large)")
     args = ap.parse_args()
     if args.calibrate:
         blob, meta = load_model(args.calibrate)
@@ -241,9 +243,15 @@ def main():
     X, T = [], []
     blocks = []
     for r in range(args.rollouts):
-        # 65k..262k particles: two blocks of bx x bx x 2bx with bx in 20..32
-        bx = int(rng.integers(20, 33))
-        by = int(rng.integers(max(8, bx // 2), bx + 1))
+        if args.sizes == "large":
+            # 65k..262k particles: two bx x by x 2bx blocks, bx in 21..32, columns
+            # from half as tall as wide up to twice as tall (64 layers)
+            bx = int(rng.integers(21, 33))
+            by = int(rng.integers(max(bx // 2, -(-65536 // (4 * bx * bx))), 2 * bx + 1))
+        else:
+            # 16k..131k particles: bx in 20..32, columns no taller than wide
+            bx = int(rng.integers(20, 33))
+            by = int(rng.integers(max(8, bx // 2), bx + 1))
         blocks.append((bx, by, 2 * bx))
         x, t, _ = collect_rollout((bx, by, 2 * bx), seed=1000 + r, steps=args.steps, per_step=args.per_step, rng=rng)
         X.append(x)
@@ -258,7 +266,7 @@ def main():
     meta = dict(samples=int(X.shape[0]), rollouts=args.rollouts, steps=args.steps, per_step=args.per_step,
                 epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
                 train_s=time.time() - t0 - t_collect, target_var=float((T / blob[O_SCALE]).var() * 3),
-                blocks=blocks[:8])
+                sizes=args.sizes, blocks=blocks[:8])
     alpha, table = calibrate_damping(blob)
     blob[O_SCALE] *= alpha
     meta["output_damping"] = alpha

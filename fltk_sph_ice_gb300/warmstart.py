@@ -221,7 +221,7 @@ def main():
     ap.add_argument("--rollouts", type=int, default=256)
     ap.add_argument("--steps", type=int, default=160)
     ap.add_argument("--per-step", type=int, default=256)
-    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--sizes", default="small", choices=["small", "large"],

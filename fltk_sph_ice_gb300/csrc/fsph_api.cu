@@ -295,8 +295,8 @@ int alloc_particles(fsph_ctx *c, int cap) {
     FSPH_TRY(dalloc(c, &c->tmp4, n)); FSPH_TRY(dalloc(c, &c->feat, n * kFeatures));
     FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, n * sizeof(float4), c->stream));
     FSPH_CUDA(c, cudaMemsetAsync(c->feat, 0, n * kFeatures * sizeof(float), c->stream));
-    FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n)));
-    FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n)));
+    FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n, kPassBlock)));
+    FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n, kPassBlock)));
     for (int k = 0; k < 2; ++k) {
         FSPH_CUDA(c, cudaMemsetAsync(c->set[k].pos, 0, n * sizeof(float4), c->stream));
         FSPH_CUDA(c, cudaMemsetAsync(c->set[k].vel, 0, n * sizeof(float4), c->stream));

@@ -321,14 +321,14 @@ __global__ void k_pbf_visc(DevParams p, const unsigned int *__restrict__ cell_st
  * fixed order, advances the iteration counter and decides whether the
  * device-side loop continues. */
 template <bool KAHAN>
-__global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
+__global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_lambda(DevParams p, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens,
                                                    DevCtl *ctl, ErrPartial *part,
                                                    cudaGraphConditionalHandle hwhile, int use_graph,
                                                    const ListEntry *__restrict__ list,
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb) {
-    __shared__ unsigned int s_rs[9 * kBlock];
+    __shared__ unsigned int s_rs[9 * kPassBlock];
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     float4 *pp = par ? ppos1 : ppos0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_lambda(DevParams p, 
  * x*_i <- walls(x*_i + dp_i) into the other ping-pong buffer; the largest
  * displacement since the last grid build decides whether the grid must be
  * rebuilt before the next pass. */
-__global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_correction(DevParams p, const unsigned int *__restrict__ cell_start,
+__global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_correction(DevParams p, const unsigned int *__restrict__ cell_start,
                                                        float4 *ppos0, float4 *ppos1,
                                                        const float4 *__restrict__ xb, DevCtl *ctl, float *part,
                                                        cudaGraphConditionalHandle hif,
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kBlock, FSPH_PASS_MINB) k_correction(DevParams
                                                        const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
                                                        const unsigned int *__restrict__ cellb) {
-    __shared__ unsigned int s_rs[9 * kBlock];
+    __shared__ unsigned int s_rs[9 * kPassBlock];
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     const float4 *__restrict__ src = par ? ppos1 : ppos0;
     float4 *__restrict__ dst = par ? ppos0 : ppos1;
@@ -777,7 +777,7 @@ void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *p
                    DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
                    const NbrLists &nl, cudaStream_t s) {
     auto k = p.compensated ? k_lambda<true> : k_lambda<false>;
-    k<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
+    k<<<blocks_for(p.n, kPassBlock), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
                                          (cudaGraphConditionalHandle)while_handle, use_graph,
                                          p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
@@ -790,7 +790,7 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
                        const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,
                        unsigned long long if_handle2, int use_graph, float4 *dp_out, const NbrLists &nl,
                        cudaStream_t s) {
-    k_correction<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb, ctl, part,
+    k_correction<<<blocks_for(p.n, kPassBlock), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb, ctl, part,
                                                     (cudaGraphConditionalHandle)if_handle,
                                                     (cudaGraphConditionalHandle)if_handle2, use_graph, dp_out,
                                                     p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);

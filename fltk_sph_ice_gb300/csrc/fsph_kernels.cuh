@@ -9,6 +9,11 @@
 namespace fsph {
 
 constexpr int kBlock = 256;
+/* threads per block of the two constraint passes (k_lambda, k_correction) */
+#ifndef FSPH_PASS_BLOCK
+#define FSPH_PASS_BLOCK 256
+#endif
+constexpr int kPassBlock = FSPH_PASS_BLOCK;
 constexpr int kBlockMax = 512;  /* largest block of the batched persistent kernels */
 constexpr int kScanTile = 4096; /* cells per block of the first scan phase */
 

@@ -30,10 +30,10 @@ namespace fsph {
 #define FSPH_KBATCH 4
 #endif
 
-/* resident 256-thread blocks per SM the constraint passes are compiled for:
- * 6 caps them at 42 registers, 48 warps per SM (measured best) */
+/* resident blocks per SM the constraint passes are compiled for: 1536
+ * threads cap them at 40 registers, 48 warps per SM (measured best) */
 #ifndef FSPH_PASS_MINB
-#define FSPH_PASS_MINB 6
+#define FSPH_PASS_MINB (1536 / FSPH_PASS_BLOCK)
 #endif
 constexpr int kBatch = FSPH_KBATCH;
 

@@ -10,7 +10,7 @@ change how many iterations a step takes, never the tolerance it reaches.
     python -m fltk_sph_ice_gb300.warmstart --out fltk_sph_ice_gb300/models/warmstart_mlp.npz
 
 collects rollouts of the plain solver on seeded double-dam-break scenes
-(65k-262k particles), trains on the GPU with fsph_mlp_train (Adam) and
+(16k-131k particles; --sizes large: 65k-262k), trains on the GPU with fsph_mlp_train (Adam) and
 writes the parameter blob plus its training record.
 """
 from __future__ import annotations

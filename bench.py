@@ -305,10 +305,11 @@ def ncu_traffic(kname: str):
 
 
 def roofline_of(L, abi, ps, n, mean_iters):
-    t_lam, t_cor, t_grid = ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0)
+    t_lam, t_cor, t_grid, t_list = (ctypes.c_float(0) for _ in range(4))
     L.fsph_time_pass(ps.handle, abi.PASS_LAMBDA, 20, ctypes.byref(t_lam))
     L.fsph_time_pass(ps.handle, abi.PASS_CORRECTION, 20, ctypes.byref(t_cor))
     L.fsph_time_pass(ps.handle, abi.PASS_GRID, 10, ctypes.byref(t_grid))
+    L.fsph_time_pass(ps.handle, abi.PASS_LIST, 10, ctypes.byref(t_list))
     if t_cor.value >= t_lam.value:
         kname, kms, kbytes = "k_correction", t_cor.value, BYTES_CORRECTION * n
     else:
@@ -319,6 +320,7 @@ def roofline_of(L, abi, ps, n, mean_iters):
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
             "lambda_ms": t_lam.value, "correction_ms": t_cor.value, "grid_build_ms": t_grid.value,
+            "list_build_ms": t_list.value,
             "passes_ms_per_step": mean_iters * (t_lam.value + t_cor.value)}
 
 

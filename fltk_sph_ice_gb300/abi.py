@@ -156,7 +156,7 @@ EXPORTS = [
 ]
 
 # fsph_pass
-PASS_LAMBDA, PASS_CORRECTION, PASS_GRID = 0, 1, 2
+PASS_LAMBDA, PASS_CORRECTION, PASS_GRID, PASS_LIST = 0, 1, 2, 3
 
 _LIB = None
 

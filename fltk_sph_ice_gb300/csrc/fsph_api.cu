@@ -1192,6 +1192,8 @@ int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
             g.src4[2] = c->set[1].pos; g.dst4[2] = c->acc;
             g.src1[0] = c->set[1].id; g.dst1[0] = c->set[1].attr;
             launch_gather(p.n, c->perm, g, nullptr, s);
+        } else if (pass == FSPH_PASS_LIST) {
+            launch_build_list(p, c->cell_start, c->xb, c->nl, s);
         } else {
             cudaEventDestroy(e0); cudaEventDestroy(e1);
             return fail(c, FSPH_INVALID_ARG, "unknown pass");

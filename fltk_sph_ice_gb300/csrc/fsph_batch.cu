@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(BLOCK) kb_build_list(BatchArgs b, const unsign
 /* lambda pass over all scenes; lp holds the loop constants (n = all
  * particles, min_iter = max_iter = the fixed iteration count). */
 template <int BLOCK, int LPP>
-__global__ void __launch_bounds__(BLOCK, FSPH_PASS_MINB * 256 / BLOCK)
+__global__ void __launch_bounds__(BLOCK, FSPH_PASS_THREADS / BLOCK)
     kb_lambda(BatchArgs b, DevParams lp, const unsigned int *__restrict__ cell_start,
                                                    float4 *ppos0, float4 *ppos1, float *__restrict__ dens, DevCtl *ctl,
                                                    ErrPartial *part, cudaGraphConditionalHandle hwhile, int use_graph,
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(BLOCK, FSPH_PASS_MINB * 256 / BLOCK)
 /* correction pass over all scenes; the rebuild measure is the largest
  * |x* - xb|^2 / skin2 of the particle's own scene (lp.skin2 = 1). */
 template <int BLOCK, int LPP>
-__global__ void __launch_bounds__(BLOCK, FSPH_PASS_MINB * 256 / BLOCK) kb_correction(BatchArgs b, DevParams lp,
+__global__ void __launch_bounds__(BLOCK, FSPH_PASS_THREADS / BLOCK) kb_correction(BatchArgs b, DevParams lp,
                                                        const unsigned int *__restrict__ cell_start, float4 *ppos0,
                                                        float4 *ppos1, const float4 *__restrict__ xb, DevCtl *ctl,
                                                        float *part, cudaGraphConditionalHandle hif,

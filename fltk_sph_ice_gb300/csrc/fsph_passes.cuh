@@ -30,11 +30,13 @@ namespace fsph {
 #define FSPH_KBATCH 4
 #endif
 
-/* resident blocks per SM the constraint passes are compiled for: 1536
- * threads cap them at 40 registers, 48 warps per SM (measured best) */
-#ifndef FSPH_PASS_MINB
-#define FSPH_PASS_MINB (1536 / FSPH_PASS_BLOCK)
+/* resident threads per SM the constraint passes are compiled for (single
+ * scene and batched): 1536 cap them at 40 registers, 48 warps per SM
+ * (measured best) */
+#ifndef FSPH_PASS_THREADS
+#define FSPH_PASS_THREADS 1536
 #endif
+#define FSPH_PASS_MINB (FSPH_PASS_THREADS / FSPH_PASS_BLOCK)
 constexpr int kBatch = FSPH_KBATCH;
 
 /* Neighbour-list loads do not allocate in L1 (ld.global.nc.L1::no_allocate):

@@ -317,7 +317,8 @@ int fsph_set_warm_start_model(fsph_ctx *ctx, const float *blob);
 typedef enum fsph_pass {
     FSPH_PASS_LAMBDA = 0,      /* one lambda pass (density + constraint + error reduction) */
     FSPH_PASS_CORRECTION = 1,  /* one position-correction pass */
-    FSPH_PASS_GRID = 2         /* one grid build (hash, scan, scatter, cell sort, reorder) */
+    FSPH_PASS_GRID = 2,        /* one grid build (hash, scan, scatter, cell sort, reorder) */
+    FSPH_PASS_LIST = 3         /* one neighbour-list build on the current grid */
 } fsph_pass;
 /* Time `reps` back-to-back launches of one pass of the current PBF state
  * with CUDA events on the context's stream; *avg_ms receives the mean time

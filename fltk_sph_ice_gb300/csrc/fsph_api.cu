@@ -77,6 +77,9 @@ struct fsph_ctx {
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
     bool graph_valid = false;
+    bool home_identity = true;  /* set[0] holds the particles in particle order (id = slot) */
+    unsigned int *res_id = nullptr; /* slot order of the last step's results after a SetArrayVBO */
+    bool res_in_res_id = false;     /* results are ordered by res_id rather than set[0].id */
     float graph_dt = 0.0f;
     int graph_n = -1;
     /* kernel nodes of the step graph: outside the loop, per iteration, per grid rebuild */
@@ -224,6 +227,7 @@ void free_particles(fsph_ctx *c) {
     }
     cudaFree(c->xb); cudaFree(c->acc); cudaFree(c->vort); cudaFree(c->dens); cudaFree(c->pres);
     cudaFree(c->key); cudaFree(c->rank); cudaFree(c->perm); cudaFree(c->epart); cudaFree(c->dpart);
+    cudaFree(c->res_id); c->res_id = nullptr;
     cudaFree(c->nl.list); cudaFree(c->nl.cnt); cudaFree(c->nl.cellb);
     c->nl = NbrLists{};
     cudaFree(c->xpred); cudaFree(c->dstep); cudaFree(c->dwarm); cudaFree(c->tmp4); cudaFree(c->feat);
@@ -289,6 +293,7 @@ int alloc_particles(fsph_ctx *c, int cap) {
     FSPH_TRY(dalloc(c, &c->xb, n)); FSPH_TRY(dalloc(c, &c->acc, n)); FSPH_TRY(dalloc(c, &c->vort, n));
     FSPH_TRY(dalloc(c, &c->dens, n)); FSPH_TRY(dalloc(c, &c->pres, n));
     FSPH_TRY(dalloc(c, &c->key, n)); FSPH_TRY(dalloc(c, &c->rank, n)); FSPH_TRY(dalloc(c, &c->perm, n));
+    FSPH_TRY(dalloc(c, &c->res_id, n));
     FSPH_TRY(dalloc(c, &c->nl.list, n * kListMax)); FSPH_TRY(dalloc(c, &c->nl.cnt, n));
     FSPH_TRY(dalloc(c, &c->nl.cellb, n));
     FSPH_TRY(dalloc(c, &c->xpred, n)); FSPH_TRY(dalloc(c, &c->dstep, n)); FSPH_TRY(dalloc(c, &c->dwarm, n));
@@ -628,6 +633,7 @@ int load_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int
         else FSPH_CUDA(c, cudaMemsetAsync(c->set[0].vel, 0, b, c->stream));
         FSPH_CUDA(c, cudaMemsetAsync(c->set[0].attr, 0, (size_t)n * 4, c->stream));
         launch_iota(n, c->set[0].id, c->stream);
+        c->home_identity = true;
         /* a new state has no step history for the warm start */
         FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, b, c->stream));
     }
@@ -879,22 +885,30 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
         return fail(c, FSPH_INVALID_ARG, "settable arrays: POSITION, VELOCITY, ATTRIBUTE");
     cudaStream_t s = c->stream;
     int n = c->n;
-    /* bring the home arrays to particle order, then overwrite the range */
-    launch_unsort4(n, c->set[0].id, c->set[0].pos, c->set[1].pos, 0, s);
-    launch_unsort4(n, c->set[0].id, c->set[0].vel, c->set[1].vel, 0, s);
-    launch_unsort1(n, c->set[0].id, c->set[0].attr, c->set[1].attr, s);
-    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
-    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
-    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-    /* the warm-start history (step corrections, features) follows the particles */
-    launch_unsort4(n, c->set[0].id, c->dstep, c->tmp4, 0, s);
-    FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, c->tmp4, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
-    {
-        float4 *tf = reinterpret_cast<float4 *>(c->nl.list); /* lists are rebuilt by every step */
-        launch_unsort_rows(n, c->set[0].id, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
-        FSPH_CUDA(c, cudaMemcpyAsync(c->feat, tf, (size_t)n * kFeatures * 4, cudaMemcpyDeviceToDevice, s));
+    /* bring the home arrays to particle order (once after a step), then
+     * overwrite the range */
+    if (!c->home_identity) {
+        launch_unsort4(n, c->set[0].id, c->set[0].pos, c->set[1].pos, 0, s);
+        launch_unsort4(n, c->set[0].id, c->set[0].vel, c->set[1].vel, 0, s);
+        launch_unsort1(n, c->set[0].id, c->set[0].attr, c->set[1].attr, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        /* the warm-start history (step corrections, features) follows the particles */
+        launch_unsort4(n, c->set[0].id, c->dstep, c->tmp4, 0, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, c->tmp4, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        /* the last step's other results (density, lambda, forces, ...) stay
+         * in its slot order, which res_id keeps for the getters */
+        FSPH_CUDA(c, cudaMemcpyAsync(c->res_id, c->set[0].id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        c->res_in_res_id = true;
+        {
+            float4 *tf = reinterpret_cast<float4 *>(c->nl.list); /* lists are rebuilt by every step */
+            launch_unsort_rows(n, c->set[0].id, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
+            FSPH_CUDA(c, cudaMemcpyAsync(c->feat, tf, (size_t)n * kFeatures * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        launch_iota(n, c->set[0].id, s);
+        c->home_identity = true;
     }
-    launch_iota(n, c->set[0].id, s);
     cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (type == FSPH_POSITION)
         FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos + start, data, (size_t)count * 16, k, s));
@@ -923,6 +937,8 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
         return fail(c, FSPH_UNSUPPORTED, "warm_start = 1 needs a network (fsph_set_warm_start_model)");
     DevParams p = dev_for(c, c->n, dt);
     c->dp = p;
+    c->home_identity = false; /* the step leaves the home set in cell order */
+    c->res_in_res_id = false;
     c->last_step_graph = c->P.solver == FSPH_SOLVER_PBF && c->P.use_graph;
     if (c->P.solver == FSPH_SOLVER_WCSPH) {
         FSPH_TRY(sph_step(c, p));
@@ -969,6 +985,11 @@ int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
     (void)stream;
     FSPH_CUDA(c, cudaStreamSynchronize(s));
     const unsigned int *id = c->set[0].id;
+    /* the last step's results after a SetArrayVBO keep that step's order */
+    const bool result = type == FSPH_FORCE || type == FSPH_VORTICITY || type == FSPH_PREDICT_POS ||
+                        type == FSPH_CORRECTION || type == FSPH_DENSITY || type == FSPH_PRESSURE ||
+                        type == FSPH_SCALING_FACTOR;
+    if (result && c->res_in_res_id) id = c->res_id;
     /* staging in device memory: the rank / key arrays are free between steps */
     float4 *t4 = c->set[1].pos;
     bool vec = true;
@@ -1010,7 +1031,7 @@ int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
         const unsigned int *src = type == FSPH_DENSITY ? reinterpret_cast<const unsigned int *>(c->dens)
                                   : type == FSPH_PRESSURE ? reinterpret_cast<const unsigned int *>(c->pres)
                                                           : c->set[0].attr;
-        launch_unsort1(n, id, src, c->set[1].id, s);
+        launch_unsort1(n, id, src, c->set[1].id, s); /* id = set[0].id for the attribute */
         break;
     }
     case FSPH_SCALING_FACTOR:

@@ -409,7 +409,7 @@ def gpu_arm(args):
     gpu_launches = warm["kernels"] or int(args.steps * (12 + 2 * warm["mean_iterations"]))
     if rank == 0:
         cfg = {"workload": WORKLOAD, "particles": n, "block": list(BLOCK), "dt": sc.dt, "eta_one_sided": 1e-3,
-               "constraint": "unilateral (clamped C >= 0)", "method": "learned warm start (BF16 MLP 16-64-64-3)",
+               "constraint": "unilateral (clamped C >= 0)", "method": "learned warm start (BF16 MLP 32-64-64-3)",
                "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
                "grid_builds_per_step": warm["grid_builds"],
                "model": {"samples": meta.get("samples"), "rollouts": meta.get("rollouts"),
@@ -644,7 +644,7 @@ def large_arm(args):
     if rank == 0:
         cfg = {"workload": "pbf_obstacle_drop_16M", "particles": sc.n, "boundary_particles": int(sc.boundary.shape[0]),
                "block": [256, 256, 256], "dt": sc.dt, "eta_one_sided": 1e-3, "compensated_density": True,
-               "constraint": "unilateral (clamped C >= 0)", "method": "learned warm start (BF16 MLP 16-64-64-3)",
+               "constraint": "unilateral (clamped C >= 0)", "method": "learned warm start (BF16 MLP 32-64-64-3)",
                "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
                "preroll_steps": LARGE_PREROLL, "l2": "256 MiB flush between timed steps",
                "parallelism": f"replicas x{world}", "fp64_error_per_step": fp64}

@@ -42,7 +42,7 @@ VECTOR_ARRAYS = {RX_POSITION, RX_VELOCITY, RX_FORCE, RX_PREDICT_POS, RX_PREDICT_
                  RX_STEP_CORRECTION}
 
 # learned warm start (fsph.h)
-MLP_FEATURES, MLP_HIDDEN, MLP_OUTPUTS, MLP_BLOB_SIZE = 16, 64, 3, 5476
+MLP_FEATURES, MLP_HIDDEN, MLP_OUTPUTS, MLP_BLOB_SIZE = 32, 64, 3, 6532
 WARM_NONE, WARM_LEARNED = 0, 1
 
 STATUS_NAMES = {

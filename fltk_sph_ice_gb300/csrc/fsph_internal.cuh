@@ -95,8 +95,11 @@ __host__ __device__ inline size_t list_at(int t, int i, int n) {
  *   12 C' = rho'/rho0 - 1 and 13-15 h grad_i C' at the next step's predicted
  *      relative positions x_ij + dt (v_i - v_j) (the constraint the coming
  *      iterations will have to remove, from the same neighbour loop)
+ *   16-22 the poly6-weighted means over the neighbours (self excluded) of
+ *      features 0, 6-8 and 9-11: what the particle's surroundings do
+ *   23-31 zero (the network's input is padded to two 16-wide MMA k-steps)
  * Row-major, kFeatures floats per particle. */
-constexpr int kFeatures = 16;
+constexpr int kFeatures = 32;
 struct DevCtl;
 struct FeatureOut {
     float *feat = nullptr;             /* [n][kFeatures]; nullptr: no features */

@@ -86,32 +86,41 @@ __device__ __forceinline__ void copy_model(MlpDev &sm, const MlpDev *__restrict_
  * 2c, 2c+1; columns >= 3 are padding).  Rows >= n read zero features. */
 struct Fwd {
     float h1[8][4], h2[8][4], o[4];
-    unsigned ax[4];
-    float xn[8]; /* normalised inputs of this thread: (g, 2c..2c+1), (g+8, ..), (g, 2c+8..), (g+8, 2c+8..) */
+    unsigned ax[kIn / 16][4];
+    /* normalised inputs of this thread, per 16-column k tile kt:
+     * (g, 16kt+2c..+1), (g+8, ..), (g, 16kt+2c+8..+9), (g+8, ..) */
+    float xn[kIn / 2];
 };
 
 __device__ __forceinline__ void mlp_forward(const MlpDev &sm, const float *__restrict__ x, int n, int base, int g,
                                             int c, Fwd &F) {
     const int r0 = base + g, r1 = base + g + 8;
-    const int cols[4] = {2 * c, 2 * c + 1, 2 * c + 8, 2 * c + 9};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const int col = cols[q];
-        const float v0 = r0 < n ? __ldg(x + (size_t)r0 * kIn + col) : 0.0f;
-        const float v1 = r1 < n ? __ldg(x + (size_t)r1 * kIn + col) : 0.0f;
-        F.xn[q] = r0 < n ? (v0 - sm.mu[col]) * sm.isig[col] : 0.0f;       /* row g   */
-        F.xn[4 + q] = r1 < n ? (v1 - sm.mu[col]) * sm.isig[col] : 0.0f;   /* row g+8 */
+    for (int kt = 0; kt < kIn / 16; ++kt) {
+        const int cols[4] = {16 * kt + 2 * c, 16 * kt + 2 * c + 1, 16 * kt + 2 * c + 8, 16 * kt + 2 * c + 9};
+        float *xn = F.xn + 8 * kt;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int col = cols[q];
+            const float v0 = r0 < n ? __ldg(x + (size_t)r0 * kIn + col) : 0.0f;
+            const float v1 = r1 < n ? __ldg(x + (size_t)r1 * kIn + col) : 0.0f;
+            xn[q] = r0 < n ? (v0 - sm.mu[col]) * sm.isig[col] : 0.0f;       /* row g   */
+            xn[4 + q] = r1 < n ? (v1 - sm.mu[col]) * sm.isig[col] : 0.0f;   /* row g+8 */
+        }
+        F.ax[kt][0] = pack2(xn[0], xn[1]);
+        F.ax[kt][1] = pack2(xn[4], xn[5]);
+        F.ax[kt][2] = pack2(xn[2], xn[3]);
+        F.ax[kt][3] = pack2(xn[6], xn[7]);
     }
-    F.ax[0] = pack2(F.xn[0], F.xn[1]);
-    F.ax[1] = pack2(F.xn[4], F.xn[5]);
-    F.ax[2] = pack2(F.xn[2], F.xn[3]);
-    F.ax[3] = pack2(F.xn[6], F.xn[7]);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         const float b0v = sm.b1[8 * j + 2 * c], b1v = sm.b1[8 * j + 2 * c + 1];
         F.h1[j][0] = b0v; F.h1[j][1] = b1v; F.h1[j][2] = b0v; F.h1[j][3] = b1v;
-        const __nv_bfloat16 *w = sm.w1t + (8 * j + g) * kS1 + 2 * c;
-        mma16816(F.h1[j], F.ax, ld32(w), ld32(w + 8));
+#pragma unroll
+        for (int kt = 0; kt < kIn / 16; ++kt) {
+            const __nv_bfloat16 *w = sm.w1t + (8 * j + g) * kS1 + 16 * kt + 2 * c;
+            mma16816(F.h1[j], F.ax[kt], ld32(w), ld32(w + 8));
+        }
 #pragma unroll
         for (int e = 0; e < 4; ++e) F.h1[j][e] = fmaxf(F.h1[j][e], 0.0f);
     }
@@ -216,12 +225,14 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const MlpDev *__restrict__ gm,
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, g = lane >> 2, c = lane & 3;
     const float inv_scale = sm.out_scale != 0.0f ? 1.0f / sm.out_scale : 0.0f;
     const float gscale = 2.0f / (float)n;
-    float acc2[8][4], acc3[4], acc1[2][4];
+    float acc2[8][4], acc3[4], acc1[kIn / 16][2][4];
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc2[j][0] = acc2[j][1] = acc2[j][2] = acc2[j][3] = 0.f;
     acc3[0] = acc3[1] = acc3[2] = acc3[3] = 0.f;
-    acc1[0][0] = acc1[0][1] = acc1[0][2] = acc1[0][3] = 0.f;
-    acc1[1][0] = acc1[1][1] = acc1[1][2] = acc1[1][3] = 0.f;
+#pragma unroll
+    for (int mt = 0; mt < kIn / 16; ++mt)
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj) acc1[mt][jj][0] = acc1[mt][jj][1] = acc1[mt][jj][2] = acc1[mt][jj][3] = 0.f;
     float db1 = 0.f, db2 = 0.f, db3 = 0.f, loss = 0.f;
     const int nchunks = (n + kChunk - 1) / kChunk;
     for (int ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
@@ -231,12 +242,13 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const MlpDev *__restrict__ gm,
         Fwd F;
         mlp_forward(sm, x, n, base, g, c, F);
         /* stage x~, h1, h2 transposed */
-        {
-            const int cols[4] = {2 * c, 2 * c + 1, 2 * c + 8, 2 * c + 9};
+#pragma unroll
+        for (int kt = 0; kt < kIn / 16; ++kt) {
+            const int cols[4] = {16 * kt + 2 * c, 16 * kt + 2 * c + 1, 16 * kt + 2 * c + 8, 16 * kt + 2 * c + 9};
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                sx[cols[q] * kSS + sl0] = __float2bfloat16(F.xn[q]);
-                sx[cols[q] * kSS + sl1] = __float2bfloat16(F.xn[4 + q]);
+                sx[cols[q] * kSS + sl0] = __float2bfloat16(F.xn[8 * kt + q]);
+                sx[cols[q] * kSS + sl1] = __float2bfloat16(F.xn[8 * kt + 4 + q]);
             }
         }
 #pragma unroll
@@ -332,12 +344,16 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const MlpDev *__restrict__ gm,
                 const __nv_bfloat16 *bp = sdy + g * kSS + k0;
                 mma16816(acc3, ah2, ld32(bp), ld32(bp + 8));
             }
-            unsigned axx[4] = {ld32(sx + g * kSS + k0), ld32(sx + (g + 8) * kSS + k0), ld32(sx + g * kSS + k0 + 8),
-                               ld32(sx + (g + 8) * kSS + k0 + 8)};
 #pragma unroll
-            for (int jj = 0; jj < 2; ++jj) {
-                const __nv_bfloat16 *bp = sd1 + (8 * (2 * w + jj) + g) * kSS + k0;
-                mma16816(acc1[jj], axx, ld32(bp), ld32(bp + 8));
+            for (int mt = 0; mt < kIn / 16; ++mt) {
+                const __nv_bfloat16 *xr = sx + 16 * mt * kSS;
+                unsigned axx[4] = {ld32(xr + g * kSS + k0), ld32(xr + (g + 8) * kSS + k0),
+                                   ld32(xr + g * kSS + k0 + 8), ld32(xr + (g + 8) * kSS + k0 + 8)};
+#pragma unroll
+                for (int jj = 0; jj < 2; ++jj) {
+                    const __nv_bfloat16 *bp = sd1 + (8 * (2 * w + jj) + g) * kSS + k0;
+                    mma16816(acc1[mt][jj], axx, ld32(bp), ld32(bp + 8));
+                }
             }
         }
         if (tid < kHid) {
@@ -366,13 +382,15 @@ __global__ void __launch_bounds__(128) k_mlp_grad(const MlpDev *__restrict__ gm,
         if (n0 + 1 < kOut) { P[kBW3 + m0 * kOut + n0 + 1] = acc3[1]; P[kBW3 + (m0 + 8) * kOut + n0 + 1] = acc3[3]; }
     }
 #pragma unroll
-    for (int jj = 0; jj < 2; ++jj) {
-        const int n0 = 8 * (2 * w + jj) + 2 * c;
-        P[kBW1 + g * kHid + n0] = acc1[jj][0];
-        P[kBW1 + g * kHid + n0 + 1] = acc1[jj][1];
-        P[kBW1 + (g + 8) * kHid + n0] = acc1[jj][2];
-        P[kBW1 + (g + 8) * kHid + n0 + 1] = acc1[jj][3];
-    }
+    for (int mt = 0; mt < kIn / 16; ++mt)
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj) {
+            const int n0 = 8 * (2 * w + jj) + 2 * c, m0 = 16 * mt + g;
+            P[kBW1 + m0 * kHid + n0] = acc1[mt][jj][0];
+            P[kBW1 + m0 * kHid + n0 + 1] = acc1[mt][jj][1];
+            P[kBW1 + (m0 + 8) * kHid + n0] = acc1[mt][jj][2];
+            P[kBW1 + (m0 + 8) * kHid + n0 + 1] = acc1[mt][jj][3];
+        }
     if (tid < kHid) { P[kBB1 + tid] = db1; P[kBB2 + tid] = db2; }
     if (tid < kOut) P[kBB3 + tid] = db3;
     if (tid < kBW1) P[tid] = 0.0f;

@@ -4,7 +4,7 @@
  * tensor cores, FP32 accumulation, FP32 master weights for training.
  *
  * Parameters travel as one FP32 "blob" (FSPH_MLP_BLOB_SIZE floats, layout in
- * include/fsph.h): input normalisation, W1 [16][64], b1, W2 [64][64], b2,
+ * include/fsph.h): input normalisation, W1 [kFeatures][64], b1, W2 [64][64], b2,
  * W3 [64][3], b3, output scale.  The device copy used by the kernels
  * (MlpDev) holds every weight matrix in the layouts the mma fragments load
  * from, with padded row strides so the 8 fragment rows of a warp fall in
@@ -19,6 +19,7 @@
 namespace fsph {
 
 constexpr int kIn = kFeatures, kHid = 64, kOut = 3;
+static_assert(kIn % 16 == 0, "the input is a whole number of 16-wide MMA k-steps");
 /* blob offsets (floats) */
 constexpr int kBMu = 0;
 constexpr int kBSig = kBMu + kIn;

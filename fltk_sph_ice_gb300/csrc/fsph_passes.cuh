@@ -515,6 +515,10 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
     float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
     float cntf = 0.f;
     float wpred = 0.f; /* sum q^3 at the next step's predicted relative positions */
+    /* poly6-weighted neighbour sums (self excluded) for the features:
+     * weights, density, relative velocity, step correction */
+    float nw = 0.f, nrho = 0.f;
+    float3 nv = make_float3(0.f, 0.f, 0.f), nd = make_float3(0.f, 0.f, 0.f);
     /* branch-free pair terms: q and t clamp to zero outside h, and the self
      * pair (d = 0, v_ij = 0) adds only to the neighbour count */
     for_each_candidate<1>(
@@ -528,7 +532,8 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = p.ag * t * t * inv_r;
             const float3 vij = f3(__ldg(vel + j)) - vi;
-            const float mrho = p.mass / __ldg(dens + j);
+            const float rhoj = __ldg(dens + j);
+            const float mrho = p.mass / rhoj;
             om = om + cross3(vij, (-g) * d);
             xs = xs + (p.aw * q * q * q * mrho) * vij;
             cntf += inside;
@@ -543,6 +548,11 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
                 const float ts = fmaxf(p.h - r2s * inv_rs, 0.0f);
                 wpred += qs * qs * qs;
                 cg = cg + (p.ag * ts * ts * inv_rs) * ds;
+                const float w = r2 > 0.0f ? q * q * q : 0.0f;
+                nw += w;
+                nrho += w * rhoj;
+                nv = nv + w * vij;
+                nd = nd + w * f3(__ldg(fo.dstep + j));
             }
         });
     cntf = fmaxf(cntf, 1.0f);
@@ -565,6 +575,16 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
         const float mr0 = p.mass * p.inv_rest_dens;
         f[12] = mr0 * p.aw * wpred - 1.0f;
         f[13] = mr0 * cg.x * p.h; f[14] = mr0 * cg.y * p.h; f[15] = mr0 * cg.z * p.h;
+        /* weighted neighbour means of features 0, 6-8 and 9-11 (zero without neighbours) */
+        const float inw = nw > 0.0f ? 1.0f / nw : 0.0f;
+        const float vs = p.dt * inv_h;
+        f[16] = nw > 0.0f ? nrho * inw * p.inv_rest_dens - 1.0f : 0.0f;
+        f[17] = nw > 0.0f ? (vi.x + nv.x * inw) * vs : 0.0f;
+        f[18] = nw > 0.0f ? (vi.y + nv.y * inw) * vs : 0.0f;
+        f[19] = nw > 0.0f ? (vi.z + nv.z * inw) * vs : 0.0f;
+        f[20] = nd.x * inw * inv_h; f[21] = nd.y * inw * inv_h; f[22] = nd.z * inw * inv_h;
+#pragma unroll
+        for (int k = 23; k < kFeatures; ++k) f[k] = 0.0f;
         float4 *out = reinterpret_cast<float4 *>(fo.feat + (size_t)i * kFeatures);
 #pragma unroll
         for (int k = 0; k < kFeatures / 4; ++k) out[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);

@@ -31,6 +31,7 @@ MODEL_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "models")
 DEFAULT_MODEL = os.path.join(MODEL_DIR, "warmstart_mlp.npz")
 
 NI, NH, NO = abi.MLP_FEATURES, abi.MLP_HIDDEN, abi.MLP_OUTPUTS
+BASE_FEATURES = 16  # particle-local features; 16-22 are neighbour means, the rest padding
 O_MU, O_SIG = 0, NI
 O_W1 = 2 * NI
 O_B1 = O_W1 + NI * NH
@@ -224,8 +225,14 @@ def main():
     ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--sizes", default="small", choices=["small", "large"],
-                    help="training scenes of 16k-131k particles (small) or 65k-262k with taller columns (large)")
+    ap.add_argument("--sizes", default="small", choices=["small", "large", "config"],
+                    help="training scenes of 16k-131k particles (small), 65k-262k with columns up to twice as "
+                         "tall as wide (large), or 65k-262k with columns no taller than wide (config)")
+    ap.add_argument("--features", default="all", choices=["all", "base"],
+                    help="all features, or only the first 16 (the neighbour means are given no weight)")
+    ap.add_argument("--seed", type=int, default=0, help="initialisation and shuffling seed of the training")
+    ap.add_argument("--data", default=None, metavar="NPZ",
+                    help="reuse the rollout samples stored in NPZ (written there when it does not exist)")
     args = ap.parse_args()
     if args.calibrate:
         blob, meta = load_model(args.calibrate)
@@ -242,8 +249,16 @@ def main():
     rng = np.random.default_rng(12345)
     X, T = [], []
     blocks = []
-    for r in range(args.rollouts):
-        if args.sizes == "large":
+    loaded = args.data is not None and os.path.isfile(args.data)
+    if loaded:
+        d = np.load(args.data)
+        X, T, blocks = [d["X"]], [d["T"]], [tuple(int(v) for v in b) for b in d["blocks"]]
+    for r in range(0 if loaded else args.rollouts):
+        if args.sizes == "config":
+            # 65k..262k particles: bx in 26..40, columns from half as tall as wide up to square
+            bx = int(rng.integers(26, 41))
+            by = int(rng.integers(max(bx // 2, -(-65536 // (4 * bx * bx))), bx + 1))
+        elif args.sizes == "large":
             # 65k..262k particles: two bx x by x 2bx blocks, bx in 21..32, columns
             # from half as tall as wide up to twice as tall (64 layers)
             bx = int(rng.integers(21, 33))
@@ -258,15 +273,20 @@ def main():
         T.append(t)
     X = np.concatenate(X).astype(np.float32)
     T = np.concatenate(T).astype(np.float32)
+    if args.data is not None and not loaded:
+        np.savez(args.data, X=X, T=T, blocks=np.asarray(blocks))
     t_collect = time.time() - t0
-    blob = init_blob(X, T)
+    blob = init_blob(X, T, seed=args.seed)
+    if args.features == "base":
+        # the neighbour means get an infinite spread: their normalised inputs are zero
+        blob[O_SIG + BASE_FEATURES:O_W1] = np.float32(1e30)
     net = WarmStartNet(blob)
-    hist = net.train(X, T, epochs=args.epochs, batch=args.batch, lr=args.lr)
+    hist = net.train(X, T, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed)
     blob = net.get_blob()
     meta = dict(samples=int(X.shape[0]), rollouts=args.rollouts, steps=args.steps, per_step=args.per_step,
                 epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
                 train_s=time.time() - t0 - t_collect, target_var=float((T / blob[O_SCALE]).var() * 3),
-                sizes=args.sizes, blocks=blocks[:8])
+                sizes=args.sizes, features=args.features, seed=args.seed, blocks=blocks[:8])
     alpha, table = calibrate_damping(blob)
     blob[O_SCALE] *= alpha
     meta["output_damping"] = alpha

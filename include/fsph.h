@@ -282,15 +282,15 @@ int fsph_get_boundary(fsph_ctx *ctx, int which, float *dst);
 /* ---- learned warm start ---- */
 /* The network: FSPH_MLP_FEATURES -> 64 -> 64 -> 3, ReLU, BF16 tensor-core
  * arithmetic with FP32 accumulation.  Its parameters are one FP32 blob of
- * FSPH_MLP_BLOB_SIZE floats: mu[16], sigma[16] (input standardisation),
- * W1[16][64], b1[64], W2[64][64], b2[64], W3[64][3], b3[3], out_scale[1].
+ * FSPH_MLP_BLOB_SIZE floats: mu[32], sigma[32] (input standardisation),
+ * W1[32][64], b1[64], W2[64][64], b2[64], W3[64][3], b3[3], out_scale[1].
  * Output = (network of (x - mu) / sigma) * out_scale = predicted step
  * correction / h.  No counterpart in the reference (its PBF loop always
  * starts from the prediction, rx_sph_pbd.cpp:418-425). */
-#define FSPH_MLP_FEATURES 16
+#define FSPH_MLP_FEATURES 32
 #define FSPH_MLP_HIDDEN 64
 #define FSPH_MLP_OUTPUTS 3
-#define FSPH_MLP_BLOB_SIZE 5476
+#define FSPH_MLP_BLOB_SIZE 6532
 typedef struct fsph_mlp fsph_mlp;
 int fsph_mlp_create(fsph_mlp **out);
 int fsph_mlp_destroy(fsph_mlp *m);

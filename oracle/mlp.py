@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import numpy as np
 
-NI, NH, NO = 16, 64, 3
+NI, NH, NO = 32, 64, 3
 O_MU = 0
 O_SIG = O_MU + NI
 O_W1 = O_SIG + NI

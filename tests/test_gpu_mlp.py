@@ -19,7 +19,8 @@ BLOCKS = {"W1": (omlp.O_W1, omlp.O_B1), "b1": (omlp.O_B1, omlp.O_W2), "W2": (oml
 def random_problem(n, seed=0):
     from fltk_sph_ice_gb300 import warmstart
     rng = np.random.default_rng(seed)
-    x = (rng.standard_normal((n, 16)) * rng.uniform(0.1, 3.0, 16) + rng.uniform(-1, 1, 16)).astype(np.float32)
+    ni = omlp.NI
+    x = (rng.standard_normal((n, ni)) * rng.uniform(0.1, 3.0, ni) + rng.uniform(-1, 1, ni)).astype(np.float32)
     t = (rng.standard_normal((n, 3)) * 0.02).astype(np.float32)
     blob = warmstart.init_blob(x, t, seed=seed)
     blob[omlp.O_B1:omlp.O_W2] = rng.standard_normal(64) * 0.1
@@ -65,7 +66,7 @@ def test_training_reduces_loss(gpu):
     """Regression onto a fixed teacher network: Adam on the GPU kernels."""
     from fltk_sph_ice_gb300 import warmstart
     rng = np.random.default_rng(3)
-    x = rng.standard_normal((65536, 16)).astype(np.float32)
+    x = rng.standard_normal((65536, omlp.NI)).astype(np.float32)
     _, _, teacher = random_problem(16, seed=7)
     teacher[omlp.O_MU:omlp.O_SIG] = 0.0
     teacher[omlp.O_SIG:omlp.O_W1] = 1.0
@@ -74,7 +75,7 @@ def test_training_reduces_loss(gpu):
     blob = warmstart.init_blob(x, t, seed=11)
     net = warmstart.WarmStartNet(blob)
     _, loss0 = net.gradient(x[:8192], t[:8192])
-    hist = net.train(x, t, epochs=8, batch=4096, lr=3e-3)
+    hist = net.train(x, t, epochs=16, batch=4096, lr=3e-3)
     _, loss1 = net.gradient(x[:8192], t[:8192])
     print("loss", loss0, "->", loss1, hist)
     assert loss1 < 0.1 * loss0

@@ -44,7 +44,7 @@ def test_step_correction_and_features(gpu):
     x_before = ps.GetArrayVBO(abi.RX_POSITION)
     v_before = ps.GetArrayVBO(abi.RX_VELOCITY)
     feats = ps.GetArrayVBO(abi.FSPH_FEATURES)
-    assert feats.shape == (sc.n, 16) and np.isfinite(feats).all()
+    assert feats.shape == (sc.n, abi.MLP_FEATURES) and np.isfinite(feats).all()
     # features 9-11 are the last step's correction over h
     d_last = ps.GetArrayVBO(abi.RX_STEP_CORRECTION)[:, :3]
     assert_rel(feats[:, 9:12], d_last / p.h, 1e-6, "correction feature")
@@ -62,7 +62,7 @@ def test_step_correction_and_features(gpu):
 
 
 def features_numpy(x, v, dens, lam, dstep, p, dt):
-    """The 16 end-of-step features restated by brute force over all pairs (FP64)."""
+    """The end-of-step features restated by brute force over all pairs (FP64)."""
     h, r0, m = float(p.h), float(p.rest_dens), float(p.mass)
     aw = 315.0 / (64.0 * np.pi * h ** 9)
     ag = -45.0 / (np.pi * h ** 6)
@@ -76,7 +76,7 @@ def features_numpy(x, v, dens, lam, dstep, p, dt):
     qs = np.maximum(h * h - rs * rs, 0.0)
     with np.errstate(divide="ignore", invalid="ignore"):
         gs = np.where((rs > 0) & (rs < h), ag * (h - rs) ** 2 / rs, 0.0)
-    f = np.zeros((x.shape[0], 16))
+    f = np.zeros((x.shape[0], abi.MLP_FEATURES))
     f[:, 0] = dens / r0 - 1.0
     f[:, 1] = lam * r0 * h * h
     f[:, 2] = inside.sum(1) / 33.0
@@ -85,6 +85,14 @@ def features_numpy(x, v, dens, lam, dstep, p, dt):
     f[:, 9:12] = dstep[:, :3] / h
     f[:, 12] = m / r0 * aw * (qs ** 3).sum(1) - 1.0
     f[:, 13:16] = m / r0 * h * (gs[..., None] * ds).sum(1)
+    # poly6-weighted means over the neighbours, self excluded
+    w = np.where(r > 0, np.maximum(h * h - r * r, 0.0) ** 3, 0.0)
+    nw = w.sum(1)
+    has = nw > 0
+    inw = np.where(has, 1.0 / np.where(has, nw, 1.0), 0.0)
+    f[:, 16] = np.where(has, (w @ dens.astype(np.float64)) * inw / r0 - 1.0, 0.0)
+    f[:, 17:20] = (w @ V) * inw[:, None] * dt / h
+    f[:, 20:23] = (w @ dstep[:, :3].astype(np.float64)) * inw[:, None] / h
     return f
 
 
@@ -94,11 +102,11 @@ def test_features_match_numpy(gpu):
     sc, p = make(block=(10, 8, 20), collect=1, seed=5)
     p.xsph_c, p.vort_eps = 0.0, 0.0
     ps, _, _ = run(sc, p, 25)
-    f = ps.GetArrayVBO(abi.FSPH_FEATURES).reshape(sc.n, 16)
+    f = ps.GetArrayVBO(abi.FSPH_FEATURES).reshape(sc.n, abi.MLP_FEATURES)
     ref = features_numpy(ps.GetArrayVBO(abi.RX_POSITION), ps.GetArrayVBO(abi.RX_VELOCITY),
                          ps.GetArrayVBO(abi.RX_DENSITY), ps.GetArrayVBO(abi.RX_SCALING_FACTOR),
                          ps.GetArrayVBO(abi.RX_STEP_CORRECTION), p, sc.dt)
-    for k in range(16):
+    for k in range(abi.MLP_FEATURES):
         scale = max(np.abs(ref[:, k]).max(), 1e-3)
         err = np.abs(f[:, k] - ref[:, k]).max() / scale
         assert err < 2e-3, (k, err)

@@ -72,6 +72,7 @@ struct fsph_ctx {
     unsigned int *warm_valid = nullptr;
     MlpDev *mlp_dev = nullptr;
     bool model_loaded = false;
+    bool model_nbr = true;          /* the loaded network uses the neighbour-mean features */
     ErrPartial *epart = nullptr;
     float *dpart = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -458,6 +459,7 @@ void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
         FeatureOut fo;
         if (ws) {
             fo.feat = c->feat;
+            fo.nbr = (c->P.collect_features || c->model_nbr) ? 1 : 0;
             fo.dstep = c->dstep;
             fo.ppos0 = c->ppos[0];
             fo.ppos1 = c->ppos[1];
@@ -1129,6 +1131,10 @@ int fsph_set_warm_start_model(fsph_ctx *c, const float *blob) {
     cudaFree(d);
     if (e != cudaSuccess) return fail(c, FSPH_CUDA_ERROR, std::string("warm-start model: ") + cudaGetErrorString(e));
     c->model_loaded = true;
+    /* an input whose spread is given as >= 1e29 carries no weight */
+    c->model_nbr = false;
+    for (int k = kNbrFirst; k <= kNbrLast; ++k)
+        if (blob[FSPH_MLP_FEATURES + k] < 1e29f) c->model_nbr = true;
     return FSPH_OK;
 }
 

@@ -100,6 +100,7 @@ __host__ __device__ inline size_t list_at(int t, int i, int n) {
  *   23-31 zero (the network's input is padded to two 16-wide MMA k-steps)
  * Row-major, kFeatures floats per particle. */
 constexpr int kFeatures = 32;
+constexpr int kNbrFirst = 16, kNbrLast = 22; /* the neighbour-mean features */
 struct DevCtl;
 struct FeatureOut {
     float *feat = nullptr;             /* [n][kFeatures]; nullptr: no features */
@@ -107,6 +108,7 @@ struct FeatureOut {
     const float4 *ppos0 = nullptr, *ppos1 = nullptr;
     const DevCtl *ctl = nullptr;
     unsigned int *valid = nullptr;     /* set to 1 once features exist */
+    int nbr = 1;                       /* 1: the neighbour means (16-22) too; 0: left zero */
 };
 
 /* Device control block of one context: the loop state that the reference

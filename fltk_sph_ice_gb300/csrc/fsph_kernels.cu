@@ -395,6 +395,7 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
 
 /* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), and the
  * XSPH update v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij. */
+template <bool NBR>
 __global__ void __launch_bounds__(kBlock) k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_start,
                                                       const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                       const float *__restrict__ dens, float4 *__restrict__ vel_out,
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(kBlock) k_xsph_vort(DevParams p, const unsigne
     __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    xsph_vort_body(p, i, cell_start, pos, vel, dens, vel_out, vort, fo, list, cnt, cellb, s_rs + threadIdx.x);
+    xsph_vort_body<NBR>(p, i, cell_start, pos, vel, dens, vel_out, vort, fo, list, cnt, cellb, s_rs + threadIdx.x);
 }
 
 /* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
@@ -805,8 +806,10 @@ void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
                       const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, const NbrLists &nl,
                       cudaStream_t s) {
-    k_xsph_vort<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort, fo,
-                                                   p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
+    /* the neighbour means cost a gather per pair: only when they are used */
+    auto k = (fo.feat && fo.nbr) ? k_xsph_vort<true> : k_xsph_vort<false>;
+    k<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort, fo,
+                                         p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
                        const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s) {

@@ -503,6 +503,7 @@ __device__ __forceinline__ void correction_tail(const DevParams &lp, DevCtl *ctl
 /* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), the XSPH
  * update v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij, and (fo.feat) the
  * warm-start features of the particle. */
+template <bool NBR = true>
 __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
                                                const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                const float *__restrict__ dens, float4 *__restrict__ vel_out,
@@ -548,11 +549,13 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
                 const float ts = fmaxf(p.h - r2s * inv_rs, 0.0f);
                 wpred += qs * qs * qs;
                 cg = cg + (p.ag * ts * ts * inv_rs) * ds;
-                const float w = r2 > 0.0f ? q * q * q : 0.0f;
-                nw += w;
-                nrho += w * rhoj;
-                nv = nv + w * vij;
-                nd = nd + w * f3(__ldg(fo.dstep + j));
+                if (NBR) {
+                    const float w = r2 > 0.0f ? q * q * q : 0.0f;
+                    nw += w;
+                    nrho += w * rhoj;
+                    nv = nv + w * vij;
+                    nd = nd + w * f3(__ldg(fo.dstep + j));
+                }
             }
         });
     cntf = fmaxf(cntf, 1.0f);

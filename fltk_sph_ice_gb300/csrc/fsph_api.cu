@@ -411,7 +411,7 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     /* warm-start correction of every particle, home order */
     const float4 *dw = nullptr;
     if (c->P.warm_start == 1) {
-        launch_mlp_infer(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, s);
+        launch_mlp_infer(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, s, !c->model_nbr);
         dw = c->dwarm;
     }
     int src = 0, it = 1;

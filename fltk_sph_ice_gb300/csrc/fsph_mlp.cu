@@ -92,11 +92,14 @@ struct Fwd {
     float xn[kIn / 2];
 };
 
+/* KT: the 16-wide input tiles read (inputs past them contribute nothing:
+ * a network that gives them no weight runs with KT = 1) */
+template <int KT = kIn / 16>
 __device__ __forceinline__ void mlp_forward(const MlpDev &sm, const float *__restrict__ x, int n, int base, int g,
                                             int c, Fwd &F) {
     const int r0 = base + g, r1 = base + g + 8;
 #pragma unroll
-    for (int kt = 0; kt < kIn / 16; ++kt) {
+    for (int kt = 0; kt < KT; ++kt) {
         const int cols[4] = {16 * kt + 2 * c, 16 * kt + 2 * c + 1, 16 * kt + 2 * c + 8, 16 * kt + 2 * c + 9};
         float *xn = F.xn + 8 * kt;
 #pragma unroll
@@ -117,7 +120,7 @@ __device__ __forceinline__ void mlp_forward(const MlpDev &sm, const float *__res
         const float b0v = sm.b1[8 * j + 2 * c], b1v = sm.b1[8 * j + 2 * c + 1];
         F.h1[j][0] = b0v; F.h1[j][1] = b1v; F.h1[j][2] = b0v; F.h1[j][3] = b1v;
 #pragma unroll
-        for (int kt = 0; kt < kIn / 16; ++kt) {
+        for (int kt = 0; kt < KT; ++kt) {
             const __nv_bfloat16 *w = sm.w1t + (8 * j + g) * kS1 + 16 * kt + 2 * c;
             mma16816(F.h1[j], F.ax[kt], ld32(w), ld32(w + 8));
         }
@@ -161,6 +164,7 @@ __device__ __forceinline__ void mlp_forward(const MlpDev &sm, const float *__res
 
 /* y = net(x) * out_scale * scale into float4 rows (inference in the step) or
  * plain rows of 3 (y3). */
+template <int KT>
 __global__ void __launch_bounds__(128) k_mlp_infer(const MlpDev *__restrict__ gm, const float *__restrict__ x, int n,
                                                    float4 *__restrict__ y, float *__restrict__ y3, float scale,
                                                    const unsigned int *__restrict__ valid) {
@@ -181,7 +185,7 @@ __global__ void __launch_bounds__(128) k_mlp_infer(const MlpDev *__restrict__ gm
             continue;
         }
         Fwd F;
-        mlp_forward(sm, x, n, base, g, c, F);
+        mlp_forward<KT>(sm, x, n, base, g, c, F);
         const float y2a = __shfl_down_sync(0xffffffffu, F.o[0], 1);
         const float y2b = __shfl_down_sync(0xffffffffu, F.o[2], 1);
         if (c == 0) {
@@ -439,11 +443,12 @@ static unsigned int infer_blocks(int n) {
 }
 
 void launch_mlp_infer(const MlpDev *m, const float *x, int n, float4 *y, float scale, const unsigned int *valid,
-                      cudaStream_t s) {
-    k_mlp_infer<<<infer_blocks(n), 128, 0, s>>>(m, x, n, y, nullptr, scale, valid);
+                      cudaStream_t s, bool local_only) {
+    auto k = local_only ? k_mlp_infer<1> : k_mlp_infer<kIn / 16>;
+    k<<<infer_blocks(n), 128, 0, s>>>(m, x, n, y, nullptr, scale, valid);
 }
 void launch_mlp_forward3(const MlpDev *m, const float *x, int n, float *y, cudaStream_t s) {
-    k_mlp_infer<<<infer_blocks(n), 128, 0, s>>>(m, x, n, nullptr, y, 1.0f, nullptr);
+    k_mlp_infer<kIn / 16><<<infer_blocks(n), 128, 0, s>>>(m, x, n, nullptr, y, 1.0f, nullptr);
 }
 void launch_mlp_grad(const MlpDev *m, const float *x, const float *t, int n, float *part, float *loss_part,
                      cudaStream_t s) {

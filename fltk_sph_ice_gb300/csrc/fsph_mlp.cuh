@@ -53,9 +53,10 @@ struct MlpDev {
 void launch_mlp_pack(const float *blob, MlpDev *dev, cudaStream_t s);
 /* y[i] = network(x[i]) * out_scale * scale (first 3 components; w = 0);
  * x: n rows of kIn raw features.  If valid != NULL and *valid == 0 the
- * outputs are zero (no features yet). */
+ * outputs are zero (no features yet).  local_only: read only the first 16
+ * inputs (for a network that gives the others no weight). */
 void launch_mlp_infer(const MlpDev *m, const float *x, int n, float4 *y, float scale, const unsigned int *valid,
-                      cudaStream_t s);
+                      cudaStream_t s, bool local_only = false);
 /* same network, plain n x 3 output (for training checks) */
 void launch_mlp_forward3(const MlpDev *m, const float *x, int n, float *y, cudaStream_t s);
 /* per-block partial gradients of L = mean_i sum_k (y_ik - t_ik / out_scale)^2

@@ -10,8 +10,9 @@ change how many iterations a step takes, never the tolerance it reaches.
     python -m fltk_sph_ice_gb300.warmstart --out fltk_sph_ice_gb300/models/warmstart_mlp.npz
 
 collects rollouts of the plain solver on seeded double-dam-break scenes
-(16k-131k particles; --sizes large: 65k-262k), trains on the GPU with fsph_mlp_train (Adam) and
-writes the parameter blob plus its training record.
+(65k-262k particles), trains on the GPU with fsph_mlp_train (Adam) and
+writes the parameter blob plus its training record; the defaults reproduce
+the committed network.
 """
 from __future__ import annotations
 
@@ -225,12 +226,14 @@ def main():
     ap.add_argument("--epochs", type=int, default=24)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--sizes", default="small", choices=["small", "large", "config"],
+    ap.add_argument("--sizes", default="config", choices=["small", "large", "config"],
                     help="training scenes of 16k-131k particles (small), 65k-262k with columns up to twice as "
                          "tall as wide (large), or 65k-262k with columns no taller than wide (config)")
-    ap.add_argument("--features", default="all", choices=["all", "base"],
+    ap.add_argument("--features", default="base", choices=["all", "base"],
                     help="all features, or only the first 16 (the neighbour means are given no weight)")
-    ap.add_argument("--seed", type=int, default=0, help="initialisation and shuffling seed of the training")
+    ap.add_argument("--seed", type=int, default=4,
+                    help="initialisation and shuffling seed of the training (the committed network: seed 4, the "
+                         "best of seeds 0-5 on the held-out validation scenes)")
     ap.add_argument("--data", default=None, metavar="NPZ",
                     help="reuse the rollout samples stored in NPZ (written there when it does not exist)")
     args = ap.parse_args()

@@ -285,7 +285,9 @@ int fsph_get_boundary(fsph_ctx *ctx, int which, float *dst);
  * FSPH_MLP_BLOB_SIZE floats: mu[32], sigma[32] (input standardisation),
  * W1[32][64], b1[64], W2[64][64], b2[64], W3[64][3], b3[3], out_scale[1].
  * Output = (network of (x - mu) / sigma) * out_scale = predicted step
- * correction / h.  No counterpart in the reference (its PBF loop always
+ * correction / h.  An input whose sigma is >= 1e29 carries no weight; when
+ * inputs 16-22 (the neighbour means) all carry none, the step neither
+ * computes nor reads them.  No counterpart in the reference (its PBF loop always
  * starts from the prediction, rx_sph_pbd.cpp:418-425). */
 #define FSPH_MLP_FEATURES 32
 #define FSPH_MLP_HIDDEN 64

@@ -1,0 +1,57 @@
+"""The committed warm-start network and the training options, on the CPU:
+blob layout, the unweighted-input convention (an input whose sigma is at
+least 1e29 carries no weight) and the oracle network's response to it."""
+import json
+import os
+
+import numpy as np
+
+import oracle.mlp as omlp
+from fltk_sph_ice_gb300 import abi, warmstart
+
+
+def _committed():
+    assert os.path.isfile(warmstart.DEFAULT_MODEL)
+    return warmstart.load_model(warmstart.DEFAULT_MODEL)
+
+
+def test_committed_blob_layout():
+    blob, meta = _committed()
+    assert blob.shape == (abi.MLP_BLOB_SIZE,) == (omlp.BLOB,)
+    assert np.isfinite(blob).all()
+    assert blob[warmstart.O_SCALE] > 0
+    assert meta["epochs"] > 0 and len(meta["loss"]) == meta["epochs"]
+    assert 0.5 <= meta["output_damping"] <= 1.0
+
+
+def test_committed_network_weights_only_what_its_record_says():
+    blob, meta = _committed()
+    sig = blob[warmstart.O_SIG:warmstart.O_W1]
+    local = sig[:warmstart.BASE_FEATURES]
+    assert (local < 1e29).all()
+    if meta.get("features") == "base":
+        assert (sig[warmstart.BASE_FEATURES:] >= 1e29).all()
+
+
+def test_unweighted_inputs_do_not_change_the_output():
+    """With sigma >= 1e29 on inputs 16-31, any finite values there leave the
+    network's output unchanged (FP64 oracle, and with the BF16 rounding the
+    kernels apply)."""
+    blob, _ = _committed()
+    b = np.array(blob, np.float32)
+    b[warmstart.O_SIG + warmstart.BASE_FEATURES:warmstart.O_W1] = np.float32(1e30)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((257, abi.MLP_FEATURES)).astype(np.float32)
+    x2 = x.copy()
+    x2[:, warmstart.BASE_FEATURES:] = rng.uniform(-1e3, 1e3, (257, abi.MLP_FEATURES - warmstart.BASE_FEATURES))
+    for emul in (False, True):
+        y1, _ = omlp.forward(b, x, bf16_emul=emul)
+        y2, _ = omlp.forward(b, x2, bf16_emul=emul)
+        assert np.allclose(y1, y2, rtol=0, atol=1e-12 * max(1.0, np.abs(y1).max()))
+
+
+def test_training_record_is_json():
+    _, meta = _committed()
+    json.dumps(meta)
+    for k in ("samples", "rollouts", "epochs", "loss", "damping_table"):
+        assert k in meta

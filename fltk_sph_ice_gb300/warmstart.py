@@ -215,6 +215,56 @@ def calibrate_damping(blob, alphas=(0.6, 0.7, 0.8, 0.9, 1.0)):
     return best, table
 
 
+def next_block(sizes: str, rng) -> tuple[int, int, int]:
+    """The (bx, by, 2 bx) blocks of the next training rollout: two such blocks
+    of a double dam break, so 4 bx^2 by particles.
+      config: 65k-262k particles, bx in 26..40, columns from half as tall as
+              wide up to square (the configuration's stated range);
+      large:  65k-262k particles, bx in 21..32, columns up to twice as tall
+              as wide;
+      small:  16k-131k particles, bx in 20..32, columns no taller than wide."""
+    if sizes == "config":
+        bx = int(rng.integers(26, 41))
+        by = int(rng.integers(max(bx // 2, -(-65536 // (4 * bx * bx))), bx + 1))
+    elif sizes == "large":
+        bx = int(rng.integers(21, 33))
+        by = int(rng.integers(max(bx // 2, -(-65536 // (4 * bx * bx))), 2 * bx + 1))
+    elif sizes == "small":
+        bx = int(rng.integers(20, 33))
+        by = int(rng.integers(max(8, bx // 2), bx + 1))
+    else:
+        raise ValueError(f"unknown training sizes {sizes!r}")
+    return bx, by, 2 * bx
+
+
+# held-out validation scenes (block, seed): neither training, calibration, test nor bench scenes
+VALID_SCENES = (((56, 56, 112), 600), ((48, 40, 96), 601))
+
+
+def validation_iterations(blob) -> float:
+    """Mean constraint iterations per step over the validation scenes, steps
+    104-143 of each (after the dam has broken)."""
+    return float(np.mean([mean_iterations(blob, blk, seed, steps=144, skip=104) for blk, seed in VALID_SCENES]))
+
+
+def train_network(X, T, features: str, seed: int, epochs: int, batch: int, lr: float):
+    """One network on the samples: (blob, loss per epoch).  features "base"
+    gives the inputs from BASE_FEATURES on an infinite spread (no weight)."""
+    blob = init_blob(X, T, seed=seed)
+    if features == "base":
+        blob[O_SIG + BASE_FEATURES:O_W1] = np.float32(1e30)
+    net = WarmStartNet(blob)
+    hist = net.train(X, T, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    out = net.get_blob()
+    net.close()
+    return out, hist
+
+
+def select_seed(scores: dict) -> int:
+    """The seed with the fewest validation iterations (the lowest seed on a tie)."""
+    return min(sorted(scores), key=lambda k: scores[k])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=DEFAULT_MODEL)
@@ -234,6 +284,9 @@ def main():
     ap.add_argument("--seed", type=int, default=4,
                     help="initialisation and shuffling seed of the training (the committed network: seed 4, the "
                          "best of seeds 0-5 on the held-out validation scenes)")
+    ap.add_argument("--seeds", default=None, metavar="LIST",
+                    help="train one network per seed (e.g. 0,1,2,3,4,5) on the same samples and keep the one "
+                         "with the fewest iterations on the validation scenes")
     ap.add_argument("--data", default=None, metavar="NPZ",
                     help="reuse the rollout samples stored in NPZ (written there when it does not exist)")
     args = ap.parse_args()
@@ -257,21 +310,9 @@ def main():
         d = np.load(args.data)
         X, T, blocks = [d["X"]], [d["T"]], [tuple(int(v) for v in b) for b in d["blocks"]]
     for r in range(0 if loaded else args.rollouts):
-        if args.sizes == "config":
-            # 65k..262k particles: bx in 26..40, columns from half as tall as wide up to square
-            bx = int(rng.integers(26, 41))
-            by = int(rng.integers(max(bx // 2, -(-65536 // (4 * bx * bx))), bx + 1))
-        elif args.sizes == "large":
-            # 65k..262k particles: two bx x by x 2bx blocks, bx in 21..32, columns
-            # from half as tall as wide up to twice as tall (64 layers)
-            bx = int(rng.integers(21, 33))
-            by = int(rng.integers(max(bx // 2, -(-65536 // (4 * bx * bx))), 2 * bx + 1))
-        else:
-            # 16k..131k particles: bx in 20..32, columns no taller than wide
-            bx = int(rng.integers(20, 33))
-            by = int(rng.integers(max(8, bx // 2), bx + 1))
-        blocks.append((bx, by, 2 * bx))
-        x, t, _ = collect_rollout((bx, by, 2 * bx), seed=1000 + r, steps=args.steps, per_step=args.per_step, rng=rng)
+        blk = next_block(args.sizes, rng)
+        blocks.append(blk)
+        x, t, _ = collect_rollout(blk, seed=1000 + r, steps=args.steps, per_step=args.per_step, rng=rng)
         X.append(x)
         T.append(t)
     X = np.concatenate(X).astype(np.float32)
@@ -279,21 +320,27 @@ def main():
     if args.data is not None and not loaded:
         np.savez(args.data, X=X, T=T, blocks=np.asarray(blocks))
     t_collect = time.time() - t0
-    blob = init_blob(X, T, seed=args.seed)
-    if args.features == "base":
-        # the neighbour means get an infinite spread: their normalised inputs are zero
-        blob[O_SIG + BASE_FEATURES:O_W1] = np.float32(1e30)
-    net = WarmStartNet(blob)
-    hist = net.train(X, T, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed)
-    blob = net.get_blob()
-    meta = dict(samples=int(X.shape[0]), rollouts=args.rollouts, steps=args.steps, per_step=args.per_step,
-                epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
-                train_s=time.time() - t0 - t_collect, target_var=float((T / blob[O_SCALE]).var() * 3),
-                sizes=args.sizes, features=args.features, seed=args.seed, blocks=blocks[:8])
-    alpha, table = calibrate_damping(blob)
-    blob[O_SCALE] *= alpha
-    meta["output_damping"] = alpha
-    meta["damping_table"] = {str(k): v for k, v in table.items()}
+    seeds = [int(v) for v in args.seeds.split(",")] if args.seeds else [args.seed]
+    candidates, scores = {}, {}
+    for sd in seeds:
+        t1 = time.time()
+        blob, hist = train_network(X, T, args.features, sd, args.epochs, args.batch, args.lr)
+        meta = dict(samples=int(X.shape[0]), rollouts=len(blocks), steps=args.steps, per_step=args.per_step,
+                    epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
+                    train_s=time.time() - t1, target_var=float((T / blob[O_SCALE]).var() * 3),
+                    sizes=args.sizes, features=args.features, seed=sd, blocks=blocks[:8])
+        alpha, table = calibrate_damping(blob)
+        blob[O_SCALE] *= alpha
+        meta["output_damping"] = alpha
+        meta["damping_table"] = {str(k): v for k, v in table.items()}
+        candidates[sd] = (blob, meta)
+        if len(seeds) > 1:
+            scores[sd] = validation_iterations(blob)
+            print(json.dumps({"seed": sd, "loss": hist[-1], "validation_iterations": scores[sd]}), flush=True)
+    best = select_seed(scores) if scores else seeds[0]
+    blob, meta = candidates[best]
+    if scores:
+        meta["selection"] = {str(k): v for k, v in scores.items()}
     save_model(args.out, blob, meta)
     print(json.dumps({k: v for k, v in meta.items() if k != "blocks"}))
 

@@ -55,3 +55,21 @@ def test_training_record_is_json():
     json.dumps(meta)
     for k in ("samples", "rollouts", "epochs", "loss", "damping_table"):
         assert k in meta
+
+
+def test_training_scene_sizes():
+    """The stated particle ranges of the three training distributions
+    (4 bx^2 by particles per double dam break)."""
+    for sizes, lo, hi, tall in (("config", 65536, 262144, 1.0), ("large", 65536, 262144, 2.0),
+                                ("small", 16000, 131072, 1.0)):
+        rng = np.random.default_rng(12345)
+        for _ in range(500):
+            bx, by, bz = warmstart.next_block(sizes, rng)
+            n = 4 * bx * bx * by
+            assert bz == 2 * bx and lo <= n <= hi, (sizes, bx, by, n)
+            assert by <= tall * bx
+
+
+def test_seed_selection():
+    assert warmstart.select_seed({0: 5.65, 1: 4.86, 2: 6.95, 4: 4.33, 5: 4.94}) == 4
+    assert warmstart.select_seed({3: 2.0, 1: 2.0}) == 1

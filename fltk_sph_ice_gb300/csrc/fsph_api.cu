@@ -885,6 +885,7 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
     if (start < 0 || count < 0 || start + count > c->n) return fail(c, FSPH_INVALID_ARG, "range outside [0, n)");
     if (type != FSPH_POSITION && type != FSPH_VELOCITY && type != FSPH_ATTRIBUTE)
         return fail(c, FSPH_INVALID_ARG, "settable arrays: POSITION, VELOCITY, ATTRIBUTE");
+    if (count == 0) return FSPH_OK; /* nothing to overwrite (and no kernel for an empty range) */
     cudaStream_t s = c->stream;
     int n = c->n;
     /* bring the home arrays to particle order (once after a step), then

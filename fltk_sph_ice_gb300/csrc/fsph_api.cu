@@ -636,6 +636,7 @@ int load_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int
         FSPH_CUDA(c, cudaMemsetAsync(c->set[0].attr, 0, (size_t)n * 4, c->stream));
         launch_iota(n, c->set[0].id, c->stream);
         c->home_identity = true;
+        c->res_in_res_id = false;
         /* a new state has no step history for the warm start */
         FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, b, c->stream));
     }

@@ -314,6 +314,44 @@ def ncu_traffic(kname: str):
     return None
 
 
+def ncu_warp_instructions(kname: str):
+    """Warp instructions of one launch of kname at 1M particles, from the
+    committed ncu summary's 'warp instructions' row; None if absent."""
+    import re
+    if not os.path.isfile(TRAFFIC_PROFILE):
+        return None
+    with open(TRAFFIC_PROFILE) as f:
+        for line in f:
+            if line.startswith("| warp instructions"):
+                m = [float(x) for x in re.findall(r"([0-9.]+) M", line)]
+                col = {"k_lambda": 0, "k_correction": 1}.get(kname)
+                if col is not None and len(m) >= 2:
+                    return m[col] * 1e6
+    return None
+
+
+def issue_bound(kname: str, launch_ms: float):
+    """The pass against the instruction-issue bound: the profiled warp
+    instructions of one launch over its live launch time, against one warp
+    instruction per SM sub-partition per clock (152 SMs x 4 at the maximum
+    SM clock of MEASURED_PEAKS.json, else 2070 MHz); None without a profile."""
+    try:
+        inst = ncu_warp_instructions(kname)
+        if inst is None or not launch_ms > 0:
+            return None
+        mhz = 2070.0
+        p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.isfile(p):
+            with open(p) as f:
+                mhz = float(json.load(f).get("sm_max_mhz", mhz))
+        peak = 152 * 4 * mhz * 1e6 / 1e12
+        achieved = inst / (launch_ms / 1000.0) / 1e12
+        return {"unit": "T warp instructions/s", "warp_instructions": inst, "achieved": achieved, "peak": peak,
+                "frac": achieved / peak}
+    except (OSError, ValueError, TypeError):
+        return None
+
+
 def roofline_of(L, abi, ps, n, mean_iters):
     t_lam, t_cor, t_grid, t_list = (ctypes.c_float(0) for _ in range(4))
     L.fsph_time_pass(ps.handle, abi.PASS_LAMBDA, 20, ctypes.byref(t_lam))
@@ -330,7 +368,7 @@ def roofline_of(L, abi, ps, n, mean_iters):
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
             "lambda_ms": t_lam.value, "correction_ms": t_cor.value, "grid_build_ms": t_grid.value,
-            "list_build_ms": t_list.value,
+            "list_build_ms": t_list.value, "issue": issue_bound(kname, kms),
             "passes_ms_per_step": mean_iters * (t_lam.value + t_cor.value)}
 
 

@@ -208,6 +208,17 @@ public:
         if (!out.empty()) m_status = fsph_get_boundary(m_ctx, which, out.data());
         return out;
     }
+    /* The learned warm start (no counterpart in the reference): a network
+     * blob of FSPH_MLP_BLOB_SIZE floats (the layout of fsph.h), used by the
+     * steps while the parameters have warm_start = 1. */
+    bool SetWarmStartModel(const std::vector<float> &blob) {
+        if (blob.size() != (size_t)FSPH_MLP_BLOB_SIZE) {
+            m_status = FSPH_INVALID_ARG;
+            return false;
+        }
+        m_status = fsph_set_warm_start_model(m_ctx, blob.data());
+        return m_status == FSPH_OK;
+    }
     /* Initialize(env) derivation (rx_sph_pbd.cpp:102-201) */
     static fsph_params ParamsFromEnv(const fsph_env &env) {
         fsph_params p;

@@ -73,3 +73,39 @@ def test_training_scene_sizes():
 def test_seed_selection():
     assert warmstart.select_seed({0: 5.65, 1: 4.86, 2: 6.95, 4: 4.33, 5: 4.94}) == 4
     assert warmstart.select_seed({3: 2.0, 1: 2.0}) == 1
+
+
+def test_damping_calibration_picks_fewest_iterations(monkeypatch):
+    """calibrate_damping scores every alpha on the held-out scenes and keeps
+    the one with the fewest mean iterations (solver calls replaced by a fake)."""
+    blob, _ = _committed()
+    seen = []
+
+    def fake(b, block, seed, steps=60, skip=30):
+        a = float(b[warmstart.O_SCALE] / blob[warmstart.O_SCALE])
+        seen.append((round(a, 3), seed))
+        return 10.0 + 40.0 * (a - 0.8) ** 2 + seed * 1e-3
+
+    monkeypatch.setattr(warmstart, "mean_iterations", fake)
+    alpha, table = warmstart.calibrate_damping(blob)
+    assert alpha == 0.8
+    assert sorted(table) == [0.6, 0.7, 0.8, 0.9, 1.0]
+    assert len(seen) == 5 * len(warmstart.CALIB_SCENES)
+    assert {s for _, s in seen} == {s for _, s in warmstart.CALIB_SCENES}
+
+
+def test_validation_score_is_the_mean_over_the_validation_scenes(monkeypatch):
+    calls = []
+
+    def fake(b, block, seed, steps=60, skip=30):
+        calls.append((block, seed, steps, skip))
+        return float(seed - 590)
+
+    monkeypatch.setattr(warmstart, "mean_iterations", fake)
+    v = warmstart.validation_iterations(np.zeros(abi.MLP_BLOB_SIZE, np.float32))
+    assert [c[:2] for c in calls] == [tuple(s) for s in warmstart.VALID_SCENES]
+    assert all(c[2] == 144 and c[3] == 104 for c in calls)
+    assert v == np.mean([s - 590 for _, s in warmstart.VALID_SCENES])
+    # validation scenes are neither calibration nor training scenes
+    assert not {s for _, s in warmstart.VALID_SCENES} & {s for _, s in warmstart.CALIB_SCENES}
+    assert all(s < 1000 for _, s in warmstart.VALID_SCENES)

@@ -146,7 +146,8 @@ EXPORTS = [
     "fsph_params_default", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params",
     "fsph_num_particles", "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats",
     "fsph_get_array", "fsph_device_ptr", "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda",
-    "fsph_pbf_eval_correction", "fsph_sph_eval_forces", "fsph_time_pass", "fsph_pbf_eval_lambda_noalloc",
+    "fsph_pbf_eval_correction", "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_time_pass",
+    "fsph_pbf_eval_lambda_noalloc",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
     "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
     "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
@@ -189,6 +190,8 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_pbf_eval_lambda.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_void_p]
     L.fsph_pbf_eval_correction.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p]
     L.fsph_sph_eval_forces.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+    L.fsph_pbf_eval_xsph_vorticity.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p,
+                                               c_void_p]
     L.fsph_time_pass.argtypes = [c_void_p, c_int, c_int, P(c_float)]
     L.fsph_mlp_create.argtypes = [P(c_void_p)]
     L.fsph_mlp_destroy.argtypes = [c_void_p]
@@ -228,7 +231,7 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
                  "fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",
                  "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats", "fsph_get_array",
                  "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda", "fsph_pbf_eval_correction",
-                 "fsph_sph_eval_forces", "fsph_params_from_env"]:
+                 "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_params_from_env"]:
         getattr(L, name).restype = c_int
     return L
 

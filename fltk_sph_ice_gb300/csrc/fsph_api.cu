@@ -883,7 +883,7 @@ int fsph_set_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n,
 
 int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count, int where) {
     if (!c || !data) return FSPH_INVALID_ARG;
-    if (start < 0 || count < 0 || start + count > c->n) return fail(c, FSPH_INVALID_ARG, "range outside [0, n)");
+    if (start < 0 || count < 0 || count > c->n - start) return fail(c, FSPH_INVALID_ARG, "range outside [0, n)");
     if (type != FSPH_POSITION && type != FSPH_VELOCITY && type != FSPH_ATTRIBUTE)
         return fail(c, FSPH_INVALID_ARG, "settable arrays: POSITION, VELOCITY, ATTRIBUTE");
     if (count == 0) return FSPH_OK; /* nothing to overwrite (and no kernel for an empty range) */
@@ -914,12 +914,22 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
         c->home_identity = true;
     }
     cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    if (type == FSPH_POSITION)
-        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos + start, data, (size_t)count * 16, k, s));
-    else if (type == FSPH_VELOCITY)
-        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel + start, data, (size_t)count * 16, k, s));
-    else
+    if (type == FSPH_POSITION || type == FSPH_VELOCITY) {
+        /* staged and checked before it replaces anything: a range with a
+         * non-finite value is rejected and the state stays as it was (the
+         * same rule as fsph_set_particles) */
+        FSPH_CUDA(c, cudaMemcpyAsync(c->tmp4, data, (size_t)count * 16, k, s));
+        FSPH_CUDA(c, cudaMemsetAsync(c->flag, 0, sizeof(unsigned int), s));
+        launch_check_finite(count, c->tmp4, nullptr, c->flag, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->flag_host, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        FSPH_TRY(check_launch(c));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        if (*c->flag_host) return fail(c, FSPH_NAN_DETECTED, "non-finite position or velocity");
+        float4 *dst = (type == FSPH_POSITION ? c->set[0].pos : c->set[0].vel) + start;
+        FSPH_CUDA(c, cudaMemcpyAsync(dst, c->tmp4, (size_t)count * 16, cudaMemcpyDeviceToDevice, s));
+    } else {
         FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr + start, data, (size_t)count * 4, k, s));
+    }
     FSPH_TRY(check_launch(c));
     FSPH_CUDA(c, cudaStreamSynchronize(s));
     return FSPH_OK;
@@ -1276,6 +1286,45 @@ int fsph_pbf_eval_correction(fsph_ctx *c, const float *pos4, const float *lambda
     FSPH_CUDA(c, cudaStreamSynchronize(s));
     /* the context's particles are left at the given positions, zero velocity */
     FSPH_TRY(fsph_set_particles(c, pos4, nullptr, n, FSPH_HOST));
+    return FSPH_OK;
+}
+
+int fsph_pbf_eval_xsph_vorticity(fsph_ctx *c, const float *pos4, const float *vel4, const float *dens, int n,
+                                 float dt, float *vel_out4, float *vort4) {
+    if (!c || !pos4 || !vel4 || !dens || !vel_out4 || !vort4) return FSPH_INVALID_ARG;
+    if (c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "XSPH / vorticity: PBF only");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
+    FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
+    if (n == 0) return FSPH_OK;
+    DevParams p = dev_for(c, n, dt);
+    cudaStream_t s = c->stream;
+    /* densities in particle order ride through the sort as a 32-bit stream */
+    unsigned int *dh = reinterpret_cast<unsigned int *>(c->pres);
+    float *ds = reinterpret_cast<float *>(c->dens);
+    FSPH_CUDA(c, cudaMemcpyAsync(dh, dens, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    enqueue_sort(c, p, c->set[0].pos, s);
+    Gather g{};
+    g.n4 = 3; g.n1 = 3;
+    g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+    g.src4[1] = c->set[0].pos; g.dst4[1] = c->xb;
+    g.src4[2] = c->set[0].vel; g.dst4[2] = c->set[1].vel;
+    g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
+    g.src1[1] = c->key; g.dst1[1] = c->nl.cellb;
+    g.src1[2] = dh; g.dst1[2] = reinterpret_cast<unsigned int *>(ds);
+    launch_gather(n, c->perm, g, nullptr, s);
+    launch_build_list(p, c->cell_start, c->xb, c->nl, s);
+    /* the end-of-step passes of a PBF step, on these inputs */
+    launch_xsph_vort(p, c->cell_start, c->set[1].pos, c->set[1].vel, ds, c->acc, c->vort, FeatureOut{}, c->nl, s);
+    launch_vort_apply(p, c->cell_start, c->set[1].pos, c->vort, ds, c->acc, c->tmp4, c->nl, s);
+    FSPH_TRY(check_launch(c));
+    launch_unsort4(n, c->set[1].id, c->tmp4, c->ppos[0], 1, s);
+    launch_unsort4(n, c->set[1].id, c->vort, c->ppos[1], 1, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(vel_out4, c->ppos[0], (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(vort4, c->ppos[1], (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(check_launch(c));
+    /* the context's particles are left at the given positions and velocities */
+    FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
     return FSPH_OK;
 }
 

@@ -206,6 +206,15 @@ class rxPBDSPH(rxParticleSystemBase):
         self._check(self.L.fsph_set_boundary(self._ctx, _ptr(b4) if b4.shape[0] else None, b4.shape[0], abi.HOST),
                     "fsph_set_boundary")
 
+    def SetWarmStartModel(self, blob):
+        """Install a trained warm-start network (FSPH_MLP_BLOB_SIZE floats);
+        used by steps with params.warm_start = 1.  No counterpart in the
+        reference (its PBF loop starts from the prediction, rx_sph_pbd.cpp:418-425)."""
+        b = np.ascontiguousarray(blob, dtype=np.float32)
+        if b.size != abi.MLP_BLOB_SIZE:
+            raise ValueError(f"a network blob has {abi.MLP_BLOB_SIZE} floats")
+        self._check(self.L.fsph_set_warm_start_model(self._ctx, _ptr(b)), "fsph_set_warm_start_model")
+
     def GetNumBoundaryParticles(self) -> int:
         return int(self.L.fsph_num_boundary(self._ctx))
 
@@ -236,6 +245,18 @@ class rxPBDSPH(rxParticleSystemBase):
         self._check(self.L.fsph_pbf_eval_correction(self._ctx, _ptr(pos4), _ptr(lam), n, float(dt), _ptr(dp)),
                     "fsph_pbf_eval_correction")
         return dp
+
+    def EvalXsphVorticity(self, pos, vel, dens, dt: float):
+        """The end-of-step XSPH smoothing (rx_pbdsph_kernel.cu:1090-1162) and
+        vorticity confinement on the given state: (velocity after both, omega)."""
+        pos4, vel4 = _as4(pos), _as4(vel)
+        dens = np.ascontiguousarray(dens, dtype=np.float32)
+        n = pos4.shape[0]
+        vo = np.zeros((n, 4), np.float32)
+        om = np.zeros((n, 4), np.float32)
+        self._check(self.L.fsph_pbf_eval_xsph_vorticity(self._ctx, _ptr(pos4), _ptr(vel4), _ptr(dens), n, float(dt),
+                                                        _ptr(vo), _ptr(om)), "fsph_pbf_eval_xsph_vorticity")
+        return vo, om
 
 
 def _as4(a) -> np.ndarray:

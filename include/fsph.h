@@ -185,7 +185,9 @@ int fsph_num_particles(const fsph_ctx *ctx);
  * this resets the particle count to n (n <= max_particles). */
 int fsph_set_particles(fsph_ctx *ctx, const float *pos4, const float *vel4, int n, int where);
 /* Overwrite `count` particles from index `start` of one array
- * (SetArrayVBO, rx_ps.h:260-262).  FSPH_POSITION, FSPH_VELOCITY, FSPH_ATTRIBUTE. */
+ * (SetArrayVBO, rx_ps.h:260-262).  FSPH_POSITION, FSPH_VELOCITY, FSPH_ATTRIBUTE.
+ * Positions and velocities must be finite: a range holding a NaN or an
+ * infinity returns FSPH_NAN_DETECTED and leaves the state unchanged. */
 int fsph_set_array(fsph_ctx *ctx, int type, const void *data, int start, int count, int where);
 
 /* ---- step (Update) ---- */
@@ -225,6 +227,17 @@ int fsph_pbf_eval_lambda(fsph_ctx *ctx, const float *pos4, int n, float *dens, f
  * rx_sph_pbd.cpp:925-1026) for given positions and lambdas.  Host arrays. */
 int fsph_pbf_eval_correction(fsph_ctx *ctx, const float *pos4, const float *lambda, int n,
                              float dt, float *dp4);
+/* The end-of-step passes of a PBF step on given inputs: the XSPH velocity
+ * smoothing v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij (xsphVisocosity,
+ * rx_pbdsph_kernel.cu:1090-1162, disabled in the reference at
+ * rx_sph_pbd_gpu.cpp:926-927) and the vorticity confinement of Macklin &
+ * Mueller 2013, eq. 15-16 (only a flag in the reference, rx_ps.h:161,238,
+ * the paper cited at rx_sph.h:1281), with params.xsph_c / vort_eps and dt.
+ * pos4, vel4 (n float4) and dens (n floats, the densities the passes divide
+ * by) in; vel_out4 (the velocity after both) and vort4 (omega) out.  Host
+ * arrays; synchronises. */
+int fsph_pbf_eval_xsph_vorticity(fsph_ctx *ctx, const float *pos4, const float *vel4, const float *dens, int n,
+                                 float dt, float *vel_out4, float *vort4);
 /* WCSPH density + force passes (rxSPH::calDensity / calForce,
  * rx_sph_cpu.cpp:495-656).  Host arrays; acc4 receives the acceleration. */
 int fsph_sph_eval_forces(fsph_ctx *ctx, const float *pos4, const float *vel4, int n,
@@ -241,7 +254,9 @@ int fsph_sph_eval_forces(fsph_ctx *ctx, const float *pos4, const float *vel4, in
  * pool, or a real-time loop where an allocation's latency or failure is not
  * acceptable.  No counterpart in the reference.
  *   - pos4, dens and lambda are DEVICE pointers owned by the caller
- *     (n float4 in, n floats out each), in particle order.  No context is used.
+ *     (n float4 in, n floats out each), in particle order.  No context is used,
+ *     so static boundary particles (fsph_set_boundary) never enter: the
+ *     results equal fsph_pbf_eval_lambda's only for a context without a boundary.
  *   - It allocates nothing: no cudaMalloc / cudaFree / allocating library call.
  *     Its working memory (grid tables, sorted copies) is one file-scope
  *     __device__ array that every GPU loading the library holds until exit.

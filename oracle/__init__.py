@@ -63,6 +63,7 @@ def orc_lib() -> ctypes.CDLL:
         L.fsph_orc_pbf_step.argtypes = [vp, cf, ci, vp]
         L.fsph_orc_pbf_step.restype = ci
         L.fsph_orc_sph_step.argtypes = [vp, cf]
+        L.fsph_orc_finalize_ext.argtypes = [vp, vp, vp, vp, cf, vp, vp]
         L.fsph_orc_neighbors.argtypes = [vp, vp, vp, vp, ctypes.c_longlong]
         L.fsph_orc_neighbors.restype = ctypes.c_longlong
         L.fsph_orc_pbf_lambda.argtypes = [vp, vp, vp, vp]
@@ -126,6 +127,16 @@ class Oracle:
 
     def sph_step(self, dt: float):
         self.L.fsph_orc_sph_step(self.h, dt)
+
+    def finalize_ext(self, pos4, vel4, dens, dt: float):
+        """XSPH + vorticity confinement alone on the given state: (velocity after both, omega)."""
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
+        dens = np.ascontiguousarray(dens, dtype=np.float32)
+        vo = np.zeros((self.n, 4), np.float32)
+        om = np.zeros((self.n, 4), np.float32)
+        self.L.fsph_orc_finalize_ext(self.h, _vp(pos4), _vp(vel4), _vp(dens), dt, _vp(vo), _vp(om))
+        return vo, om
 
     def neighbors(self, pos4):
         pos4 = np.ascontiguousarray(pos4, dtype=np.float32)

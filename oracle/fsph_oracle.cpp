@@ -756,6 +756,20 @@ int fsph_orc_pbf_step(fsph_orc *o, float dt, int fixed_iters, double *errs) {
 
 void fsph_orc_sph_step(fsph_orc *o, float dt) { ORC_DISPATCH(o, S->sph_step(dt)); }
 
+/* XSPH + vorticity confinement alone (the end of pbf_step) on the given
+ * positions, velocities and densities: velocity after both, and omega. */
+void fsph_orc_finalize_ext(fsph_orc *o, const float *pos4, const float *vel4, const float *dens, float dt,
+                           float *vel_out4, float *vort4) {
+    ORC_DISPATCH(o, {
+        load4(S->pos, pos4, S->n);
+        load4(S->vel, vel4, S->n);
+        for (int i = 0; i < S->n; ++i) S->dens[i] = dens[i];
+        S->finalize_extensions(dt);
+        store(vel_out4, S->vel);
+        store(vort4, S->vort);
+    });
+}
+
 /* Neighbour CSR of the given positions (ascending indices). */
 long long fsph_orc_neighbors(fsph_orc *o, const float *pos4, int *offsets, int *idx, long long cap) {
     long long total = 0;

@@ -43,7 +43,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 REF_OUT = os.path.join(ORACLE, "_ref")
 SRC_OUT = os.path.join(REF_OUT, "src")
-REF_ROOT = os.environ.get("FSPH_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $FSPH_REFERENCE_ROOT, else a sibling directory
+# "reference" beside this repository.
+REF_ROOT = os.environ.get("FSPH_REFERENCE_ROOT") or os.path.normpath(
+    os.path.join(ORACLE, "..", "..", "reference"))
 
 
 def _read(name: str) -> list[str]:

@@ -76,3 +76,25 @@ def assert_same_sets(off_a, idx_a, off_b, idx_b):
     ra, rb = csr_rows(off_a, idx_a), csr_rows(off_b, idx_b)
     bad = [i for i, (x, y) in enumerate(zip(ra, rb)) if not np.array_equal(x, y)]
     assert not bad, f"{len(bad)} particles with different neighbour sets, first {bad[:5]}"
+
+
+def assert_close(a, b, what, tol=1e-5, etol=1e-4, floor=1e-2, atol=None):
+    """Norm-wise: |a - b| <= tol max|b| + atol.  Element-wise, on the entries
+    above floor max|b|: |a - b| <= etol |b| + atol.  atol (per entry): the
+    FP32 storage error of the stored results a compared quantity is a
+    difference of (e.g. a position change), else 0."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = np.abs(b).max()
+    at = np.zeros(b.shape) if atol is None else np.broadcast_to(np.asarray(atol, np.float64), b.shape)
+    err = np.abs(a - b) - at
+    assert err.max() <= tol * scale, f"{what}: max(|a-b| - atol) / max|b| = {err.max() / scale:.3e} > {tol:.1e}"
+    big = np.abs(b) > floor * scale
+    assert big.any()
+    excess = err[big] - etol * np.abs(b)[big]
+    assert excess.max() <= 0.0, f"{what}: element-wise bar exceeded on {(excess > 0).sum()} of {big.sum()} entries"
+
+
+def ulp32(x):
+    """Spacing of float32 numbers at |x|: the rounding of a stored FP32 result."""
+    return np.spacing(np.abs(np.asarray(x, np.float32))).astype(np.float64)

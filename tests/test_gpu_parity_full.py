@@ -1,0 +1,282 @@
+"""GPU parity at the configured sizes, against the reference's OWN CPU code
+(oracle/_ref: rxPBDSPH::Update, rxSPH::Update, calScalingFactor,
+calPositionCorrection and rxNNGrid::GetNN cut from the reference sources and
+compiled here), started from identical states:
+
+  * 262,144 particles, the 64^3 PBF dam break (4 fixed iterations, as
+    configured), from the initial lattice and from a state 100 steps into the
+    collapse: whole steps, and the lambda / delta-p passes on their own;
+  * the 1,048,576-particle double dam break of the benchmark after its
+    100-step pre-roll: neighbour sets bit-exact, and one step at the
+    benchmark's list skin and at a skin so small that the grid and lists
+    are rebuilt inside the iteration loop;
+  * 32,768 particles, the 32^3 WCSPH dam break: ten steps.
+
+Reference steps are run with the reference's own loop (two-sided error,
+eta = 0, min = max = 4 iterations) and without XSPH / vorticity / clamp,
+which the reference's CPU path does not have.
+
+Bars (written in each call):
+  norm-wise   max|a - b| <= 1e-5 max|b| for density, lambda, delta-p,
+              position change, velocity and acceleration;
+  element-wise density 1e-5 relative on every particle; position change and
+              velocity 1e-4 relative plus the FP32 storage error (one ulp) of
+              the positions they are differences of, on entries above 1 % of
+              the largest; lambda and delta-p with each particle's condition
+              number (assert_lambda_close, assert_dp_close);
+  neighbour sets bit-exact.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import assert_close, ulp32
+from fltk_sph_ice_gb300 import abi, rxPBDSPH, rxSPH, scenes
+
+pytestmark = pytest.mark.gpu
+
+PBF_DT = 0.0016
+
+
+@pytest.fixture(scope="module")
+def ref_available():
+    if oracle.ref_lib() is None:
+        pytest.fail("the reference-code library oracle/_ref is not built (build() compiles it from "
+                    "oracle/_ref/src, extracted from the reference sources)")
+    return True
+
+
+def reference_setup(p):
+    """Parameters of a reference-comparable PBF run: the reference CPU loop
+    (two-sided error, exactly 4 iterations), no XSPH / vorticity / clamp."""
+    q = abi.FsphParams.from_buffer_copy(p)
+    q.eta, q.min_iter, q.max_iter = 0.0, 4, 4
+    q.error_mode = abi.ERR_TWO_SIDED
+    q.xsph_c, q.vort_eps, q.clamp_constraint = 0.0, 0.0, 0
+    q.warm_start = 0
+    return q
+
+
+def sorted_csr(off, idx):
+    """(row id, column) pairs of a CSR in (row, column) order: an order-free
+    form of the neighbour sets, compared without a Python loop."""
+    off = np.asarray(off, np.int64)
+    idx = np.asarray(idx, np.int64)
+    rows = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    o = np.lexsort((idx, rows))
+    return rows[o], idx[o]
+
+
+def assert_sets_equal(off_a, idx_a, off_b, idx_b):
+    assert np.array_equal(np.asarray(off_a), np.asarray(off_b)), \
+        f"neighbour counts differ for {(np.diff(off_a) != np.diff(off_b)).sum()} particles"
+    ra, ca = sorted_csr(off_a, idx_a)
+    rb, cb = sorted_csr(off_b, idx_b)
+    assert np.array_equal(ra, rb) and np.array_equal(ca, cb), \
+        f"{len(np.unique(ra[ca != cb]))} particles with different neighbour sets"
+
+
+def assert_step_equal(gpu, ref, x0, what):
+    """One step's results: the position change (element-wise with the
+    storage ulp of both positions), velocity and density."""
+    xg, xr = gpu.GetArrayVBO(abi.RX_POSITION)[:, :3], ref.get("pos")[:, :3]
+    x0 = np.asarray(x0)[:, :3]
+    storage = ulp32(xr) + ulp32(x0)
+    assert_close(xg - x0, xr.astype(np.float64) - x0, f"{what}: position change", atol=storage)
+    # v = (x* - x) / dt: the position storage error divided by dt
+    vg, vr = gpu.GetArrayVBO(abi.RX_VELOCITY)[:, :3], ref.get("vel")[:, :3]
+    assert_close(vg, vr, f"{what}: velocity", atol=storage / PBF_DT)
+    dg, dr = gpu.GetArrayVBO(abi.RX_DENSITY), ref.get("dens")
+    assert_close(dg, dr, f"{what}: density", etol=1e-5, floor=0.0)
+
+
+EPS32 = float(np.finfo(np.float32).eps)
+
+
+def assert_lambda_close(lg, lr, dg, dr, rho0, what):
+    """lambda = -C / (sum |grad C|^2 + eps) with C = rho / rho0 - 1: an FP32
+    density difference d(rho) moves C by d(rho) / rho0 and lambda by that
+    over |C| relative.  Norm-wise 1e-5; element-wise, on entries above 1 % of
+    max|lambda|: |dl| <= |l| (1e-4 + (|d(rho)| / rho0 + 4 eps32) / |C|)."""
+    lg, lr = np.asarray(lg, np.float64), np.asarray(lr, np.float64)
+    assert_close(lg, lr, what, etol=np.inf)
+    big = np.abs(lr) > 1e-2 * np.abs(lr).max()
+    C = np.asarray(dr, np.float64) / rho0 - 1.0
+    dC = np.abs(np.asarray(dg, np.float64) - np.asarray(dr, np.float64)) / rho0 + 4 * EPS32
+    bound = np.abs(lr) * (1e-4 + dC / np.maximum(np.abs(C), 1e-30))
+    bad = (np.abs(lg - lr) > bound) & big
+    assert not bad.any(), f"{what}: element-wise bar exceeded on {bad.sum()} of {big.sum()} entries"
+
+
+def dp_condition(x, lam, p, off, idx, dt):
+    """sum_j |(lambda_i + lambda_j + s_corr_ij) grad W_ij / rho0| per particle,
+    over the reference's neighbour sets (FP64): the scale of the terms whose
+    cancellation gives delta-p."""
+    off = np.asarray(off, np.int64)
+    rows = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    cols = np.asarray(idx, np.int64)
+    h, r0 = float(np.float32(p.h)), float(np.float32(p.rest_dens))
+    d = x[rows, :3].astype(np.float64) - x[cols, :3].astype(np.float64)
+    r = np.sqrt((d * d).sum(1))
+    ag = 45.0 / (np.pi * h ** 6)
+    aw = 315.0 / (64.0 * np.pi * h ** 9)
+    gw = np.where((r > 0) & (r <= h), ag * (h - r) ** 2, 0.0)
+    wq = aw * (h * h - (p.ap_q * h) ** 2) ** 3
+    sc = -p.ap_k * (aw * np.maximum(h * h - r * r, 0.0) ** 3 / wq) ** p.ap_n * dt * dt if p.use_ap else 0.0
+    lam = np.asarray(lam, np.float64)
+    term = np.abs(lam[rows] + lam[cols] + sc) * gw / r0
+    return np.bincount(rows, weights=term, minlength=len(off) - 1)
+
+
+def assert_dp_close(dg, dr, cond, what):
+    """Norm-wise 1e-5; element-wise, on components above 1 % of max|dp|:
+    |d(dp)| <= 1e-4 |dp| + 16 eps32 x the particle's term scale."""
+    dg, dr = np.asarray(dg, np.float64), np.asarray(dr, np.float64)
+    assert_close(dg, dr, what, etol=np.inf)
+    big = np.abs(dr) > 1e-2 * np.abs(dr).max()
+    bound = 1e-4 * np.abs(dr) + 16 * EPS32 * cond[:, None]
+    bad = (np.abs(dg - dr) > bound) & big
+    assert not bad.any(), f"{what}: element-wise bar exceeded on {bad.sum()} of {big.sum()} entries"
+
+
+def pbf_pair(p, pos, vel):
+    g = rxPBDSPH(p)
+    g.Set(pos, vel)
+    r = oracle.RefSolver(p, pos.shape[0], "pbf")
+    r.set(pos, vel)
+    return g, r
+
+
+def steps_vs_reference(p, pos, vel, nsteps, what):
+    g, r = pbf_pair(p, pos, vel)
+    for k in range(nsteps):
+        x0 = g.GetArrayVBO(abi.RX_POSITION)
+        g.Update(PBF_DT)
+        it, eta = r.update(PBF_DT)
+        assert g.last_stats.iterations == 4 and it == 4
+        assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-4 * eta, (g.last_stats.density_error_two_sided, eta)
+        assert_step_equal(g, r, x0, f"{what} step {k + 1}")
+    g.close()
+
+
+@pytest.fixture(scope="module")
+def c2_rolled():
+    """The 64^3 dam break as configured (4 iterations, XSPH, vorticity) 100
+    steps into its collapse, stepped by the GPU path: an identical start for
+    both sides of the comparisons below."""
+    sc = scenes.pbf_dam_break(64)
+    p = abi.FsphParams.from_buffer_copy(sc.params)
+    p.eta, p.min_iter, p.max_iter = 0.0, 4, 4
+    g = rxPBDSPH(p)
+    g.Set(sc.pos, sc.vel)
+    for _ in range(100):
+        g.Update(sc.dt, stats=False)
+    x, v = g.GetArrayVBO(abi.RX_POSITION), g.GetArrayVBO(abi.RX_VELOCITY)
+    g.close()
+    assert np.abs(v[:, :3]).max() > 0.5  # the collapse is under way
+    return sc, x, v
+
+
+def test_c2_initial_steps_match_reference(gpu, ref_available):
+    sc = scenes.pbf_dam_break(64)
+    assert sc.n == 262144
+    steps_vs_reference(reference_setup(sc.params), sc.pos, sc.vel, 3, "262k initial")
+
+
+def test_c2_collapsing_steps_match_reference(gpu, ref_available, c2_rolled):
+    sc, x, v = c2_rolled
+    steps_vs_reference(reference_setup(sc.params), x, v, 2, "262k after 100 steps")
+
+
+def test_c2_passes_match_reference(gpu, ref_available, c2_rolled):
+    """lambda and delta-p passes alone on the collapsing 262k state."""
+    sc, x, _ = c2_rolled
+    p = reference_setup(sc.params)
+    r = oracle.RefSolver(p, sc.n, "pbf")
+    dr, lr = r.lambda_pass(x, PBF_DT)
+    dpr = r.correction_pass(x, lr, PBF_DT)
+    g = rxPBDSPH(p)
+    dg, lg = g.EvalScalingFactor(x)
+    dpg = g.EvalPositionCorrection(x, lr, PBF_DT)
+    g.close()
+    assert_close(dg, dr, "density", etol=1e-5, floor=0.0)
+    assert_lambda_close(lg, lr, dg, dr, float(np.float32(p.rest_dens)), "lambda")
+    off, idx, _ = r.neighbors(x)
+    assert_dp_close(dpg[:, :3], dpr[:, :3], dp_condition(x, lr, p, off, idx, PBF_DT), "delta p")
+
+
+@pytest.fixture(scope="module")
+def bench_rolled():
+    """The 1,048,576-particle double dam break of the benchmark (unilateral
+    constraint, iterate to 0.1 %, XSPH, vorticity, list skin 0.1 h) after its
+    100-step pre-roll on the GPU path."""
+    sc = scenes.pbf_double_dam_break()
+    p = abi.FsphParams.from_buffer_copy(sc.params)
+    p.clamp_constraint, p.max_iter, p.cell_skin = 1, 400, 0.1
+    g = rxPBDSPH(p)
+    g.Set(sc.pos, sc.vel)
+    for _ in range(100):
+        g.Update(sc.dt, stats=False)
+    x, v = g.GetArrayVBO(abi.RX_POSITION), g.GetArrayVBO(abi.RX_VELOCITY)
+    g.close()
+    return sc, x, v
+
+
+def test_bench_state_neighbour_sets_bit_exact(gpu, ref_available, bench_rolled):
+    sc, x, _ = bench_rolled
+    assert sc.n == 1048576
+    g = rxPBDSPH(sc.params)
+    g.Set(x)
+    off, idx = g.GetNeights()
+    g.close()
+    r = oracle.RefSolver(reference_setup(sc.params), sc.n, "pbf")
+    off_r, idx_r, _ = r.neighbors(x)
+    assert_sets_equal(off, idx, off_r, idx_r)
+    assert np.diff(off).min() >= 1 and np.diff(off).max() > 40
+
+
+def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
+    """One reference step from the pre-rolled 1M state against the GPU step
+    at the benchmark's list skin (0.1 h) and at 0.005 h, where the lists
+    go stale within the loop and the in-loop rebuild runs."""
+    sc, x, v = bench_rolled
+    base = reference_setup(sc.params)
+    r = oracle.RefSolver(base, sc.n, "pbf")
+    r.set(x, v)
+    it, eta = r.update(PBF_DT)
+    assert it == 4
+    for skin, rebuilds in ((0.1, False), (0.005, True)):
+        p = abi.FsphParams.from_buffer_copy(base)
+        p.cell_skin = skin
+        g = rxPBDSPH(p)
+        g.Set(x, v)
+        g.Update(PBF_DT)
+        assert g.last_stats.iterations == 4
+        if rebuilds:
+            assert g.last_stats.grid_builds > 1, g.last_stats.grid_builds
+        assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-4 * eta
+        assert_step_equal(g, r, x, f"1M, skin {skin}")
+        g.close()
+
+
+def test_c1_wcsph_steps_match_reference(gpu, ref_available):
+    sc = scenes.wcsph_dam_break(32)
+    assert sc.n == 32768
+    p = sc.params
+    g = rxSPH(p)
+    g.Set(sc.pos, sc.vel)
+    r = oracle.RefSolver(p, sc.n, "sph")
+    r.set(sc.pos, sc.vel)
+    for k in range(10):
+        x0 = g.GetArrayVBO(abi.RX_POSITION)[:, :3]
+        g.Update(sc.dt)
+        r.update(sc.dt)
+        xg, xr = g.GetArrayVBO(abi.RX_POSITION)[:, :3], r.get("pos")[:, :3]
+        assert_close(xg - x0, xr.astype(np.float64) - x0, f"WCSPH step {k + 1}: position change",
+                     atol=ulp32(xr) + ulp32(x0))
+        assert_close(g.GetArrayVBO(abi.RX_DENSITY), r.get("dens"), f"WCSPH step {k + 1}: density", etol=1e-5,
+                     floor=0.0)
+        # accelerations are sums of cancelling pressure terms: norm-wise bar
+        assert_close(g.GetArrayVBO(abi.RX_FORCE)[:, :3], r.get("force")[:, :3], f"WCSPH step {k + 1}: acceleration",
+                     etol=np.inf)
+    g.close()

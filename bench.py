@@ -185,17 +185,32 @@ def cpu_sample(pos, vel, params, iters: int, steps: int = 1):
     return dt, kind
 
 
+def cpu_sample_state(preroll: int = PREROLL, threads: int = 0):
+    """The CPU legs' sample: the REF_BLOCK double dam break with the GPU arms'
+    constants (unilateral constraint, iterate to 0.1 %, XSPH, vorticity)
+    after `preroll` steps, stepped by the FP32 oracle on the host cores.  The
+    cpu_baseline leg and the reference arm both time the reference's step on
+    this one state.  Returns (scene, positions, velocities)."""
+    import oracle
+    sc = make_scene(REF_BLOCK)
+    o = oracle.Oracle(sc.params, sc.n, "float", threads=threads or host_cores())
+    o.set(sc.pos, sc.vel)
+    for _ in range(preroll):
+        o.pbf_step(sc.dt)
+    return sc, o.get("pos"), o.get("vel")
+
+
 def _reference_worker(job):
     """One host core: warm-up + timed steps of the reference CPU Update on
-    its own copy of the sample scene; returns (seconds per timed step, kind)."""
-    warmup, steps = job
+    its own copy of the sample state; returns (seconds per timed step, kind)."""
+    warmup, steps, pos, vel, iters = job
     sc = make_scene(REF_BLOCK)
     kind = "reference"
     for _ in range(warmup):
-        cpu_sample(sc.pos, sc.vel, sc.params, REF_ITERS)
+        cpu_sample(pos, vel, sc.params, iters)
     times = []
     for _ in range(steps):
-        t, kind = cpu_sample(sc.pos, sc.vel, sc.params, REF_ITERS)
+        t, kind = cpu_sample(pos, vel, sc.params, iters)
         times.append(t)
     return times, kind
 
@@ -216,15 +231,18 @@ def reference_arm(args):
     if rank != 0:
         return 0
     cores = host_cores()
-    n = make_scene(REF_BLOCK).n
+    sc, xs, vs = cpu_sample_state(args.preroll)
+    n = sc.n
     with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(_reference_worker, [(max(args.warmup, 0), args.steps)] * cores)
+        res = pool.map(_reference_worker, [(max(args.warmup, 0), args.steps, xs, vs, REF_ITERS)] * cores)
     kind = res[0][1]
     tot = max(sum(t) for t, _ in res)
     value = cores * n * args.steps / tot
     sample = (f"one PBF step of the {n}-particle double dam break (blocks {REF_BLOCK[0]}x{REF_BLOCK[1]}x"
-              f"{REF_BLOCK[2]}, initial state) per timed step and process, {REF_ITERS} fixed constraint "
-              f"iterations (the plain GPU method's mean on the 1M window), {cores} processes, one per host core")
+              f"{REF_BLOCK[2]}) after a {args.preroll}-step pre-roll (FP32 oracle, the GPU arms' constants), "
+              f"the same state as the GPU line's cpu_baseline, per timed step and process; {REF_ITERS} fixed "
+              f"constraint iterations (the plain GPU method's mean on the 1M window); {cores} processes, one "
+              f"per host core")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
@@ -295,14 +313,46 @@ def run_leg(ctx, warm: bool, blob):
 
 
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_lambda_k_correction_pbf_double_dam_break_1M.md")
+# the sources of the constraint-pass kernels: a profile's figures hold for the
+# kernels built from exactly these files
+KERNEL_SOURCES = ("fltk_sph_ice_gb300/csrc/fsph_passes.cuh", "fltk_sph_ice_gb300/csrc/fsph_kernels.cu",
+                  "fltk_sph_ice_gb300/csrc/fsph_kernels.cuh", "fltk_sph_ice_gb300/csrc/fsph_internal.cuh")
+
+
+def kernel_sources_digest() -> str:
+    """sha256 (first 12 hex digits) of the constraint-pass kernel sources."""
+    import hashlib
+    h = hashlib.sha256()
+    for rel in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:12]
+
+
+def profile_digest():
+    """The kernel-sources digest the committed profile was captured at (its
+    'Kernel sources digest' line), or None."""
+    import re
+    if not os.path.isfile(TRAFFIC_PROFILE):
+        return None
+    with open(TRAFFIC_PROFILE) as f:
+        m = re.search(r"Kernel sources digest: `([0-9a-f]+)`", f.read())
+    return m.group(1) if m else None
+
+
+def profile_current() -> bool:
+    """The committed profile describes the kernels of this build."""
+    d = profile_digest()
+    return d is not None and d == kernel_sources_digest()
 
 
 def ncu_traffic(kname: str):
     """DRAM bytes (read + write) of one launch of kname at 1M particles, from
     the committed ncu summary's 'traffic per launch' row (its first two
-    columns are the current kernels); None if absent."""
+    columns are the current kernels); None if absent or captured from other
+    kernel sources than these."""
     import re
-    if not os.path.isfile(TRAFFIC_PROFILE):
+    if not profile_current():
         return None
     with open(TRAFFIC_PROFILE) as f:
         for line in f:
@@ -316,9 +366,10 @@ def ncu_traffic(kname: str):
 
 def ncu_warp_instructions(kname: str):
     """Warp instructions of one launch of kname at 1M particles, from the
-    committed ncu summary's 'warp instructions' row; None if absent."""
+    committed ncu summary's 'warp instructions' row; None if absent or
+    captured from other kernel sources than these."""
     import re
-    if not os.path.isfile(TRAFFIC_PROFILE):
+    if not profile_current():
         return None
     with open(TRAFFIC_PROFILE) as f:
         for line in f:
@@ -365,11 +416,66 @@ def roofline_of(L, abi, ps, n, mean_iters):
     peak, peak_kind = measured_peaks()
     achieved = kbytes / (kms / 1000.0) / 1e9
     traffic = ncu_traffic(kname)
+    digest = kernel_sources_digest()
+    src = (f"ncu, profiles/{os.path.basename(TRAFFIC_PROFILE)} (kernel sources {digest})" if profile_current()
+           else f"none: the committed profile was captured from other kernel sources than these ({digest})")
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
+            "traffic": traffic, "traffic_source": src, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
             "lambda_ms": t_lam.value, "correction_ms": t_cor.value, "grid_build_ms": t_grid.value,
             "list_build_ms": t_list.value, "issue": issue_bound(kname, kms),
             "passes_ms_per_step": mean_iters * (t_lam.value + t_cor.value)}
+
+
+# compulsory HBM bytes per particle-step of a PBF step with I constraint
+# iterations: B(I) = 396 + 60 I (prediction 48, one grid build 120, 60 per
+# iteration, finalize / XSPH / vorticity 228); the learned warm start adds its
+# network inputs (16 floats read, 64 B) and the predicted correction (16 B)
+def step_bytes(iters: float, warm_start: bool = False) -> float:
+    return 396.0 + 60.0 * iters + (80.0 if warm_start else 0.0)
+
+
+def step_roofline(value: float, iters: float, builds: float, warm_start: bool = False):
+    """The whole step against HBM: compulsory bytes per particle-step x
+    particle-steps/s.  In-loop grid rebuilds (builds - 1 per step) are the
+    implementation's choice and are not counted."""
+    peak, peak_kind = measured_peaks()
+    b = step_bytes(iters, warm_start)
+    achieved = value * b / 1e9
+    return {"bytes_per_particle_step": b, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind, "iterations": iters, "grid_builds": builds}
+
+
+FP64_REPLICA = (12, 12, 24)
+FP64_STEPS = 20
+FP64_ITERS = 10
+
+
+def fp64_error_headline(abi, rxPBDSPH):
+    """FP32 GPU against the FP64 oracle, step by step, on a 6,912-particle
+    replica of the headline scene (same constants: unilateral constraint,
+    XSPH, vorticity), both with a fixed iteration count so the two runs do
+    the same work: max |x_gpu - x_fp64| / h per step, and the density error
+    of the last step's lambda pass."""
+    import oracle
+    sc = make_scene(FP64_REPLICA)
+    p = sc.params
+    p.min_iter = p.max_iter = FP64_ITERS
+    p.eta = 0.0
+    ps = rxPBDSPH(p)
+    ps.Set(sc.pos, sc.vel)
+    o = oracle.Oracle(p, sc.n, precision="double", threads=host_cores())
+    o.set(sc.pos, sc.vel)
+    out = []
+    for _ in range(FP64_STEPS):
+        ps.Update(sc.dt)
+        o.pbf_step(sc.dt, fixed_iters=FP64_ITERS)
+        d = ps.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64) - o.get("pos")[:, :3]
+        out.append(float(np.abs(d).max() / p.h))
+    rho = ps.GetArrayVBO(abi.RX_DENSITY).astype(np.float64)
+    rho64 = o.get("dens").astype(np.float64)
+    ps.close()
+    return {"replica_particles": sc.n, "iterations": FP64_ITERS, "max_abs_position_error_over_h": out,
+            "last_step_density_max_rel_error": float(np.abs(rho - rho64).max() / np.abs(rho64).max())}
 
 
 def e2e_leg(ctx, ps, sc):
@@ -435,20 +541,20 @@ def gpu_arm(args):
         ps2.close()
 
     cpu = None
+    fp64 = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        sm = make_scene(REF_BLOCK)
-        ps3 = rxPBDSPH(sm.params)
-        ps3.Set(sm.pos, sm.vel)
-        for _ in range(args.preroll):
-            ps3.Update(sm.dt, stats=False)
-        xs, vs = ps3.GetArrayVBO(abi.RX_POSITION), ps3.GetArrayVBO(abi.RX_VELOCITY)
-        ps3.close()
+        sm, xs, vs = cpu_sample_state(args.preroll)
         ci = max(1, int(round(plain["mean_iterations"] if plain else REF_ITERS)))
         secs, kind = cpu_sample(xs, vs, sm.params, ci)
         cpu = {"value": sm.n / secs, "unit": UNIT, "cores": 1, "kind": kind,
                "sample": (f"one PBF step of the {sm.n}-particle double dam break (blocks {REF_BLOCK[0]}x"
-                          f"{REF_BLOCK[1]}x{REF_BLOCK[2]}) after the same {args.preroll}-step pre-roll, {ci} fixed "
-                          f"constraint iterations (the plain GPU mean on the 1M window), 1 host thread")}
+                          f"{REF_BLOCK[1]}x{REF_BLOCK[2]}) after a {args.preroll}-step pre-roll (FP32 oracle, the "
+                          f"GPU arms' constants; the reference arm times the same state), {ci} fixed constraint "
+                          f"iterations (the plain GPU mean on the 1M window), 1 host thread"),
+               "gpu_warm_over_cpu": warm["value"] / (sm.n / secs)}
+        if plain:
+            cpu["gpu_plain_over_cpu"] = plain["value"] / (sm.n / secs)
+        fp64 = fp64_error_headline(abi, rxPBDSPH)
 
     # kernel launches of the timed warm-start steps, counted by the library from the step graph's
     # kernel nodes, the executed iterations and the grid rebuilds (eager mode does not count them:
@@ -463,11 +569,15 @@ def gpu_arm(args):
                "model": {"samples": meta.get("samples"), "rollouts": meta.get("rollouts"),
                          "output_damping": meta.get("output_damping")},
                "preroll_steps": args.preroll, "l2": "256 MiB flush between timed steps",
-               "parallelism": f"replicas x{world}"}
+               "parallelism": f"replicas x{world}", "fp64_error_per_step": fp64}
         if plain:
             cfg["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "mean_iterations", "max_error",
                                                   "grid_builds")}
             cfg["speedup_vs_plain"] = warm["value"] / plain["value"]
+            roofline["step_plain"] = step_roofline(plain["value"], plain["mean_iterations"],
+                                                   plain["grid_builds"])
+        roofline["step_warm"] = step_roofline(warm["value"], warm["mean_iterations"], warm["grid_builds"],
+                                              warm_start=True)
         line = {
             "metric": METRIC, "value": warm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": warm["ms_per_step"], "higher_is_better": True,
@@ -479,6 +589,154 @@ def gpu_arm(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+C2_METRIC = "PBF particle-steps/s, 262,144-particle dam break, 4 constraint iterations"
+C1_METRIC = "WCSPH particle-steps/s, 32,768-particle dam break"
+CONFIG_PREROLL = 100
+# compulsory HBM bytes per particle-step of a WCSPH step: one grid build 120,
+# density pass 24 (R x, W rho, W p), force pass 56 (R x, v, rho, p, W a),
+# integrate 80 (R x, v, a, W x, v)
+WCSPH_BYTES = 120.0 + 24.0 + 56.0 + 80.0
+
+
+def config_arm(args):
+    """The 262,144-particle PBF dam break (4 fixed iterations, XSPH,
+    vorticity) or the 32,768-particle WCSPH dam break, device-resident steps
+    after a pre-roll; e2e through the public API with host buffers; the
+    reference's CPU step on the same state (one host thread) as cpu_baseline."""
+    import torch
+    from fltk_sph_ice_gb300 import abi, build, rxPBDSPH, rxSPH, scenes
+
+    rank, world, local = rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    build.build()
+    L = abi.lib()
+    pbf = args.workload == "pbf_dam_break_262k"
+    if pbf:
+        sc = scenes.pbf_dam_break(64)
+        p = sc.params
+        p.eta, p.min_iter, p.max_iter = 0.0, 4, 4
+        cls, metric = rxPBDSPH, C2_METRIC
+    else:
+        sc = scenes.wcsph_dam_break(32)
+        p = sc.params
+        cls, metric = rxSPH, C1_METRIC
+    if args.eager:
+        p.use_graph = 0
+    stream = torch.cuda.Stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ps = cls(p)
+    ps.Set(sc.pos, sc.vel)
+
+    def step():
+        st = L.fsph_step(ps.handle, ctypes.c_float(sc.dt), sp, None)
+        if st != abi.OK:
+            raise abi.FsphError(st, L.fsph_last_error(ps.handle).decode())
+
+    for _ in range(CONFIG_PREROLL):
+        step()
+    torch.cuda.synchronize()
+    x0, v0 = ps.GetArrayVBO(abi.RX_POSITION), ps.GetArrayVBO(abi.RX_VELOCITY)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = abi.FsphStepStats()
+    kern, builds = 0, []
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            stream.synchronize()
+            L.fsph_last_stats(ps.handle, ctypes.byref(stats))
+            kern += stats.kernels
+            builds.append(stats.grid_builds)
+        torch.cuda.synchronize()
+    tot_s = sum(a.elapsed_time(c) for a, c in ev) / 1000.0
+    value, tot_s = replica_rate(sc.n, args.steps, tot_s, dist)
+    peak, peak_kind = measured_peaks()
+    if pbf:
+        roof = roofline_of(L, abi, ps, sc.n, 4.0)
+        roof["step"] = step_roofline(value, 4.0, float(np.mean(builds)))
+    else:
+        roof = sph_roofline(L, abi, ps, sc.n)
+        b = WCSPH_BYTES
+        roof["step"] = {"bytes_per_particle_step": b, "achieved": value * b / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": value * b / 1e9 / peak, "peak_kind": peak_kind}
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_leg({"torch": torch, "L": L, "abi": abi, "args": args, "dist": dist}, ps, sc)
+    ps.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle
+        nsteps = 1 if pbf else 5
+        kind = "reference"
+        try:
+            r = oracle.RefSolver(p, sc.n, "pbf" if pbf else "sph")
+        except RuntimeError:
+            kind = "port"
+            r = oracle.Oracle(p, sc.n, "float", threads=1)
+        r.set(x0, v0)
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            if kind == "reference":
+                r.update(float(sc.dt))
+            elif pbf:
+                r.pbf_step(sc.dt, fixed_iters=4)
+            else:
+                r.sph_step(sc.dt)
+        secs = (time.perf_counter() - t0) / nsteps
+        cpu = {"value": sc.n / secs, "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": (f"{nsteps} step(s) of the same {sc.n}-particle scene from the GPU's state after its "
+                          f"{CONFIG_PREROLL}-step pre-roll, 1 host thread"
+                          + (" (the reference's own loop fixed at 4 iterations; no XSPH / vorticity, which its "
+                             "CPU path lacks)" if pbf else "")),
+               "gpu_over_cpu": value / (sc.n / secs)}
+    if rank == 0:
+        line = {
+            "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1000.0 * tot_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": args.workload, "particles": sc.n, "dt": sc.dt, "preroll_steps": CONFIG_PREROLL,
+                       "iterations": 4 if pbf else None, "grid_builds_per_step": float(np.mean(builds)),
+                       "l2": "256 MiB flush between timed steps", "parallelism": f"replicas x{world}"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": kern or None,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def sph_roofline(L, abi, ps, n):
+    """The WCSPH density and force passes, each timed alone (20 launches,
+    CUDA events), against HBM with their compulsory bytes (24 and 56 B per
+    particle)."""
+    t_d, t_f = ctypes.c_float(0), ctypes.c_float(0)
+    L.fsph_time_pass(ps.handle, abi.PASS_SPH_DENSITY, 20, ctypes.byref(t_d))
+    L.fsph_time_pass(ps.handle, abi.PASS_SPH_FORCE, 20, ctypes.byref(t_f))
+    peak, peak_kind = measured_peaks()
+    if t_f.value >= t_d.value:
+        kname, kms, kb = "k_sph_force", t_f.value, 56.0 * n
+    else:
+        kname, kms, kb = "k_sph_density", t_d.value, 24.0 * n
+    achieved = kb / (kms / 1000.0) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
+            "density_ms": t_d.value, "force_ms": t_f.value}
 
 
 BATCH_METRIC = "PBF particle-steps/s, 256 batched scenes of 2k-66k particles, 4 constraint iterations"
@@ -730,9 +988,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="batched_256: skip the autotuner, default launch shape")
-    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "batched_256", "pbf_obstacle_drop_16M"],
-                    help="the headline 1M double dam break (default), the 256-scene batch, or the 16.8M "
-                         "obstacle drop with boundary particles")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    choices=[WORKLOAD, "batched_256", "pbf_obstacle_drop_16M", "pbf_dam_break_262k",
+                             "wcsph_dam_break_32k"],
+                    help="the headline 1M double dam break (default), the 256-scene batch, the 16.8M "
+                         "obstacle drop with boundary particles, the 262k PBF dam break (4 iterations) or "
+                         "the 32k WCSPH dam break")
     args = ap.parse_args()
     if args.model is None:
         from fltk_sph_ice_gb300 import warmstart
@@ -743,6 +1004,8 @@ def main():
         return batched_arm(args)
     if args.workload == "pbf_obstacle_drop_16M":
         return large_arm(args)
+    if args.workload in ("pbf_dam_break_262k", "wcsph_dam_break_32k"):
+        return config_arm(args)
     return gpu_arm(args)
 
 

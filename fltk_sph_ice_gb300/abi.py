@@ -147,7 +147,9 @@ EXPORTS = [
     "fsph_num_particles", "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats",
     "fsph_get_array", "fsph_device_ptr", "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda",
     "fsph_pbf_eval_correction", "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_time_pass",
-    "fsph_pbf_eval_lambda_noalloc",
+    "fsph_pbf_eval_lambda_noalloc", "fsph_neighbors_ex", "fsph_step_fields",
+    "fsph_set_box_obstacle", "fsph_set_sphere_obstacle", "fsph_move_sphere_obstacle", "fsph_get_sphere_obstacle_pos",
+    "fsph_clear_obstacles", "fsph_num_obstacles",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
     "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
     "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
@@ -157,7 +159,7 @@ EXPORTS = [
 ]
 
 # fsph_pass
-PASS_LAMBDA, PASS_CORRECTION, PASS_GRID, PASS_LIST = 0, 1, 2, 3
+PASS_LAMBDA, PASS_CORRECTION, PASS_GRID, PASS_LIST, PASS_SPH_DENSITY, PASS_SPH_FORCE = 0, 1, 2, 3, 4, 5
 
 _LIB = None
 
@@ -192,6 +194,15 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_sph_eval_forces.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
     L.fsph_pbf_eval_xsph_vorticity.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p,
                                                c_void_p]
+    L.fsph_neighbors_ex.argtypes = [c_void_p, c_void_p, c_int, c_float, c_int, c_void_p, c_void_p, c_void_p,
+                                    ctypes.c_longlong, P(ctypes.c_longlong)]
+    L.fsph_step_fields.argtypes = [c_void_p, c_float, c_void_p]
+    L.fsph_set_box_obstacle.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+    L.fsph_set_sphere_obstacle.argtypes = [c_void_p, c_void_p, ctypes.c_double, c_void_p, c_int]
+    L.fsph_move_sphere_obstacle.argtypes = [c_void_p, c_int, c_void_p]
+    L.fsph_get_sphere_obstacle_pos.argtypes = [c_void_p, c_int, c_void_p]
+    L.fsph_clear_obstacles.argtypes = [c_void_p]
+    L.fsph_num_obstacles.argtypes = [c_void_p]
     L.fsph_time_pass.argtypes = [c_void_p, c_int, c_int, P(c_float)]
     L.fsph_mlp_create.argtypes = [P(c_void_p)]
     L.fsph_mlp_destroy.argtypes = [c_void_p]
@@ -231,7 +242,10 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
                  "fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",
                  "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats", "fsph_get_array",
                  "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda", "fsph_pbf_eval_correction",
-                 "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_params_from_env"]:
+                 "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_params_from_env",
+                 "fsph_neighbors_ex", "fsph_step_fields", "fsph_set_box_obstacle", "fsph_set_sphere_obstacle",
+                 "fsph_move_sphere_obstacle", "fsph_get_sphere_obstacle_pos", "fsph_clear_obstacles",
+                 "fsph_num_obstacles"]:
         getattr(L, name).restype = c_int
     return L
 

@@ -94,6 +94,10 @@ struct fsph_ctx {
     unsigned int *b_id = nullptr, *b_key = nullptr, *b_rank = nullptr;
     unsigned int *b_count = nullptr, *b_cell = nullptr;
     unsigned char *b_near = nullptr;
+    /* analytic obstacles: boxes first, then spheres, as uploaded */
+    std::vector<Obstacle> boxes, spheres;
+    Obstacle *obs_dev = nullptr;
+    int nobs_dev = 0;
     bool last_step_graph = false;
     bool stats_pending = false;
     std::string err;
@@ -205,7 +209,7 @@ DevParams make_dev(const fsph_params &p, int n, float dt) {
     double skin_len = 0.5 * (cw - h) * 0.999;
     d.skin2 = (float)(skin_len * skin_len);
     d.rl2 = (float)(cw * cw);
-    d.use_lists = (p.solver == FSPH_SOLVER_PBF && !p.walk_cells) ? 1 : 0;
+    d.use_lists = p.walk_cells ? 0 : 1;
     d.compensated = p.compensated_density ? 1 : 0;
     d.dt = dt;
     d.inv_dt = dt != 0.0f ? 1.0f / dt : 0.0f;
@@ -272,7 +276,42 @@ void attach_boundary(const fsph_ctx *c, DevParams &p) {
 DevParams dev_for(const fsph_ctx *c, int n, float dt) {
     DevParams p = make_dev(c->P, n, dt);
     attach_boundary(c, p);
+    p.nobs = c->nobs_dev;
+    p.obs = c->obs_dev;
     return p;
+}
+
+/* Rotation of a box obstacle from Euler angles in degrees (pitch, yaw,
+ * roll), rows world -> local, as EulerToMatrix (rx_sph_commons.h:185-210),
+ * and its inverse (the transpose). */
+void box_rotation(const double ang[3], Obstacle &o) {
+    const double d2r = kPi / 180.0;
+    const double cp = std::cos(ang[0] * d2r), sp = std::sin(ang[0] * d2r);
+    const double cy = std::cos(ang[1] * d2r), sy = std::sin(ang[1] * d2r);
+    const double cr = std::cos(ang[2] * d2r), sr = std::sin(ang[2] * d2r);
+    const double cc = cy * cr, cs = cy * sr, sc = sy * cr, ss = sy * sr;
+    const double m[3][3] = {{cc + sp * ss, cs - sp * sc, -sy * cp}, {-cp * sr, cp * cr, -sp},
+                            {sc - sp * cs, ss + sp * cc, cy * cp}};
+    for (int r = 0; r < 3; ++r) {
+        o.rot[r] = make_float4((float)m[r][0], (float)m[r][1], (float)m[r][2], 0.0f);
+        o.inv[r] = make_float4((float)m[0][r], (float)m[1][r], (float)m[2][r], 0.0f);
+    }
+}
+
+/* the obstacle table on the device (boxes, then spheres) */
+int upload_obstacles(fsph_ctx *c) {
+    std::vector<Obstacle> all(c->boxes);
+    all.insert(all.end(), c->spheres.begin(), c->spheres.end());
+    if (!c->obs_dev) FSPH_CUDA(c, cudaMalloc((void **)&c->obs_dev, kMaxObstacles * sizeof(Obstacle)));
+    if (!all.empty())
+        FSPH_CUDA(c, cudaMemcpyAsync(c->obs_dev, all.data(), all.size() * sizeof(Obstacle), cudaMemcpyHostToDevice,
+                                     c->stream));
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    if ((int)all.size() != c->nobs_dev) { /* the count is a launch constant of the captured step */
+        c->nobs_dev = (int)all.size();
+        c->graph_valid = false;
+    }
+    return FSPH_OK;
 }
 
 void drop_graph(fsph_ctx *c) {
@@ -595,10 +634,29 @@ int sph_step(fsph_ctx *c, const DevParams &p) {
     g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
     g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
     launch_gather(p.n, c->perm, g, c->ctl, s);
-    launch_sph_density(p, c->cell_start, c->set[1].pos, c->dens, c->pres, s);
-    launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->acc, s);
+    launch_sph_density(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->nl, s);
+    launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->acc, c->nl, s);
     launch_sph_integrate(p, c->set[1].pos, c->set[1].vel, c->acc, c->set[1].id, c->set[1].attr, c->set[0].pos,
                          c->set[0].vel, c->set[0].id, c->set[0].attr, s);
+    return FSPH_OK;
+}
+
+/* Capture one WCSPH step (grid build, density + lists, forces, integration)
+ * into a graph: the step is launch-bound at the configured 32k particles. */
+int build_sph_graph(fsph_ctx *c, const DevParams &p) {
+    drop_graph(c);
+    cudaGraph_t g;
+    FSPH_CUDA(c, cudaGraphCreate(&g, 0));
+    c->graph = g;
+    FSPH_CUDA(c, cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    sph_step(c, p);
+    FSPH_CUDA(c, cudaStreamEndCapture(c->stream, &g));
+    c->k_top = kernel_nodes(g);
+    c->k_iter = c->k_rebuild = 0;
+    FSPH_CUDA(c, cudaGraphInstantiate(&c->gexec, g, 0));
+    c->graph_valid = true;
+    c->graph_dt = p.dt;
+    c->graph_n = p.n;
     return FSPH_OK;
 }
 
@@ -819,6 +877,7 @@ int fsph_destroy(fsph_ctx *c) {
     if (c->flag_host) cudaFreeHost(c->flag_host);
     cudaFree(c->warm_valid);
     cudaFree(c->mlp_dev);
+    cudaFree(c->obs_dev);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->s2) cudaStreamDestroy(c->s2);
     if (c->s3) cudaStreamDestroy(c->s3);
@@ -953,9 +1012,14 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
     c->dp = p;
     c->home_identity = false; /* the step leaves the home set in cell order */
     c->res_in_res_id = false;
-    c->last_step_graph = c->P.solver == FSPH_SOLVER_PBF && c->P.use_graph;
+    c->last_step_graph = c->P.use_graph != 0;
     if (c->P.solver == FSPH_SOLVER_WCSPH) {
-        FSPH_TRY(sph_step(c, p));
+        if (c->P.use_graph) {
+            if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n) FSPH_TRY(build_sph_graph(c, p));
+            FSPH_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+        } else {
+            FSPH_TRY(sph_step(c, p));
+        }
     } else if (c->P.use_graph) {
         if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n) FSPH_TRY(build_pbf_graph(c, p));
         FSPH_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
@@ -1083,48 +1147,127 @@ const void *fsph_device_ptr(fsph_ctx *c, int type) {
     return nullptr;
 }
 
-int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long long *total) {
+int fsph_neighbors_ex(fsph_ctx *c, const float *pos4, int n, float radius, int where, int *offsets, int *indices,
+                      float *dist2, long long cap, long long *total) {
     if (!c || !offsets || !total) return FSPH_INVALID_ARG;
-    int n = c->n;
     *total = 0;
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    const bool given = pos4 != nullptr;
+    if (!given) n = c->n;
+    if (n < 0 || n > c->cap) return fail(c, FSPH_INVALID_ARG, "n outside [0, max_particles]");
     if (n == 0) { offsets[0] = 0; return FSPH_OK; }
+    double cw, org[3];
+    int g3[3];
+    grid_geometry(c->P, cw, org, g3);
+    const float h = radius > 0.0f ? radius : c->P.h;
+    if (!std::isfinite(h) || (double)h > cw)
+        return fail(c, FSPH_UNSUPPORTED, "radius beyond the grid's cell width h (1 + cell_skin)");
     DevParams p = dev_for(c, n, 1.0f);
+    p.h = h;
+    p.h2 = h * h;
     cudaStream_t s = c->stream;
-    FSPH_TRY(build_on(c, p, c->set[0].pos));
-    unsigned int *cnt = c->rank;
+    const float4 *x = c->set[0].pos;
+    const unsigned int *ids = c->set[0].id;
+    if (given) {
+        /* the given positions stand in for the particles: scratch copy, ids 0..n-1 */
+        FSPH_CUDA(c, cudaMemcpyAsync(c->tmp4, pos4, (size_t)n * 16,
+                                     where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        FSPH_CUDA(c, cudaMemsetAsync(c->flag, 0, sizeof(unsigned int), s));
+        launch_check_finite(n, c->tmp4, nullptr, c->flag, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->flag_host, c->flag, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        if (*c->flag_host) return fail(c, FSPH_NAN_DETECTED, "non-finite position");
+        launch_iota(n, c->set[1].attr, s);
+        x = c->tmp4;
+        ids = c->set[1].attr;
+    }
+    enqueue_sort(c, p, x, s);
+    Gather g{};
+    g.n4 = 1; g.n1 = 1;
+    g.src4[0] = x; g.dst4[0] = c->set[1].pos;
+    g.src1[0] = ids; g.dst1[0] = c->set[1].id;
+    launch_gather(n, c->perm, g, nullptr, s);
+    unsigned int *cnt = c->rank; /* free once the scatter has run */
     launch_nb_count(p, c->cell_start, c->set[1].pos, cnt, s);
     std::vector<unsigned int> hc((size_t)n), ho((size_t)n + 1);
     FSPH_CUDA(c, cudaMemcpyAsync(hc.data(), cnt, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
     FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(check_launch(c));
     unsigned long long t = 0;
     for (int i = 0; i < n; ++i) { ho[i] = (unsigned int)t; t += hc[i]; }
     if (t > 0xffffffffull) return fail(c, FSPH_INVALID_ARG, "more than 2^32 neighbour entries");
     ho[n] = (unsigned int)t;
-    unsigned int *doff = c->key;
-    int *dout = nullptr;
-    FSPH_CUDA(c, cudaMemcpyAsync(doff, ho.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
-    FSPH_CUDA(c, cudaMallocAsync((void **)&dout, std::max<size_t>(t, 1) * 4, s));
-    launch_nb_fill(p, c->cell_start, c->set[1].pos, c->set[1].id, doff, dout, s);
-    std::vector<int> hidx((size_t)t), hid((size_t)n);
-    FSPH_CUDA(c, cudaMemcpyAsync(hidx.data(), dout, (size_t)t * 4, cudaMemcpyDeviceToHost, s));
+    /* rows in the caller's order, ascending indices within a row */
+    std::vector<int> hid((size_t)n);
     FSPH_CUDA(c, cudaMemcpyAsync(hid.data(), c->set[1].id, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
-    FSPH_CUDA(c, cudaFreeAsync(dout, s));
     FSPH_CUDA(c, cudaStreamSynchronize(s));
-    FSPH_TRY(check_launch(c));
-    /* rows to particle order, ascending indices within a row */
     std::vector<unsigned int> cntp((size_t)n + 1, 0);
     for (int d = 0; d < n; ++d) cntp[(size_t)hid[d] + 1] = hc[d];
     for (int i = 0; i < n; ++i) cntp[i + 1] += cntp[i];
     for (int i = 0; i <= n; ++i) offsets[i] = (int)cntp[i];
     *total = (long long)t;
-    if (indices && cap >= (long long)t) {
-        for (int d = 0; d < n; ++d) {
-            int pi = hid[d];
-            int *row = indices + cntp[pi];
-            std::copy(hidx.begin() + ho[d], hidx.begin() + ho[d] + hc[d], row);
-            std::sort(row, row + hc[d]);
+    if (!indices || cap < (long long)t) return FSPH_OK; /* sizes only */
+    unsigned int *doff = c->key;
+    int *dout = nullptr;
+    float *dd2 = nullptr;
+    FSPH_CUDA(c, cudaMemcpyAsync(doff, ho.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaMallocAsync((void **)&dout, std::max<size_t>(t, 1) * 4, s));
+    if (dist2) FSPH_CUDA(c, cudaMallocAsync((void **)&dd2, std::max<size_t>(t, 1) * 4, s));
+    launch_nb_fill(p, c->cell_start, c->set[1].pos, c->set[1].id, doff, dout, dd2, s);
+    std::vector<int> hidx((size_t)t);
+    std::vector<float> hd2(dist2 ? (size_t)t : 0);
+    FSPH_CUDA(c, cudaMemcpyAsync(hidx.data(), dout, (size_t)t * 4, cudaMemcpyDeviceToHost, s));
+    if (dist2) FSPH_CUDA(c, cudaMemcpyAsync(hd2.data(), dd2, (size_t)t * 4, cudaMemcpyDeviceToHost, s));
+    FSPH_CUDA(c, cudaFreeAsync(dout, s));
+    if (dd2) FSPH_CUDA(c, cudaFreeAsync(dd2, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(check_launch(c));
+    std::vector<std::pair<int, float> > row;
+    for (int d = 0; d < n; ++d) {
+        const int pi = hid[d];
+        row.clear();
+        for (unsigned int k = ho[d]; k < ho[d] + hc[d]; ++k) row.emplace_back(hidx[k], dist2 ? hd2[k] : 0.0f);
+        std::sort(row.begin(), row.end());
+        for (size_t k = 0; k < row.size(); ++k) {
+            indices[cntp[pi] + k] = row[k].first;
+            if (dist2) dist2[cntp[pi] + k] = row[k].second;
         }
     }
+    return FSPH_OK;
+}
+
+int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long long *total) {
+    return fsph_neighbors_ex(c, nullptr, 0, 0.0f, FSPH_HOST, offsets, indices, nullptr, cap, total);
+}
+
+int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {
+    if (!c) return FSPH_INVALID_ARG;
+    if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
+    if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
+    cudaStream_t user = (cudaStream_t)stream;
+    if (user && user != c->stream) FSPH_CUDA(c, cudaStreamSynchronize(user));
+    DevParams p = dev_for(c, c->n, dt);
+    cudaStream_t s = c->stream;
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    /* results keep the sorted order of this evaluation (res_id); the
+     * particles themselves stay where they are */
+    enqueue_sort(c, p, c->set[0].pos, s);
+    Gather g{};
+    g.n4 = 2; g.n1 = 1;
+    g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+    g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+    g.src1[0] = c->set[0].id; g.dst1[0] = c->res_id;
+    launch_gather(p.n, c->perm, g, nullptr, s);
+    if (c->P.solver == FSPH_SOLVER_WCSPH) {
+        launch_sph_density(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->nl, s);
+        launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->acc, c->nl, s);
+    } else {
+        launch_pbf_density(p, c->cell_start, c->set[1].pos, c->dens, s);
+        launch_pbf_visc(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->acc, s);
+    }
+    FSPH_TRY(check_launch(c));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    c->res_in_res_id = true;
     return FSPH_OK;
 }
 
@@ -1202,12 +1345,103 @@ int fsph_get_boundary(fsph_ctx *c, int which, float *dst) {
 
 int fsph_num_boundary(const fsph_ctx *c) { return c ? c->nb : -1; }
 
+int fsph_set_box_obstacle(fsph_ctx *c, const double *cen, const double *ext, const double *ang,
+                          const double *vel, int flg) {
+    if (!c || !cen || !ext) return FSPH_INVALID_ARG;
+    (void)vel; /* stored by the reference too, and not used by its fluid step */
+    if (!flg) return FSPH_OK; /* a disabled obstacle is skipped (rx_pbdsph_kernel.cu:873) */
+    if ((int)c->boxes.size() >= kMaxBoxObstacles) return fail(c, FSPH_INVALID_ARG, "at most 10 box obstacles");
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(cen[a]) || !(ext[a] > 0.0) || !std::isfinite(ext[a]) || (ang && !std::isfinite(ang[a])))
+            return fail(c, FSPH_INVALID_ARG, "box obstacle: finite centre and angles, positive extents");
+    Obstacle o{};
+    o.cen = make_float4((float)cen[0], (float)cen[1], (float)cen[2], 0.0f);
+    o.ext = make_float4((float)ext[0], (float)ext[1], (float)ext[2], 0.0f);
+    const double zero[3] = {0.0, 0.0, 0.0};
+    box_rotation(ang ? ang : zero, o);
+    c->boxes.push_back(o);
+    return upload_obstacles(c);
+}
+
+int fsph_set_sphere_obstacle(fsph_ctx *c, const double *cen, double rad, const double *vel, int flg) {
+    if (!c || !cen) return FSPH_INVALID_ARG;
+    (void)vel;
+    if (!flg) return FSPH_OK;
+    if ((int)c->spheres.size() >= kMaxSphereObstacles) return fail(c, FSPH_INVALID_ARG, "at most 10 sphere obstacles");
+    if (!(rad > 0.0) || !std::isfinite(rad) || !std::isfinite(cen[0]) || !std::isfinite(cen[1]) ||
+        !std::isfinite(cen[2]))
+        return fail(c, FSPH_INVALID_ARG, "sphere obstacle: finite centre, positive radius");
+    Obstacle o{};
+    o.cen = make_float4((float)cen[0], (float)cen[1], (float)cen[2], (float)rad);
+    o.ext = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+    c->spheres.push_back(o);
+    return upload_obstacles(c);
+}
+
+int fsph_move_sphere_obstacle(fsph_ctx *c, int b, const double *disp) {
+    if (!c || !disp) return FSPH_INVALID_ARG;
+    if (b < 0 || b >= (int)c->spheres.size()) return fail(c, FSPH_INVALID_ARG, "no such sphere obstacle");
+    float4 &q = c->spheres[(size_t)b].cen;
+    q = make_float4((float)(q.x + disp[0]), (float)(q.y + disp[1]), (float)(q.z + disp[2]), q.w);
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream)); /* not under a step that reads the table */
+    return upload_obstacles(c);
+}
+
+int fsph_get_sphere_obstacle_pos(const fsph_ctx *c, int b, double *pos) {
+    if (!c || !pos || b < 0 || b >= (int)c->spheres.size()) return FSPH_INVALID_ARG;
+    const float4 q = c->spheres[(size_t)b].cen;
+    pos[0] = q.x; pos[1] = q.y; pos[2] = q.z;
+    return FSPH_OK;
+}
+
+int fsph_clear_obstacles(fsph_ctx *c) {
+    if (!c) return FSPH_INVALID_ARG;
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->boxes.clear();
+    c->spheres.clear();
+    return upload_obstacles(c);
+}
+
+int fsph_num_obstacles(const fsph_ctx *c) { return c ? (int)(c->boxes.size() + c->spheres.size()) : -1; }
+
 int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
     if (!c || !avg_ms || reps <= 0) return FSPH_INVALID_ARG;
     if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
-    if (c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "pass timing covers the PBF passes");
+    const bool sph_pass = pass == FSPH_PASS_SPH_DENSITY || pass == FSPH_PASS_SPH_FORCE;
+    if (sph_pass != (c->P.solver == FSPH_SOLVER_WCSPH))
+        return fail(c, FSPH_UNSUPPORTED, "this pass belongs to the other solver");
     DevParams p = dev_for(c, c->n, c->dp.dt > 0.0f ? c->dp.dt : 1e-3f);
     cudaStream_t s = c->stream;
+    if (sph_pass) {
+        /* the state of a WCSPH step before its passes: grid on x, sorted x, v */
+        enqueue_sort(c, p, c->set[0].pos, s);
+        Gather g{};
+        g.n4 = 2;
+        g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+        g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+        launch_gather(p.n, c->perm, g, nullptr, s);
+        launch_sph_density(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->nl, s);
+        cudaEvent_t e0, e1;
+        FSPH_CUDA(c, cudaEventCreate(&e0));
+        FSPH_CUDA(c, cudaEventCreate(&e1));
+        FSPH_CUDA(c, cudaEventRecord(e0, s));
+        for (int k = 0; k < reps; ++k) {
+            if (pass == FSPH_PASS_SPH_DENSITY)
+                launch_sph_density(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->nl, s);
+            else
+                launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->acc, c->nl, s);
+        }
+        FSPH_CUDA(c, cudaEventRecord(e1, s));
+        FSPH_CUDA(c, cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        FSPH_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        FSPH_TRY(check_launch(c));
+        *avg_ms = ms / (float)reps;
+        /* the home set keeps the particles; only scratch arrays were written */
+        return FSPH_OK;
+    }
     /* the state after a step: x* = x in the home set, already cell-ordered */
     FSPH_TRY(build_on(c, p, c->set[0].pos));
     FSPH_CUDA(c, cudaMemsetAsync(c->ctl, 0, sizeof(DevCtl), s));
@@ -1342,8 +1576,8 @@ int fsph_sph_eval_forces(fsph_ctx *c, const float *pos4, const float *vel4, int 
     g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
     g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
     launch_gather(n, c->perm, g, nullptr, s);
-    launch_sph_density(p, c->cell_start, c->set[1].pos, c->dens, c->pres, s);
-    launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->acc, s);
+    launch_sph_density(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->dens, c->pres, c->nl, s);
+    launch_sph_force(p, c->cell_start, c->set[1].pos, c->set[1].vel, c->acc, c->nl, s);
     FSPH_TRY(check_launch(c));
     FSPH_TRY(copy_out_scalar(c, c->dens, c->set[1].id, dens, n));
     FSPH_CUDA(c, cudaStreamSynchronize(s));

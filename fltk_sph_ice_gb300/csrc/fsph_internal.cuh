@@ -24,6 +24,17 @@
 
 namespace fsph {
 
+/* An analytic obstacle (the reference's box and sphere obstacles,
+ * rx_cu_common.cuh:135-136, at most 10 of each): 128 bytes. */
+constexpr int kMaxBoxObstacles = 10, kMaxSphereObstacles = 10;
+constexpr int kMaxObstacles = kMaxBoxObstacles + kMaxSphereObstacles;
+struct Obstacle {
+    float4 cen;              /* centre; w = sphere radius */
+    float4 ext;              /* box half extents; w = 0 box, 1 sphere */
+    float4 rot[3];           /* box: rows of the world -> local rotation */
+    float4 inv[3];           /* box: rows of its inverse */
+};
+
 /* Launch-time constants of one solver; passed by value to every kernel. */
 struct DevParams {
     int n;
@@ -52,6 +63,9 @@ struct DevParams {
     const float *blam;          /* lambda_b of the current lambda pass */
     const unsigned int *bcell;  /* boundary slots of cell c: [bcell[c], bcell[c + 1]) */
     const unsigned char *bnear; /* 1 when boundary particles lie in the 27 cells around c */
+    /* analytic obstacles (nobs = 0: none) */
+    int nobs;
+    const Obstacle *obs;
 };
 
 /* Neighbour lists: up to kListMax entries per particle, transposed (entry
@@ -152,6 +166,49 @@ __device__ inline float3 wall_project(float3 x, const DevParams &p) {
     x.y = fminf(fmaxf(x.y, p.wall_lo.y), p.wall_hi.y);
     x.z = fminf(fmaxf(x.z, p.wall_lo.z), p.wall_hi.z);
     return x;
+}
+
+/* Obstacle projection: a point inside an obstacle moves to its surface --
+ * a box (in its own rotated frame) through the nearest face, ties in x, y,
+ * z order; a sphere radially -- as collisionPointBox / collisionPointSphere
+ * (rx_cu_common.cu:748-831) with calCollisionSolidPB (rx_pbdsph_kernel.cu:
+ * 863-911).  The velocity is left alone, as the CPU path leaves it
+ * (rx_sph_pbd.cpp:1384; a PBF step recomputes it from the positions). */
+__device__ inline float3 rot3(const float4 *r, float3 v) {
+    return make_float3(r[0].x * v.x + r[0].y * v.y + r[0].z * v.z, r[1].x * v.x + r[1].y * v.y + r[1].z * v.z,
+                       r[2].x * v.x + r[2].y * v.y + r[2].z * v.z);
+}
+__device__ inline float3 obstacle_project(float3 x, const DevParams &p) {
+    for (int k = 0; k < p.nobs; ++k) {
+        const Obstacle &o = p.obs[k];
+        const float4 c4 = o.cen, e4 = o.ext;
+        const float3 c = make_float3(c4.x, c4.y, c4.z);
+        if (e4.w != 0.0f) { /* sphere */
+            const float3 l = make_float3(x.x - c.x, x.y - c.y, x.z - c.z);
+            const float ll = sqrtf(l.x * l.x + l.y * l.y + l.z * l.z);
+            if (ll < c4.w && ll > 0.0f) {
+                const float s = c4.w / ll;
+                x = make_float3(c.x + s * l.x, c.y + s * l.y, c.z + s * l.z);
+            }
+        } else { /* box */
+            float3 cp = rot3(o.rot, make_float3(x.x - c.x, x.y - c.y, x.z - c.z));
+            const float tx = fabsf(cp.x) - e4.x, ty = fabsf(cp.y) - e4.y, tz = fabsf(cp.z) - e4.z;
+            if (tx < 0.0f && ty < 0.0f && tz < 0.0f) {
+                const float ax = -tx, ay = -ty, az = -tz;
+                if (ax <= ay && ax <= az) cp.x = cp.x > 0.0f ? e4.x : -e4.x;
+                else if (ay <= ax && ay <= az) cp.y = cp.y > 0.0f ? e4.y : -e4.y;
+                else cp.z = cp.z > 0.0f ? e4.z : -e4.z;
+                const float3 w = rot3(o.inv, cp);
+                x = make_float3(w.x + c.x, w.y + c.y, w.z + c.z);
+            }
+        }
+    }
+    return x;
+}
+/* obstacles, then the box walls (the order of rx_sph_pbd.cpp:1380-1395) */
+__device__ inline float3 solid_project(float3 x, const DevParams &p) {
+    if (p.nobs) x = obstacle_project(x, p);
+    return wall_project(x, p);
 }
 
 /* Cell coordinates of a position, clamped to the interior cells [1, G-2] so

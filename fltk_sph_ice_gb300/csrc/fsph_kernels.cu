@@ -21,6 +21,8 @@
  *   k_xsph_vort        xsphVisocosity (rx_pbdsph_kernel.cu:1130-1162) + vorticity
  *   k_sph_*            rxSPH::calDensity / calForce / integrate (rx_sph_cpu.cpp:495-1077)
  */
+#include <algorithm>
+
 #include "fsph_kernels.cuh"
 #include "fsph_passes.cuh"
 
@@ -331,14 +333,25 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_lambda(DevParams
     __shared__ unsigned int s_rs[9 * kPassBlock];
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     float4 *pp = par ? ppos1 : ppos0;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float e1 = 0.f, e2 = 0.f, em = 0.f;
-    if (i < p.n) {
-        const float C =
-            lambda_body<1, KAHAN>(p, cell_start, pp, dens, ctl, list, cnt, cellb, s_rs + threadIdx.x, i, 0, true);
-        e1 = C > 0.0f ? C : 0.0f;
-        e2 = fabsf(C);
-        em = e2;
+#if FSPH_PERSIST
+    /* persistent warps: warp w takes the 32-slot chunks w, w + W, ... in a
+     * fixed order (the error sums stay deterministic) */
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * 32 < p.n; c += nw) {
+        const int i = c * 32 + lane;
+#else
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+        if (i < p.n) {
+            const float C = lambda_body<1, KAHAN>(p, cell_start, pp, dens, ctl, list, cnt, cellb, s_rs + threadIdx.x,
+                                                  i, 0, true);
+            e1 += C > 0.0f ? C : 0.0f;
+            e2 += fabsf(C);
+            em = fmaxf(em, fabsf(C));
+        }
     }
     lambda_tail(p, ctl, part, e1, e2, em, hwhile, use_graph);
 }
@@ -360,11 +373,20 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_correction(DevPa
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     const float4 *__restrict__ src = par ? ppos1 : ppos0;
     float4 *__restrict__ dst = par ? ppos0 : ppos1;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float disp2 = 0.f;
-    if (i < p.n)
-        disp2 = correction_body<1>(p, cell_start, src, dst, xb, ctl, dp_out, list, cnt, cellb, s_rs + threadIdx.x, i,
-                                   0, true);
+#if FSPH_PERSIST
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * 32 < p.n; c += nw) {
+        const int i = c * 32 + lane;
+#else
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+#endif
+        if (i < p.n)
+            disp2 = fmaxf(disp2, correction_body<1>(p, cell_start, src, dst, xb, ctl, dp_out, list, cnt, cellb,
+                                                    s_rs + threadIdx.x, i, 0, true));
+    }
     correction_tail(p, ctl, part, disp2, par, hif, hif2, use_graph);
 }
 
@@ -534,65 +556,110 @@ void launch_boundary_lambda(const DevParams &p, const unsigned int *cell_start, 
 /* WCSPH                                                                    */
 /* ======================================================================== */
 
-__global__ void k_sph_density(DevParams p, const unsigned int *__restrict__ cell_start,
-                              const float4 *__restrict__ pos, float *__restrict__ dens, float *__restrict__ pres) {
+/* rho_i = m aw sum_j (h^2 - r^2)^3 (r < h, self included) and p_i = k (rho_i -
+ * rho0) (rxSPH::calDensity, rx_sph_cpu.cpp:495-552, 569), in the same walk
+ * over the 27 cells as the neighbour list of the following force pass
+ * (every slot within the list radius, here the cell width h (1 + 1e-3));
+ * the force pass's per-neighbour factors ride in the .w words of the sorted
+ * copies: pos.w = p / rho^2, vel.w = 1 / rho.  Only .w words are written, so
+ * the x, y, z the other threads read stay as they are. */
+__global__ void __launch_bounds__(kBlock) k_sph_density(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                        float4 *pos, float4 *vel, float *__restrict__ dens,
+                                                        float *__restrict__ pres, ListEntry *__restrict__ list,
+                                                        unsigned char *__restrict__ cnt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    float3 xi = f3(pos[i]);
-    int3 c = cell_of(xi, p);
+    const float3 xi = f3(pos[i]);
+    const int3 c = cell_of(xi, p);
     float acc = 0.0f;
+    int k = 0;
+    bool ovf = false;
+    ListEntry last = (ListEntry)i;
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy) {
             unsigned int s, e;
             row_range(cell_start, c, dy, dz, p, s, e);
-            for (unsigned int j = s; j < e; ++j) {
-                float3 d = xi - f3(__ldg(pos + j));
-                float r2 = dot3(d, d);
-                if (r2 < p.h2) {
-                    float q = p.h2 - r2;
-                    acc += q * q * q;
+            /* four candidates' loads in flight before their tests */
+            for (unsigned int j0 = s; j0 < e; j0 += 4) {
+                float4 xc[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xc[u] = __ldg(pos + min(j0 + u, e - 1));
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (j0 + u >= e) break;
+                    const float3 d = xi - f3(xc[u]);
+                    const float r2 = dot3(d, d);
+                    if (r2 < p.h2) {
+                        const float q = p.h2 - r2;
+                        acc += q * q * q;
+                    }
+                    if (list && r2 < p.rl2) {
+                        last = (ListEntry)(j0 + u);
+                        if (k < kListMax) list[list_at(k, i, p.n)] = last;
+                        ++k;
+                    }
                 }
             }
         }
-    float rho = p.mass * p.aw * acc;
+    if (list) {
+        ovf = k > kListMax;
+#ifdef FSPH_LIST_GROUPED
+        if (!ovf) /* pad the last group (k >= 1: the slot itself is always listed) */
+            for (int t = k; (t & 3) != 0; ++t) list[list_at(t, i, p.n)] = last;
+#endif
+        cnt[i] = ovf ? kListOverflow : (unsigned char)k;
+    }
+    const float rho = p.mass * p.aw * acc;
+    const float prs = p.gas_k * (rho - p.rest_dens);
     dens[i] = rho;
-    pres[i] = p.gas_k * (rho - p.rest_dens);
+    pres[i] = prs;
+    reinterpret_cast<float *>(pos + i)[3] = prs / (rho * rho);
+    reinterpret_cast<float *>(vel + i)[3] = 1.0f / rho;
 }
 
-__global__ void k_sph_force(DevParams p, const unsigned int *__restrict__ cell_start, const float4 *__restrict__ pos,
-                            const float4 *__restrict__ vel, const float *__restrict__ dens,
-                            const float *__restrict__ pres, float4 *__restrict__ acc) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    float3 xi = f3(pos[i]), vi = f3(vel[i]);
-    float rhoi = dens[i];
-    float prsi = pres[i] / (rhoi * rhoi);
-    int3 c = cell_of(xi, p);
+/* a_i = -sum_j m (p_i/rho_i^2 + p_j/rho_j^2) grad W_ij + mu sum_j m (v_j - v_i)
+ * lapW_ij / rho_j + g over 0 < r_ij < h (rxSPH::calForce, rx_sph_cpu.cpp:558-656),
+ * from the list of the density pass (or the 27 cells when lists are off),
+ * with LPP lanes per particle (small scenes then still fill the GPU).
+ * Branch-free pair terms: t = max(h - r, 0) is 0 at and beyond h, and at
+ * r = 0 too (h - 0 * rsqrt(0) is NaN, which fmaxf maps to 0), so the self
+ * pair and coincident particles add nothing, as the reference skips them. */
+struct PosVel {
+    float4 x, v;
+};
+template <int LPP>
+__global__ void __launch_bounds__(kBlock) k_sph_force(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                      const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                                                      float4 *__restrict__ acc, const ListEntry *__restrict__ list,
+                                                      const unsigned char *__restrict__ cnt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sub = t % LPP;
+    const bool valid = t / LPP < p.n;
+    const int i = valid ? t / LPP : p.n - 1; /* padding lanes run a real slot and write nothing */
+    const float4 xi4 = pos[i], vi4 = vel[i];
+    const float3 xi = f3(xi4), vi = f3(vi4);
+    const float prsi = xi4.w;
     float3 fp = make_float3(0.f, 0.f, 0.f), fv = make_float3(0.f, 0.f, 0.f);
-    for (int dz = -1; dz <= 1; ++dz)
-        for (int dy = -1; dy <= 1; ++dy) {
-            unsigned int s, e;
-            row_range(cell_start, c, dy, dz, p, s, e);
-            for (unsigned int j = s; j < e; ++j) {
-                if (j == (unsigned int)i) continue;
-                float3 d = xi - f3(__ldg(pos + j));
-                float r2 = dot3(d, d);
-                if (r2 < p.h2 && r2 > 0.0f) {
-                    float r = sqrtf(r2);
-                    float t = p.h - r;
-                    float rhoj = __ldg(dens + j);
-                    float prsj = __ldg(pres + j) / (rhoj * rhoj);
-                    float g = p.ag * t * t / r;
-                    fp = fp + ((prsi + prsj) * g) * d;
-                    float lw = p.al * t / rhoj;
-                    fv = fv + lw * (f3(__ldg(vel + j)) - vi);
-                }
-            }
-        }
-    float3 a = (-p.mass) * fp + (p.viscosity * p.mass) * fv + p.gravity;
+    for_each_candidate<LPP>(
+        p, cell_start, list, cnt, nullptr, i, xi, nullptr, sub,
+        [&](unsigned int j) { return PosVel{__ldg(pos + j), __ldg(vel + j)}; },
+        [&](unsigned int, const PosVel &b) {
+            const float3 d = xi - f3(b.x);
+            const float r2 = dot3(d, d);
+            const float inv_r = rsqrtf(r2);
+            const float tt = fmaxf(fmaf(-r2, inv_r, p.h), 0.0f);
+            const float g = p.ag * tt * tt * fminf(inv_r, 1e30f);
+            fp = fp + ((prsi + b.x.w) * g) * d;
+            fv = fv + (p.al * tt * b.v.w) * (f3(b.v) - vi);
+        });
+    if (LPP > 1) {
+        fp.x = group_sum<LPP>(fp.x); fp.y = group_sum<LPP>(fp.y); fp.z = group_sum<LPP>(fp.z);
+        fv.x = group_sum<LPP>(fv.x); fv.y = group_sum<LPP>(fv.y); fv.z = group_sum<LPP>(fv.z);
+    }
+    if (!valid || sub != 0) return;
+    const float3 a = (-p.mass) * fp + (p.viscosity * p.mass) * fv + p.gravity;
     acc[i] = make_float4(a.x, a.y, a.z, 0.0f);
 }
-
 __global__ void k_sph_integrate(DevParams p, const float4 *__restrict__ pos_b, const float4 *__restrict__ vel_b,
                                 const float4 *__restrict__ acc, const unsigned int *__restrict__ id_b,
                                 const unsigned int *__restrict__ attr_b, float4 *__restrict__ pos_a,
@@ -602,7 +669,7 @@ __global__ void k_sph_integrate(DevParams p, const float4 *__restrict__ pos_b, c
     if (i >= p.n) return;
     float3 v = f3(vel_b[i]) + p.dt * f3(acc[i]);
     float3 x = f3(pos_b[i]) + p.dt * v;
-    x = wall_project(x, p);
+    x = solid_project(x, p);
     pos_a[i] = make_float4(x.x, x.y, x.z, 0.0f);
     vel_a[i] = make_float4(v.x, v.y, v.z, 0.0f);
     id_a[i] = id_b[i];
@@ -643,9 +710,17 @@ __global__ void k_nb_count(DevParams p, const unsigned int *__restrict__ cell_st
     cnt[i] = k;
 }
 
+/* squared distance as the reference's rxNeigh::Dist2: the difference of the
+ * float coordinates and its squares summed in double, x + y + z in that
+ * order with no fused multiply-add, rounded to float (rx_nnsearch.h:499-507) */
+__device__ inline float ref_dist2(float3 xi, float3 xj) {
+    double ex = (double)xi.x - (double)xj.x, ey = (double)xi.y - (double)xj.y, ez = (double)xi.z - (double)xj.z;
+    return __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)));
+}
+
 __global__ void k_nb_fill(DevParams p, const unsigned int *__restrict__ cell_start, const float4 *__restrict__ pos,
                           const unsigned int *__restrict__ id, const unsigned int *__restrict__ offsets,
-                          int *__restrict__ out) {
+                          int *__restrict__ out, float *__restrict__ d2out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     float3 xi = f3(pos[i]);
@@ -655,8 +730,13 @@ __global__ void k_nb_fill(DevParams p, const unsigned int *__restrict__ cell_sta
         for (int dy = -1; dy <= 1; ++dy) {
             unsigned int s, e;
             row_range(cell_start, c, dy, dz, p, s, e);
-            for (unsigned int j = s; j < e; ++j)
-                if (ref_neighbor(xi, f3(pos[j]), p.h2)) out[k++] = (int)id[j];
+            for (unsigned int j = s; j < e; ++j) {
+                const float3 xj = f3(pos[j]);
+                if (ref_neighbor(xi, xj, p.h2)) {
+                    if (d2out) d2out[k] = ref_dist2(xi, xj);
+                    out[k++] = (int)id[j];
+                }
+            }
         }
 }
 
@@ -774,11 +854,31 @@ void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const f
                      const float *dens, float4 *acc, cudaStream_t s) {
     k_pbf_visc<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, acc);
 }
+/* blocks of a constraint-pass launch: one per kPassBlock slots, or (with
+ * persistent warps) the resident blocks of the whole GPU, at most that */
+static unsigned int pass_blocks(int n, const void *kernel) {
+    unsigned int b = blocks_for(n, kPassBlock);
+#if FSPH_PERSIST
+    static int resident = 0;
+    if (resident == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kPassBlock, 0);
+        resident = std::max(1, sms * std::max(per, 1));
+    }
+    b = std::min(b, (unsigned int)resident);
+#else
+    (void)kernel;
+#endif
+    return b;
+}
+
 void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1, float *dens,
                    DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
                    const NbrLists &nl, cudaStream_t s) {
     auto k = p.compensated ? k_lambda<true> : k_lambda<false>;
-    k<<<blocks_for(p.n, kPassBlock), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
+    k<<<pass_blocks(p.n, (const void *)k), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
                                          (cudaGraphConditionalHandle)while_handle, use_graph,
                                          p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
@@ -791,7 +891,8 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
                        const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,
                        unsigned long long if_handle2, int use_graph, float4 *dp_out, const NbrLists &nl,
                        cudaStream_t s) {
-    k_correction<<<blocks_for(p.n, kPassBlock), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb, ctl, part,
+    k_correction<<<pass_blocks(p.n, (const void *)k_correction), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb,
+                                                                                    ctl, part,
                                                     (cudaGraphConditionalHandle)if_handle,
                                                     (cudaGraphConditionalHandle)if_handle2, use_graph, dp_out,
                                                     p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
@@ -816,13 +917,40 @@ void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const
     k_vort_apply<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vort, dens, vel_in, vel_out,
                                                     p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
-void launch_sph_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
-                        float *pres, cudaStream_t s) {
-    k_sph_density<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, dens, pres);
+void launch_sph_density(const DevParams &p, const unsigned int *cell_start, float4 *pos, float4 *vel, float *dens,
+                        float *pres, const NbrLists &nl, cudaStream_t s) {
+    k_sph_density<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres,
+                                                     p.use_lists ? nl.list : nullptr, nl.cnt);
+}
+/* lanes per particle of the WCSPH force pass: enough that the launch holds
+ * about as many threads as the GPU keeps resident (1536 per SM), at most 8 */
+int sph_force_lanes(int n) {
+    static int resident = 0;
+    if (resident == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        resident = std::max(sms, 1) * 1536;
+    }
+#ifdef FSPH_SPH_LANES
+    return FSPH_SPH_LANES;
+#else
+    int lanes = 1;
+    while (lanes < 8 && (long long)n * lanes < (long long)resident) lanes *= 2;
+    return lanes;
+#endif
 }
 void launch_sph_force(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                      const float *dens, const float *pres, float4 *acc, cudaStream_t s) {
-    k_sph_force<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres, acc);
+                      float4 *acc, const NbrLists &nl, cudaStream_t s) {
+    const ListEntry *l = p.use_lists ? nl.list : nullptr;
+    const int lanes = sph_force_lanes(p.n);
+    const unsigned int g = blocks_for((long long)p.n * lanes);
+    switch (lanes) {
+    case 1: k_sph_force<1><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, acc, l, nl.cnt); break;
+    case 2: k_sph_force<2><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, acc, l, nl.cnt); break;
+    case 4: k_sph_force<4><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, acc, l, nl.cnt); break;
+    default: k_sph_force<8><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, acc, l, nl.cnt); break;
+    }
 }
 void launch_sph_integrate(const DevParams &p, const float4 *pos_b, const float4 *vel_b, const float4 *acc,
                           const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a, float4 *vel_a,
@@ -835,8 +963,8 @@ void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const f
     k_nb_count<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, cnt);
 }
 void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
-                    const unsigned int *offsets, int *out, cudaStream_t s) {
-    k_nb_fill<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, id, offsets, out);
+                    const unsigned int *offsets, int *out, float *d2out, cudaStream_t s) {
+    k_nb_fill<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, id, offsets, out, d2out);
 }
 void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s) {
     k_unsort4<<<blocks_for(n), kBlock, 0, s>>>(n, id, src, dst, zero_w);

@@ -107,10 +107,15 @@ void launch_boundary_lambda(const DevParams &p, const unsigned int *cell_start, 
                             const float4 *ppos1, const DevCtl *ctl, const float2 *bstat, float *blam, cudaStream_t s);
 
 /* ---- WCSPH ---- */
-void launch_sph_density(const DevParams &p, const unsigned int *cell_start, const float4 *pos, float *dens,
-                        float *pres, cudaStream_t s);
+/* density + pressure of the sorted positions, the force pass's neighbour
+ * lists (nl.list / nl.cnt, when p.use_lists) and its per-neighbour factors
+ * in pos.w = p / rho^2 and vel.w = 1 / rho */
+void launch_sph_density(const DevParams &p, const unsigned int *cell_start, float4 *pos, float4 *vel, float *dens,
+                        float *pres, const NbrLists &nl, cudaStream_t s);
+/* acceleration from the lists and .w factors of launch_sph_density */
 void launch_sph_force(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                      const float *dens, const float *pres, float4 *acc, cudaStream_t s);
+                      float4 *acc, const NbrLists &nl, cudaStream_t s);
+int sph_force_lanes(int n);
 void launch_sph_integrate(const DevParams &p, const float4 *pos_b, const float4 *vel_b, const float4 *acc,
                           const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a, float4 *vel_a,
                           unsigned int *id_a, unsigned int *attr_a, cudaStream_t s);
@@ -118,8 +123,10 @@ void launch_sph_integrate(const DevParams &p, const float4 *pos_b, const float4 
 /* ---- neighbour sets under the reference criterion ---- */
 void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const float4 *pos, unsigned int *cnt,
                      cudaStream_t s);
+/* CSR rows from offsets: neighbour slots mapped through id, and (d2out,
+ * when given) each pair's squared distance as the reference's Dist2 */
 void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
-                    const unsigned int *offsets, int *out, cudaStream_t s);
+                    const unsigned int *offsets, int *out, float *d2out, cudaStream_t s);
 
 /* ---- particle order <-> device order ---- */
 void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s);

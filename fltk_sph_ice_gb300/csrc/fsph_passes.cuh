@@ -17,7 +17,7 @@ namespace fsph {
 
 /* ---------------- candidate loop ---------------- */
 
-/* Calls f(j, x[j]) for every candidate slot j of slot i handled by lane
+/* Calls f(j, load(j)) for every candidate slot j of slot i handled by lane
  * `sub` of its LPP-lane group: the list entries sub, sub + LPP, ... or -- for
  * an overflowed list or when lists are off -- every LPP-th slot of the 27
  * cells around the current position.  List entries are taken kBatch at a
@@ -39,6 +39,17 @@ namespace fsph {
 #define FSPH_PASS_MINB (FSPH_PASS_THREADS / FSPH_PASS_BLOCK)
 constexpr int kBatch = FSPH_KBATCH;
 
+/* FSPH_FOLD 1: the constraint passes keep constant factors out of the pair
+ * loop (fewer instructions per candidate; same results to rounding) */
+#ifndef FSPH_FOLD
+#define FSPH_FOLD 0
+#endif
+/* FSPH_PERSIST 1: the single-scene constraint passes run as many blocks as
+ * are resident on the GPU, each warp taking 32-slot chunks round-robin */
+#ifndef FSPH_PERSIST
+#define FSPH_PERSIST 0
+#endif
+
 /* Neighbour-list loads do not allocate in L1 (ld.global.nc.L1::no_allocate):
  * a pass streams ≈ 160 B of list per particle once, while the gathered
  * positions (16 B per particle, each read ≈ 40 times per pass) keep L1 to
@@ -53,6 +64,16 @@ __device__ __forceinline__ uint4 load_list_group(const uint4 *a) {
     asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
         : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
         : "l"(a));
+    return r;
+#elif FSPH_LIST_HINT == 2
+    /* also first in line for eviction from L2: the streamed lists make room
+     * before the gathered positions do */
+    uint4 r;
+    unsigned long long pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+        : "l"(a), "l"(pol));
     return r;
 #else
     return __ldg(a);
@@ -94,7 +115,7 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
             if (t0 + 4 * kListAhead < k) prefetch_list_group(lg + (size_t)((t0 >> 2) + kListAhead) * (size_t)p.n);
             const uint4 e = load_list_group(lg + (size_t)(t0 >> 2) * (size_t)p.n);
             const unsigned int j[4] = {e.x, e.y, e.z, e.w};
-            float4 xj[4];
+            decltype(load(0u)) xj[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) xj[u] = load(j[u]);
 #pragma unroll
@@ -114,7 +135,7 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
 #endif
         for (int t0 = sub; t0 < k; t0 += kBatch * LPP) {
             unsigned int j[kBatch];
-            float4 xj[kBatch];
+            decltype(load(0u)) xj[kBatch];
 #pragma unroll
             for (int u = 0; u < kBatch; ++u) {
                 const int t = t0 + u * LPP < k ? t0 + u * LPP : k - 1;
@@ -181,11 +202,11 @@ __device__ __forceinline__ void predict_body(const DevParams &p, int i, const fl
     float3 a = acc ? f3(acc[i]) : p.gravity;
     v = v + p.dt * a;
     x = x + p.dt * v;
-    x = wall_project(x, p);
+    x = solid_project(x, p);
     if (xpred_out) xpred_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
     /* warm start: the iterations begin from walls(x* + predicted correction);
      * the grid and lists are then built on that start */
-    if (dwarm) x = wall_project(x + f3(dwarm[i]), p);
+    if (dwarm) x = solid_project(x + f3(dwarm[i]), p);
     ppos_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
     unsigned int c = cell_index(cell_of(x, p), p);
     key[i] = c;
@@ -258,6 +279,13 @@ __device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned 
     float wsum = 0.f, wc = 0.f, sd = 0.f;
     float3 gs = make_float3(0.f, 0.f, 0.f);
     const float agr = p.ag * p.inv_rest_dens;
+#if FSPH_FOLD
+    /* the pair loop sums g' = (h - r)^2 / r; the coefficient agr (grad W /
+     * rho0 = agr g' d) multiplies the sums once after the loop */
+    const float agl = 1.0f;
+#else
+    const float agl = agr;
+#endif
     /* plain (L1-cached) loads: only the .w words of pp are written by this
      * pass, and the neighbour loop reads x, y, z */
     for_each_candidate<LPP>(
@@ -270,7 +298,7 @@ __device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned 
             const float q = fmaxf(p.h2 - r2, 0.0f);
             const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
-            const float g = agr * t * t * inv_r; /* grad W / rho0 = g d */
+            const float g = agl * t * t * inv_r; /* grad W / rho0 = (agr / agl) g d */
             if (KAHAN) { /* compensated sum of the density terms */
                 const float y = q * q * q - wc;
                 const float s = wsum + y;
@@ -291,6 +319,9 @@ __device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned 
     }
     float rho = p.mass * p.aw * wsum;
     sd += dot3(gs, gs);
+#if FSPH_FOLD
+    sd *= agr * agr;
+#endif
     if (p.nb) {
         /* boundary particles (rx_sph_pbd.cpp:728-748, 795-818): density
          * rho0 psi_b W and |grad C|^2 terms of (rho0 psi_b / m) grad W / rho0,
@@ -399,6 +430,16 @@ __device__ __forceinline__ float correction_body(const DevParams &p, const unsig
     const float k_dt2 = -p.ap_k * p.dt * p.dt;
     const float agr = p.ag * p.inv_rest_dens;
     const float awq = p.aw * p.inv_wq;
+#if FSPH_FOLD
+    /* agr multiplies the sum once after the loop; for n = 4 the tensile
+     * term -k dt^2 (awq q^3)^4 is K q^12 with K = -k dt^2 awq^4 (|K| ~ 1e26
+     * for the configured h, well inside FP32) */
+    const float agl = 1.0f;
+    const float awq2 = awq * awq;
+    const float k12 = k_dt2 * (awq2 * awq2);
+#else
+    const float agl = agr;
+#endif
     for_each_candidate<LPP>(
         p, cell_start, list, cnt, cellb, i, xi, rs, sub, [&](unsigned int j) { return __ldg(src + j); },
         [&](unsigned int, const float4 &xj4) {
@@ -407,21 +448,33 @@ __device__ __forceinline__ float correction_body(const DevParams &p, const unsig
             const float r2 = dot3(d, d);
             const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
-            const float g = agr * t * t * inv_r;
-            float sc = 0.0f;
+            const float g = agl * t * t * inv_r;
+            float coef = li + xj4.w;
             if (p.use_ap) {
                 const float q = fmaxf(p.h2 - r2, 0.0f);
+#if FSPH_FOLD
+                if (p.ap_n == 4.0f) {
+                    const float q2 = q * q, q4 = q2 * q2;
+                    coef = fmaf(k12, (q4 * q4) * q4, coef);
+                } else {
+                    coef += k_dt2 * __powf(awq * q * q * q, p.ap_n);
+                }
+#else
                 const float ww = awq * q * q * q;
                 const float pw = (p.ap_n == 4.0f) ? (ww * ww) * (ww * ww) : __powf(ww, p.ap_n);
-                sc = k_dt2 * pw;
+                coef += k_dt2 * pw;
+#endif
             }
-            acc = acc + ((li + xj4.w + sc) * g) * d;
+            acc = acc + (coef * g) * d;
         });
     if (LPP > 1) {
         acc.x = group_sum<LPP>(acc.x);
         acc.y = group_sum<LPP>(acc.y);
         acc.z = group_sum<LPP>(acc.z);
     }
+#if FSPH_FOLD
+    acc = agr * acc;
+#endif
     if (p.nb) {
         /* boundary terms (rx_sph_pbd.cpp:977-1019): lambda_b, and s_corr of
          * the (rho0 psi_b / m)-scaled W */
@@ -445,7 +498,7 @@ __device__ __forceinline__ float correction_body(const DevParams &p, const unsig
     }
     if (!valid || sub != 0) return 0.0f;
     if (dp_out) dp_out[i] = make_float4(acc.x, acc.y, acc.z, 0.0f);
-    float3 xn = wall_project(xi + acc, p);
+    float3 xn = solid_project(xi + acc, p);
     dst[i] = make_float4(xn.x, xn.y, xn.z, 0.0f);
     float3 dd = xn - f3(xb[i]);
     if (!(xn.x == xn.x && xn.y == xn.y && xn.z == xn.z)) ctl->nan_flag = 1u;
@@ -500,9 +553,14 @@ __device__ __forceinline__ void correction_tail(const DevParams &lp, DevCtl *ctl
 
 /* ---------------- end of step ---------------- */
 
-/* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), the XSPH
- * update v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij, and (fo.feat) the
- * warm-start features of the particle. */
+/* omega_i = sum_j (m / rho_j)(v_j - v_i) x grad_j W_ij (grad_j = -grad_i):
+ * the SPH curl of v, each neighbour weighted by its volume m / rho_j as in
+ * the XSPH sum and the eta gradient below (Macklin & Mueller 2013, eq. 15,
+ * writes the sum without the volume, whose scale their eps absorbs; in
+ * SI units that sum is ~1e5 times the curl at h = 0.0457 and the configured
+ * eps = 1e-4 then drives the flow unstable).  The XSPH update
+ * v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij, and (fo.feat) the warm-start
+ * features of the particle. */
 template <bool NBR = true>
 __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
                                                const float4 *__restrict__ pos, const float4 *__restrict__ vel,
@@ -535,7 +593,7 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
             const float3 vij = f3(__ldg(vel + j)) - vi;
             const float rhoj = __ldg(dens + j);
             const float mrho = p.mass / rhoj;
-            om = om + cross3(vij, (-g) * d);
+            om = om + cross3(vij, (-g * mrho) * d);
             xs = xs + (p.aw * q * q * q * mrho) * vij;
             cntf += inside;
             off = off - inside * d;

@@ -162,6 +162,25 @@ class rxParticleSystemBase:
         return self.last_stats
 
     # -- neighbours --------------------------------------------------------
+    def SetParticlesToCell(self, prts=None, h: float = -1.0):
+        """SetParticlesToCell() / (prts, n, h) (rx_sph_pbd.cpp:1735-1750): the
+        neighbour sets of the current particles, or of the given positions
+        among themselves, within h (default: the kernel radius), kept for
+        GetNeights.  Returns CSR (offsets[n+1], indices ascending in each row,
+        dist2 = each pair's squared distance as the reference's rxNeigh::Dist2)."""
+        p4 = None if prts is None else _as4(prts)
+        n = self.GetNumParticles() if p4 is None else p4.shape[0]
+        off = np.zeros(n + 1, dtype=np.int32)
+        total = ctypes.c_longlong(0)
+        self._check(self.L.fsph_neighbors_ex(self._ctx, _ptr(p4), n, float(h), abi.HOST, _ptr(off), None, None, 0,
+                                             ctypes.byref(total)), "fsph_neighbors_ex")
+        idx = np.zeros(max(total.value, 1), dtype=np.int32)
+        d2 = np.zeros(max(total.value, 1), dtype=np.float32)
+        self._check(self.L.fsph_neighbors_ex(self._ctx, _ptr(p4), n, float(h), abi.HOST, _ptr(off), _ptr(idx),
+                                             _ptr(d2), total.value, ctypes.byref(total)), "fsph_neighbors_ex")
+        self._neighs = (off, idx[:total.value], d2[:total.value])
+        return self._neighs
+
     def GetNeights(self):
         """Neighbour sets of the current positions (GetNeights, rx_sph.h:1196) as
         CSR (offsets[n+1], indices), particle indices ascending in each row."""
@@ -174,7 +193,37 @@ class rxParticleSystemBase:
                     "fsph_neighbors")
         return off, idx[:total.value]
 
-    SetParticlesToCell = GetNeights
+    # -- analytic obstacles (rx_ps.h:266-272) ------------------------------
+    def SetBoxObstacle(self, cen, ext, ang=(0.0, 0.0, 0.0), vel=(0.0, 0.0, 0.0), flg: int = 1):
+        """A box obstacle: centre, half extents, Euler angles in degrees."""
+        d = lambda v: np.ascontiguousarray(v, dtype=np.float64)  # noqa: E731
+        c, e, a, v = d(cen), d(ext), d(ang), d(vel)
+        self._check(self.L.fsph_set_box_obstacle(self._ctx, _ptr(c), _ptr(e), _ptr(a), _ptr(v), int(flg)),
+                    "fsph_set_box_obstacle")
+
+    def SetSphereObstacle(self, cen, rad: float, vel=(0.0, 0.0, 0.0), flg: int = 1):
+        c, v = np.ascontiguousarray(cen, np.float64), np.ascontiguousarray(vel, np.float64)
+        self._check(self.L.fsph_set_sphere_obstacle(self._ctx, _ptr(c), float(rad), _ptr(v), int(flg)),
+                    "fsph_set_sphere_obstacle")
+
+    def MoveSphereObstacle(self, b: int, disp):
+        d = np.ascontiguousarray(disp, np.float64)
+        self._check(self.L.fsph_move_sphere_obstacle(self._ctx, int(b), _ptr(d)), "fsph_move_sphere_obstacle")
+
+    def GetSphereObstaclePos(self, b: int = 0) -> np.ndarray:
+        out = np.zeros(3, np.float64)
+        self._check(self.L.fsph_get_sphere_obstacle_pos(self._ctx, int(b), _ptr(out)), "fsph_get_sphere_obstacle_pos")
+        return out
+
+    def ClearObstacles(self):
+        self._check(self.L.fsph_clear_obstacles(self._ctx), "fsph_clear_obstacles")
+
+    def UpdateWithoutPosAndVel(self, dt: float, step: int = 0) -> bool:
+        """A step's fields without moving the particles (rx_ps.h:254,
+        rx_sph_gpu.cpp:925): density, pressure and acceleration (WCSPH) or the
+        PBF pre-pass density and external + viscous acceleration."""
+        self._check(self.L.fsph_step_fields(self._ctx, float(dt), None), "fsph_step_fields")
+        return True
 
 
 class rxSPH(rxParticleSystemBase):

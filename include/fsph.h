@@ -218,6 +218,27 @@ int fsph_sync(fsph_ctx *ctx);
  * (particle indices, ascending within each row) holds at most cap entries;
  * *total receives the number of entries.  Synchronises. */
 int fsph_neighbors(fsph_ctx *ctx, int *offsets, int *indices, long long cap, long long *total);
+/* The same for any positions (SetParticlesToCell(prts, n, h) + GetNeights,
+ * rx_sph_pbd.cpp:1735-1750, rx_nnsearch.h:454-515): pos4 = n float4 (host or
+ * device, `where`) whose neighbours among themselves are wanted, or NULL for
+ * the context's particles (n ignored); radius <= 0 means params.h, and it
+ * may not exceed the grid's cell width h (1 + cell_skin) (FSPH_UNSUPPORTED).
+ * dist2 (optional, same length as indices) receives each pair's squared
+ * distance as the reference's rxNeigh::Dist2: float coordinates differenced
+ * and squared in double, rounded to float.  With indices NULL or cap below
+ * the total, only offsets and *total are written.  Synchronises. */
+int fsph_neighbors_ex(fsph_ctx *ctx, const float *pos4, int n, float radius, int where, int *offsets,
+                      int *indices, float *dist2, long long cap, long long *total);
+
+/* ---- fields without moving the particles (UpdateWithoutPosAndVel) ---- */
+/* rxSPH_GPU::UpdateWithoutPosAndVel (rx_sph_gpu.cpp:925-1060; the pure
+ * virtual of rx_ps.h:254): a step's field evaluation without its position
+ * and velocity update.  WCSPH: density, pressure and acceleration
+ * (calDensity + calForce); PBF: the step's pre-pass, density and the
+ * external + viscous acceleration (calDensity + calForceExtAndVisc,
+ * rx_sph_pbd.cpp:599-689).  FSPH_DENSITY / FSPH_PRESSURE / FSPH_FORCE then
+ * read them; positions and velocities are unchanged.  Synchronises. */
+int fsph_step_fields(fsph_ctx *ctx, float dt, void *stream);
 
 /* ---- single passes, for parity checks against the CPU path ---- */
 /* PBF lambda pass on the given positions (rxPBDSPH::calScalingFactor,
@@ -294,6 +315,30 @@ int fsph_num_boundary(const fsph_ctx *ctx);
 /* host dst, the given order of the boundary particles */
 int fsph_get_boundary(fsph_ctx *ctx, int which, float *dst);
 
+/* ---- analytic obstacles ---- */
+/* SetBoxObstacle / SetSphereObstacle / MoveSphereObstacle /
+ * GetSphereObstaclePos (rx_ps.h:266-272; rxPBDSPH_GPU, rx_sph_pbd_gpu.cpp:
+ * 2425-2480): at most 10 boxes and 10 spheres (MAX_BOX_NUM /
+ * MAX_SPHERE_NUM, rx_cu_common.cuh:135-136).  A particle that the
+ * prediction, a position correction or a WCSPH integration leaves inside an
+ * obstacle moves to its surface: a box -- centre cen, half extents ext,
+ * rotated by the Euler angles ang (degrees; pitch, yaw, roll as
+ * EulerToMatrix, rx_sph_commons.h:185-210) -- through its nearest face, a
+ * sphere radially (collisionPointBox / collisionPointSphere,
+ * rx_cu_common.cu:748-831), obstacles before the box walls.  The velocity
+ * is not reflected (the CPU path's reflection is commented out,
+ * rx_sph_pbd.cpp:1384); vel is accepted and unused, as in the reference's
+ * fluid step; flg = 0 adds nothing.  Obstacles apply to both solvers; the
+ * batched scenes take none. */
+int fsph_set_box_obstacle(fsph_ctx *ctx, const double *cen, const double *ext, const double *ang,
+                          const double *vel, int flg);
+int fsph_set_sphere_obstacle(fsph_ctx *ctx, const double *cen, double rad, const double *vel, int flg);
+/* moves sphere b (in the order added) by disp; takes effect at the next step */
+int fsph_move_sphere_obstacle(fsph_ctx *ctx, int b, const double *disp);
+int fsph_get_sphere_obstacle_pos(const fsph_ctx *ctx, int b, double *pos);
+int fsph_clear_obstacles(fsph_ctx *ctx);
+int fsph_num_obstacles(const fsph_ctx *ctx);
+
 /* ---- learned warm start ---- */
 /* The network: FSPH_MLP_FEATURES -> 64 -> 64 -> 3, ReLU, BF16 tensor-core
  * arithmetic with FP32 accumulation.  Its parameters are one FP32 blob of
@@ -335,12 +380,16 @@ typedef enum fsph_pass {
     FSPH_PASS_LAMBDA = 0,      /* one lambda pass (density + constraint + error reduction) */
     FSPH_PASS_CORRECTION = 1,  /* one position-correction pass */
     FSPH_PASS_GRID = 2,        /* one grid build (hash, scan, scatter, cell sort, reorder) */
-    FSPH_PASS_LIST = 3         /* one neighbour-list build on the current grid */
+    FSPH_PASS_LIST = 3,        /* one neighbour-list build on the current grid */
+    FSPH_PASS_SPH_DENSITY = 4, /* WCSPH: one density + pressure pass */
+    FSPH_PASS_SPH_FORCE = 5    /* WCSPH: one force (pressure + viscosity + gravity) pass */
 } fsph_pass;
-/* Time `reps` back-to-back launches of one pass of the current PBF state
- * with CUDA events on the context's stream; *avg_ms receives the mean time
- * of one launch.  The state is advanced as the passes would advance it
- * (corrections are applied), so call it after the steps to be kept.
+/* Time `reps` back-to-back launches of one pass of the current state (the
+ * PBF passes on a PBF context, the WCSPH passes on a WCSPH one) with CUDA
+ * events on the context's stream; *avg_ms receives the mean time of one
+ * launch.  A PBF state is advanced as the passes would advance it
+ * (corrections are applied), so call it after the steps to be kept; the
+ * WCSPH passes leave the particles unchanged.
  * No counterpart in the reference (its timing was the GUI's RXTIMER splits,
  * rx_sph.h:40-58). */
 int fsph_time_pass(fsph_ctx *ctx, int pass, int reps, float *avg_ms);

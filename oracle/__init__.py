@@ -64,6 +64,8 @@ def orc_lib() -> ctypes.CDLL:
         L.fsph_orc_pbf_step.restype = ci
         L.fsph_orc_sph_step.argtypes = [vp, cf]
         L.fsph_orc_finalize_ext.argtypes = [vp, vp, vp, vp, cf, vp, vp]
+        L.fsph_orc_set_obstacles.argtypes = [vp, vp, ci]
+        L.fsph_orc_project.argtypes = [vp, vp, ci, vp]
         L.fsph_orc_neighbors.argtypes = [vp, vp, vp, vp, ctypes.c_longlong]
         L.fsph_orc_neighbors.restype = ctypes.c_longlong
         L.fsph_orc_pbf_lambda.argtypes = [vp, vp, vp, vp]
@@ -127,6 +129,19 @@ class Oracle:
 
     def sph_step(self, dt: float):
         self.L.fsph_orc_sph_step(self.h, dt)
+
+    def set_obstacles(self, boxes=(), spheres=()):
+        """Analytic obstacles: boxes as (cen, ext, ang_degrees), spheres as (cen, rad)."""
+        rec = [[0.0, *c, *e, *a, 0.0] for c, e, a in boxes] + [[1.0, *c, 0, 0, 0, 0, 0, 0, r] for c, r in spheres]
+        arr = np.ascontiguousarray(rec, dtype=np.float64).reshape(-1, 11)
+        self.L.fsph_orc_set_obstacles(self.h, _vp(arr), arr.shape[0])
+
+    def project(self, pos4):
+        """The solid projection (obstacles, then the box walls) of the given points."""
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        out = np.zeros_like(pos4)
+        self.L.fsph_orc_project(self.h, _vp(pos4), pos4.shape[0], _vp(out))
+        return out
 
     def finalize_ext(self, pos4, vel4, dens, dt: float):
         """XSPH + vorticity confinement alone on the given state: (velocity after both, omega)."""

@@ -44,6 +44,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -105,6 +106,13 @@ struct Solver {
     std::vector<T> bpos, bvol, blam;
     std::vector<int> bb_off, bb_idx, fb_off, fb_idx, bf_off, bf_idx;
     Kern K;
+    /* analytic obstacles: type (0 box, 1 sphere), centre, half extents,
+     * world -> local rotation (rows), sphere radius */
+    struct Obs {
+        int type;
+        double cen[3], ext[3], R[3][3], rad;
+    };
+    std::vector<Obs> obs;
     int last_iters = 0;
     double last_err1 = 0, last_err2 = 0, last_errmax = 0;
 
@@ -288,7 +296,39 @@ struct Solver {
      * (rxSolidBox::GetDistanceR -> AABB_point_dist with sgn = 1, contact =
      * pos + n |d|).  Velocity is left unchanged: the reflection is commented
      * out in the reference (rx_sph_pbd.cpp:1392). */
+    /* Obstacle projection, the rule of collisionPointBox / collisionPointSphere
+     * with calCollisionSolidPB (rx_cu_common.cu:748-831, rx_pbdsph_kernel.cu:
+     * 863-911): a point inside a box (in its rotated frame) moves to the
+     * nearest face (ties x, y, z), inside a sphere radially to its surface.
+     * The reference's CPU path sets obstacles up as rxSolid objects whose
+     * particle-radius handling is inverted for obstacles (AABB_point_dist with
+     * sgn = -1, rx_sph_solid.cpp:44-108), so the GPU rule is the one restated. */
+    V3 obstacles(V3 x) const {
+        for (const Obs &o : obs) {
+            V3 l = x - v3(o.cen[0], o.cen[1], o.cen[2]);
+            if (o.type == 1) {
+                double ll = std::sqrt(dot(l, l));
+                if (ll < o.rad && ll > 0.0) x = v3(o.cen[0], o.cen[1], o.cen[2]) + (o.rad / ll) * l;
+                continue;
+            }
+            double cp[3], li[3] = {l.x, l.y, l.z};
+            for (int r = 0; r < 3; ++r) cp[r] = o.R[r][0] * li[0] + o.R[r][1] * li[1] + o.R[r][2] * li[2];
+            double t[3];
+            for (int k = 0; k < 3; ++k) t[k] = std::fabs(cp[k]) - o.ext[k];
+            if (t[0] < 0.0 && t[1] < 0.0 && t[2] < 0.0) {
+                double a[3] = {-t[0], -t[1], -t[2]};
+                int ax = (a[0] <= a[1] && a[0] <= a[2]) ? 0 : ((a[1] <= a[0] && a[1] <= a[2]) ? 1 : 2);
+                cp[ax] = cp[ax] > 0.0 ? o.ext[ax] : -o.ext[ax];
+                double w[3];
+                for (int r = 0; r < 3; ++r) w[r] = o.R[0][r] * cp[0] + o.R[1][r] * cp[1] + o.R[2][r] * cp[2];
+                x = v3(o.cen[0] + w[0], o.cen[1] + w[1], o.cen[2] + w[2]);
+            }
+        }
+        return x;
+    }
+
     V3 wall(V3 pos) const {
+        if (!obs.empty()) pos = obstacles(pos);
         const double r = (double)(T)P.particle_radius;
         double cen[3], sl[3];
         for (int k = 0; k < 3; ++k) {
@@ -562,9 +602,11 @@ struct Solver {
     }
 
     /* XSPH (rx_pbdsph_kernel.cu:1090-1162) and vorticity confinement
-     * (Macklin & Mueller 2013, eq. 15-16), both evaluated on the velocities
-     * v = (x* - x)/dt and the densities of the last lambda pass:
-     *   w_i   = sum_j (v_j - v_i) x grad_j W(x_i - x_j),  grad_j = -grad_i
+     * (Macklin & Mueller 2013, eq. 15-16, with the SPH curl weighted by the
+     * neighbour volume m / rho_j, which the paper leaves to its eps), both
+     * evaluated on the velocities v = (x* - x)/dt and the densities of the
+     * last lambda pass:
+     *   w_i   = sum_j (m / rho_j)(v_j - v_i) x grad_j W(x_i - x_j),  grad_j = -grad_i
      *   eta_i = sum_j (m / rho_j) (|w_j| - |w_i|) grad_i W(x_i - x_j)
      *   N_i   = eta_i / |eta_i|,  f_i = eps (N_i x w_i)
      *   v_i  <- v_i + c sum_j (m / rho_j)(v_j - v_i) W(r_ij) + dt f_i        */
@@ -585,7 +627,7 @@ struct Solver {
                 T r = (T)std::sqrt(dot(d, d));
                 V3 vij = at(vel, j) - vi;
                 V3 gi = K.G((double)r) * d;
-                om = om + cross(vij, -1.0 * gi);
+                om = om + (m / (double)dens[j]) * cross(vij, -1.0 * gi);
                 xs = xs + (m / (double)dens[j] * K.W((double)r)) * vij;
             }
             w[i] = om;
@@ -662,6 +704,31 @@ struct Handle {
     Solver<T> s;
     explicit Handle(const fsph_params &p) : s(p) {}
 };
+
+template <class T>
+void set_obstacles(Solver<T> *S, const double *rec, int n) {
+    S->obs.clear();
+    const double d2r = 3.14159265358979323846 / 180.0;
+    for (int k = 0; k < n; ++k) {
+        const double *q = rec + 11 * (size_t)k;
+        typename Solver<T>::Obs ob{};
+        ob.type = (int)q[0];
+        for (int a = 0; a < 3; ++a) {
+            ob.cen[a] = q[1 + a];
+            ob.ext[a] = q[4 + a];
+        }
+        ob.rad = q[10];
+        /* EulerToMatrix (rx_sph_commons.h:185-210): degrees, (pitch, yaw, roll) */
+        const double cp = std::cos(q[7] * d2r), sp = std::sin(q[7] * d2r);
+        const double cy = std::cos(q[8] * d2r), sy = std::sin(q[8] * d2r);
+        const double cr = std::cos(q[9] * d2r), sr = std::sin(q[9] * d2r);
+        const double cc = cy * cr, cs = cy * sr, sc = sy * cr, ss = sy * sr;
+        const double m[3][3] = {{cc + sp * ss, cs - sp * sc, -sy * cp}, {-cp * sr, cp * cr, -sp},
+                                {sc - sp * cs, ss + sp * cc, cy * cp}};
+        std::memcpy(ob.R, m, sizeof(m));
+        S->obs.push_back(ob);
+    }
+}
 
 template <class T>
 void load4(std::vector<T> &dst, const float *src, int n) {
@@ -755,6 +822,26 @@ int fsph_orc_pbf_step(fsph_orc *o, float dt, int fixed_iters, double *errs) {
 }
 
 void fsph_orc_sph_step(fsph_orc *o, float dt) { ORC_DISPATCH(o, S->sph_step(dt)); }
+
+/* Analytic obstacles: n records of 11 doubles -- type (0 box, 1 sphere),
+ * centre xyz, half extents xyz, Euler angles in degrees (pitch, yaw, roll;
+ * EulerToMatrix, rx_sph_commons.h:185-210), sphere radius. */
+void fsph_orc_set_obstacles(fsph_orc *o, const double *rec, int n) {
+    if (o->prec) set_obstacles((Solver<double> *)o->s, rec, n);
+    else set_obstacles((Solver<float> *)o->s, rec, n);
+}
+
+/* The solid projection (obstacles, then the box walls) of n points. */
+void fsph_orc_project(fsph_orc *o, const float *pos4, int n, float *out4) {
+    ORC_DISPATCH(o, {
+        for (int i = 0; i < n; ++i) {
+            V3 x = v3(pos4[4 * (size_t)i], pos4[4 * (size_t)i + 1], pos4[4 * (size_t)i + 2]);
+            x = S->wall(x);
+            out4[4 * (size_t)i] = (float)x.x; out4[4 * (size_t)i + 1] = (float)x.y;
+            out4[4 * (size_t)i + 2] = (float)x.z; out4[4 * (size_t)i + 3] = 0.0f;
+        }
+    });
+}
 
 /* XSPH + vorticity confinement alone (the end of pbf_step) on the given
  * positions, velocities and densities: velocity after both, and omega. */

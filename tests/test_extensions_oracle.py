@@ -7,8 +7,11 @@ These three terms have no CPU code in the reference to pin them against:
             xsphVisocosity / calXsphViscosityCell (rx_pbdsph_kernel.cu:1090-1162),
             disabled at rx_sph_pbd_gpu.cpp:926-927;
   vorticity Macklin & Mueller 2013 ("Position Based Fluids", eq. 15-16, cited
-            at rx_sph.h:1281; the reference has only the flag, rx_ps.h:161,238):
-              w_i   = sum_j (v_j - v_i) x grad_j W(x_i - x_j),  grad_j W = -grad_i W
+            at rx_sph.h:1281; the reference has only the flag, rx_ps.h:161,238),
+            with the curl weighted by the neighbour volume V_j = m / rho_j
+            (the paper's eq. 15 leaves V_j to its eps; without it the
+            configured eps = 1e-4 drives the dam breaks unstable):
+              w_i   = sum_j V_j (v_j - v_i) x grad_j W(x_i - x_j),  grad_j W = -grad_i W
               eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W(x_i - x_j)
               f_i   = eps (eta_i / |eta_i|) x w_i, applied as an acceleration:
               v_i  <- v_i(after XSPH) + dt f_i
@@ -80,7 +83,8 @@ def xsph_vorticity_numpy(pos, vel, dens, p, dt, bounds=False):
     wgt = np.where(inside, m / rho[None, :] * W(r), 0.0)
     v_x = v + c * (wgt[:, :, None] * vij).sum(1)
     g = G(r)[:, :, None] * d                                  # grad_i W
-    w = np.cross(vij, -g).sum(1)                              # sum_j v_ij x grad_j W
+    vol = m / rho[None, :]                                    # neighbour volume m / rho_j
+    w = (vol[:, :, None] * np.cross(vij, -g)).sum(1)          # sum_j V_j v_ij x grad_j W
     wm = np.linalg.norm(w, axis=1)
     eta = ((m / rho[None, :] * (wm[None, :] - wm[:, None]))[:, :, None] * g).sum(1)
     en = np.linalg.norm(eta, axis=1)
@@ -91,7 +95,7 @@ def xsph_vorticity_numpy(pos, vel, dens, p, dt, bounds=False):
     delta = 32 * np.finfo(np.float32).eps
     gn = np.linalg.norm(g, axis=-1)
     vn = np.linalg.norm(vij, axis=-1)
-    d_w = delta * (vn * gn).sum(1)                                      # omega
+    d_w = delta * (vol * vn * gn).sum(1)                                # omega
     d_x = delta * c * (wgt * vn).sum(1)                                 # XSPH change
     mr = m / rho[None, :] * gn
     d_eta = delta * (mr * np.abs(wm[None, :] - wm[:, None])).sum(1) + (mr * (d_w[None, :] + d_w[:, None])).sum(1)

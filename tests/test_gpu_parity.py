@@ -109,16 +109,17 @@ def test_pbf_variants_match_oracle(gpu, variant):
         assert_rel(ps.GetArrayVBO(abi.RX_DENSITY), o.get("dens"), 1e-5, f"{variant} density step {k + 1}")
         xg0, xo0 = xg.astype(np.float64), xo.astype(np.float64)
     if variant == "xsph_vort":
-        # omega = sum_j (v_j - v_i) x grad_j W: the velocity error above times
-        # 2 sum_j |grad W_ij| (at most 2 dv per pair), plus the FP32 rounding
-        # of the terms (32 eps x sum_j |v_ij| |grad W_ij|)
+        # omega = sum_j (m / rho_j)(v_j - v_i) x grad_j W: the velocity error
+        # above times 2 sum_j (m / rho_j) |grad W_ij| (at most 2 dv per pair),
+        # plus the FP32 rounding of the terms (32 eps x the sum of their sizes)
         off, idx = o.neighbors(o.get("pos"))
         rows = np.repeat(np.arange(sc.n), np.diff(off))
         x, v = o.get("pos")[:, :3].astype(np.float64), o.get("vel")[:, :3].astype(np.float64)
         d = x[rows] - x[idx]
         r = np.sqrt((d * d).sum(1))
         h = float(np.float32(p.h))
-        gw = np.where((r > 0) & (r <= h), 45.0 / (np.pi * h ** 6) * (h - r) ** 2, 0.0)
+        rho = o.get("dens").astype(np.float64)
+        gw = np.where((r > 0) & (r <= h), 45.0 / (np.pi * h ** 6) * (h - r) ** 2, 0.0) * float(p.mass) / rho[idx]
         sg = np.bincount(rows, weights=gw, minlength=sc.n)
         sv = np.bincount(rows, weights=gw * np.linalg.norm(v[idx] - v[rows], axis=1), minlength=sc.n)
         bound = 2.0 * dv * sg + 32 * np.finfo(np.float32).eps * sv

@@ -76,16 +76,18 @@ def assert_sets_equal(off_a, idx_a, off_b, idx_b):
         f"{len(np.unique(ra[ca != cb]))} particles with different neighbour sets"
 
 
-def assert_step_equal(gpu, ref, x0, what):
-    """One step's results: the position change (element-wise with the
-    storage ulp of both positions), velocity and density."""
+def assert_step_equal(gpu, ref, x0g, x0r, what):
+    """One step's results from the two sides' start positions x0g / x0r
+    (equal for a first step, else apart by what earlier steps left): the
+    position change (element-wise, with one storage ulp of each position and
+    the start difference), velocity (the same over dt) and density."""
     xg, xr = gpu.GetArrayVBO(abi.RX_POSITION)[:, :3], ref.get("pos")[:, :3]
-    x0 = np.asarray(x0)[:, :3]
-    storage = ulp32(xr) + ulp32(x0)
-    assert_close(xg - x0, xr.astype(np.float64) - x0, f"{what}: position change", atol=storage)
-    # v = (x* - x) / dt: the position storage error divided by dt
+    x0g = np.asarray(x0g, np.float64)[:, :3]
+    x0r = np.asarray(x0r, np.float64)[:, :3]
+    carried = ulp32(xr) + ulp32(x0r) + np.abs(x0g - x0r)
+    assert_close(xg - x0g, xr.astype(np.float64) - x0r, f"{what}: position change", atol=carried)
     vg, vr = gpu.GetArrayVBO(abi.RX_VELOCITY)[:, :3], ref.get("vel")[:, :3]
-    assert_close(vg, vr, f"{what}: velocity", atol=storage / PBF_DT)
+    assert_close(vg, vr, f"{what}: velocity", atol=carried / PBF_DT)
     dg, dr = gpu.GetArrayVBO(abi.RX_DENSITY), ref.get("dens")
     assert_close(dg, dr, f"{what}: density", etol=1e-5, floor=0.0)
 
@@ -150,12 +152,12 @@ def pbf_pair(p, pos, vel):
 def steps_vs_reference(p, pos, vel, nsteps, what):
     g, r = pbf_pair(p, pos, vel)
     for k in range(nsteps):
-        x0 = g.GetArrayVBO(abi.RX_POSITION)
+        x0g, x0r = g.GetArrayVBO(abi.RX_POSITION), r.get("pos")
         g.Update(PBF_DT)
         it, eta = r.update(PBF_DT)
         assert g.last_stats.iterations == 4 and it == 4
         assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-4 * eta, (g.last_stats.density_error_two_sided, eta)
-        assert_step_equal(g, r, x0, f"{what} step {k + 1}")
+        assert_step_equal(g, r, x0g, x0r, f"{what} step {k + 1}")
     g.close()
 
 
@@ -230,9 +232,18 @@ def test_bench_state_neighbour_sets_bit_exact(gpu, ref_available, bench_rolled):
     off, idx = g.GetNeights()
     g.close()
     r = oracle.RefSolver(reference_setup(sc.params), sc.n, "pbf")
-    off_r, idx_r, _ = r.neighbors(x)
+    off_r, idx_r, d2_r = r.neighbors(x)
     assert_sets_equal(off, idx, off_r, idx_r)
     assert np.diff(off).min() >= 1 and np.diff(off).max() > 40
+    # the squared distances as the reference's rxNeigh::Dist2, bit-exact
+    g = rxPBDSPH(sc.params)
+    g.Set(x)
+    off_g, idx_g, d2_g = g.SetParticlesToCell()
+    g.close()
+    rows_r = np.repeat(np.arange(sc.n), np.diff(off_r))
+    o = np.lexsort((idx_r, rows_r))
+    assert np.array_equal(idx_g, idx_r[o])
+    assert np.array_equal(d2_g.view(np.uint32), d2_r[o].view(np.uint32)), "Dist2 differs from the reference"
 
 
 def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
@@ -255,7 +266,7 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
         if rebuilds:
             assert g.last_stats.grid_builds > 1, g.last_stats.grid_builds
         assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-4 * eta
-        assert_step_equal(g, r, x, f"1M, skin {skin}")
+        assert_step_equal(g, r, x, x, f"1M, skin {skin}")
         g.close()
 
 
@@ -268,12 +279,13 @@ def test_c1_wcsph_steps_match_reference(gpu, ref_available):
     r = oracle.RefSolver(p, sc.n, "sph")
     r.set(sc.pos, sc.vel)
     for k in range(10):
-        x0 = g.GetArrayVBO(abi.RX_POSITION)[:, :3]
+        x0g = g.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64)
+        x0r = r.get("pos")[:, :3].astype(np.float64)
         g.Update(sc.dt)
         r.update(sc.dt)
         xg, xr = g.GetArrayVBO(abi.RX_POSITION)[:, :3], r.get("pos")[:, :3]
-        assert_close(xg - x0, xr.astype(np.float64) - x0, f"WCSPH step {k + 1}: position change",
-                     atol=ulp32(xr) + ulp32(x0))
+        assert_close(xg - x0g, xr.astype(np.float64) - x0r, f"WCSPH step {k + 1}: position change",
+                     atol=ulp32(xr) + ulp32(x0r) + np.abs(x0g - x0r))
         assert_close(g.GetArrayVBO(abi.RX_DENSITY), r.get("dens"), f"WCSPH step {k + 1}: density", etol=1e-5,
                      floor=0.0)
         # accelerations are sums of cancelling pressure terms: norm-wise bar

@@ -149,7 +149,7 @@ EXPORTS = [
     "fsph_pbf_eval_correction", "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_time_pass",
     "fsph_pbf_eval_lambda_noalloc", "fsph_neighbors_ex", "fsph_step_fields",
     "fsph_set_box_obstacle", "fsph_set_sphere_obstacle", "fsph_move_sphere_obstacle", "fsph_get_sphere_obstacle_pos",
-    "fsph_clear_obstacles", "fsph_num_obstacles",
+    "fsph_clear_obstacles", "fsph_num_obstacles", "fsph_density_grid",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
     "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
     "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
@@ -203,6 +203,7 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_get_sphere_obstacle_pos.argtypes = [c_void_p, c_int, c_void_p]
     L.fsph_clear_obstacles.argtypes = [c_void_p]
     L.fsph_num_obstacles.argtypes = [c_void_p]
+    L.fsph_density_grid.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
     L.fsph_time_pass.argtypes = [c_void_p, c_int, c_int, P(c_float)]
     L.fsph_mlp_create.argtypes = [P(c_void_p)]
     L.fsph_mlp_destroy.argtypes = [c_void_p]
@@ -245,7 +246,7 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
                  "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_params_from_env",
                  "fsph_neighbors_ex", "fsph_step_fields", "fsph_set_box_obstacle", "fsph_set_sphere_obstacle",
                  "fsph_move_sphere_obstacle", "fsph_get_sphere_obstacle_pos", "fsph_clear_obstacles",
-                 "fsph_num_obstacles"]:
+                 "fsph_num_obstacles", "fsph_density_grid"]:
         getattr(L, name).restype = c_int
     return L
 

@@ -173,6 +173,7 @@ DevParams make_dev(const fsph_params &p, int n, float dt) {
     d.inv_rest_dens = 1.0f / p.rest_dens;
     double h = (double)p.h;
     d.aw = (float)poly6_coef(h);
+    d.aw_d = poly6_coef(h);
     d.ag = (float)(-45.0 / (kPi * std::pow(h, 6.0)));
     d.al = (float)(45.0 / (kPi * std::pow(h, 6.0)));
     double r = (double)p.particle_radius;
@@ -1238,6 +1239,42 @@ int fsph_neighbors_ex(fsph_ctx *c, const float *pos4, int n, float radius, int w
 
 int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long long *total) {
     return fsph_neighbors_ex(c, nullptr, 0, 0.0f, FSPH_HOST, offsets, indices, nullptr, cap, total);
+}
+
+int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const double *d, float *out, int where) {
+    if (!c || !nn || !minp || !d || !out) return FSPH_INVALID_ARG;
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    for (int a = 0; a < 3; ++a)
+        if (nn[a] <= 0 || !std::isfinite(minp[a]) || !std::isfinite(d[a]))
+            return fail(c, FSPH_INVALID_ARG, "lattice: positive node counts, finite origin and spacing");
+    const long long tot = (long long)nn[0] * nn[1] * nn[2];
+    if (tot > (1ll << 31)) return fail(c, FSPH_INVALID_ARG, "more than 2^31 lattice nodes");
+    cudaStream_t s = c->stream;
+    float *dout = where == FSPH_DEVICE ? out : nullptr;
+    if (c->n == 0) { /* no particles: an empty field */
+        if (where == FSPH_HOST) std::memset(out, 0, (size_t)tot * sizeof(float));
+        else FSPH_CUDA(c, cudaMemsetAsync(out, 0, (size_t)tot * sizeof(float), s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        return FSPH_OK;
+    }
+    /* the simulation range: the box grown by 1 % (rx_sph_pbd.cpp:188-196) */
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        const double size = c->P.box_max[a] - c->P.box_min[a];
+        lo[a] = c->P.box_min[a] - 0.5 * 0.01 * size;
+        hi[a] = lo[a] + size * (1.0 + 0.01);
+    }
+    DevParams p = dev_for(c, c->n, 1.0f);
+    FSPH_TRY(build_on(c, p, c->set[0].pos));
+    if (!dout) FSPH_CUDA(c, cudaMallocAsync((void **)&dout, (size_t)tot * sizeof(float), s));
+    launch_density_grid(p, c->cell_start, c->set[1].pos, nn, minp, d, lo, hi, dout, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && where == FSPH_HOST)
+        e = cudaMemcpyAsync(out, dout, (size_t)tot * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (where == FSPH_HOST) cudaFreeAsync(dout, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(c, FSPH_CUDA_ERROR, std::string("density grid: ") + cudaGetErrorString(e));
+    return FSPH_OK;
 }
 
 int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {

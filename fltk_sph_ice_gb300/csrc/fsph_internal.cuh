@@ -40,6 +40,7 @@ struct DevParams {
     int n;
     float h, h2, mass, rest_dens, inv_rest_dens;
     float aw, ag, al;           /* poly6, spiky-gradient, visc-Laplacian coefficients */
+    double aw_d;                /* the poly6 coefficient in double (the reference's) */
     float3 wall_lo, wall_hi;    /* box_min + r, box_max - r */
     float3 gravity;
     float viscosity, gas_k;

@@ -741,6 +741,57 @@ __global__ void k_nb_fill(DevParams p, const unsigned int *__restrict__ cell_sta
 }
 
 /* ======================================================================== */
+/* density on a lattice (for meshing)                                       */
+/* ======================================================================== */
+
+/* The density field at the nodes of an nx x ny x nz lattice (i fastest),
+ * node (i, j, k) at minp + (i, j, k) d: 0 outside [lo, hi], else
+ * sum_j m W(r_j) over the particles with fl32(|x - x_j|^2 in double) <=
+ * fl32(h h), r_j = fl32(sqrt(Dist2)), W in double and the sum in float, as
+ * rxPBDSPH::CalColorField (rx_sph_pbd.cpp:2075-2108, the CPU form of
+ * pbdsphCalDensityInGrid, rx_pbdsph_kernel.cu:1220-1299).  A float
+ * distance test in a 1e-4 band around h^2 skips the double evaluation for
+ * the candidates far outside. */
+__global__ void __launch_bounds__(kBlock) k_density_grid(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                         const float4 *__restrict__ pos, int nx, int ny, int nz,
+                                                         double3 minp, double3 dd, double3 lo, double3 hi,
+                                                         float *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nx * ny * nz) return;
+    const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / ((long long)nx * ny));
+    /* minp + Vec3(i, j, k) * d, each product and sum rounded in double */
+    const double X = __dadd_rn(minp.x, __dmul_rn((double)i, dd.x));
+    const double Y = __dadd_rn(minp.y, __dmul_rn((double)j, dd.y));
+    const double Z = __dadd_rn(minp.z, __dmul_rn((double)k, dd.z));
+    float acc = 0.0f;
+    if (X >= lo.x && X <= hi.x && Y >= lo.y && Y <= hi.y && Z >= lo.z && Z <= hi.z) {
+        const float3 xf = make_float3((float)X, (float)Y, (float)Z);
+        const int3 c = cell_of(xf, p);
+        const float band = p.h2 * (1.0f + 1e-4f);
+        const double hd = (double)p.h, aw = (double)p.aw_d, m = (double)p.mass;
+        for (int dz = -1; dz <= 1; ++dz)
+            for (int dy = -1; dy <= 1; ++dy) {
+                unsigned int s, e;
+                row_range(cell_start, c, dy, dz, p, s, e);
+                for (unsigned int q = s; q < e; ++q) {
+                    const float4 xq = __ldg(pos + q);
+                    const float3 df = xf - f3(xq);
+                    if (dot3(df, df) > band) continue;
+                    const double ex = X - (double)xq.x, ey = Y - (double)xq.y, ez = Z - (double)xq.z;
+                    const float d2 =
+                        __double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)), __dmul_rn(ez, ez)));
+                    if (d2 <= p.h2) {
+                        const double r = (double)sqrtf(d2);
+                        const double qq = __dsub_rn(__dmul_rn(hd, hd), __dmul_rn(r, r));
+                        acc = __double2float_rn(__dadd_rn((double)acc, __dmul_rn(m, __dmul_rn(__dmul_rn(__dmul_rn(aw, qq), qq), qq))));
+                    }
+                }
+            }
+    }
+    out[t] = acc;
+}
+
+/* ======================================================================== */
 /* order conversion                                                         */
 /* ======================================================================== */
 
@@ -965,6 +1016,15 @@ void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const f
 void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
                     const unsigned int *offsets, int *out, float *d2out, cudaStream_t s) {
     k_nb_fill<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, id, offsets, out, d2out);
+}
+void launch_density_grid(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const int nn[3],
+                         const double minp[3], const double d[3], const double lo[3], const double hi[3], float *out,
+                         cudaStream_t s) {
+    const long long tot = (long long)nn[0] * nn[1] * nn[2];
+    k_density_grid<<<blocks_for(tot), kBlock, 0, s>>>(p, cell_start, pos, nn[0], nn[1], nn[2],
+                                                      make_double3(minp[0], minp[1], minp[2]),
+                                                      make_double3(d[0], d[1], d[2]), make_double3(lo[0], lo[1], lo[2]),
+                                                      make_double3(hi[0], hi[1], hi[2]), out);
 }
 void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s) {
     k_unsort4<<<blocks_for(n), kBlock, 0, s>>>(n, id, src, dst, zero_w);

@@ -128,6 +128,11 @@ void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const f
 void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
                     const unsigned int *offsets, int *out, float *d2out, cudaStream_t s);
 
+/* ---- density on a lattice (CalImplicitField) ---- */
+void launch_density_grid(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const int nn[3],
+                         const double minp[3], const double d[3], const double lo[3], const double hi[3], float *out,
+                         cudaStream_t s);
+
 /* ---- particle order <-> device order ---- */
 void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s);
 void launch_unsort1(int n, const unsigned int *id, const unsigned int *src, unsigned int *dst, cudaStream_t s);

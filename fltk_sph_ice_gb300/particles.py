@@ -193,6 +193,22 @@ class rxParticleSystemBase:
                     "fsph_neighbors")
         return off, idx[:total.value]
 
+    # -- density on a lattice (rx_ps.h:283-285) ----------------------------
+    def CalImplicitField(self, n, minp, d) -> np.ndarray:
+        """The density field of the current particles on an n[0] x n[1] x n[2]
+        lattice from minp with spacing d (CalImplicitField, rx_sph_pbd.cpp:2036):
+        an (n[2], n[1], n[0]) float32 array, 0 outside the simulation range."""
+        nn = np.ascontiguousarray(n, dtype=np.int32)
+        out = np.zeros(int(np.prod(nn)), np.float32)
+        self._check(self.L.fsph_density_grid(self._ctx, _ptr(nn), _ptr(np.ascontiguousarray(minp, np.float64)),
+                                             _ptr(np.ascontiguousarray(d, np.float64)), _ptr(out), abi.HOST),
+                    "fsph_density_grid")
+        return out.reshape(nn[2], nn[1], nn[0])
+
+    def GetImplicit(self, x: float, y: float, z: float) -> float:
+        """The density field at one point (GetImplicit, rx_sph_pbd.cpp:2024)."""
+        return float(self.CalImplicitField((1, 1, 1), (x, y, z), (1.0, 1.0, 1.0))[0, 0, 0])
+
     # -- analytic obstacles (rx_ps.h:266-272) ------------------------------
     def SetBoxObstacle(self, cen, ext, ang=(0.0, 0.0, 0.0), vel=(0.0, 0.0, 0.0), flg: int = 1):
         """A box obstacle: centre, half extents, Euler angles in degrees."""

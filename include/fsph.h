@@ -230,6 +230,19 @@ int fsph_neighbors(fsph_ctx *ctx, int *offsets, int *indices, long long cap, lon
 int fsph_neighbors_ex(fsph_ctx *ctx, const float *pos4, int n, float radius, int where, int *offsets,
                       int *indices, float *dist2, long long cap, long long *total);
 
+/* ---- density on a lattice, for surface meshing ---- */
+/* CalImplicitField / CalImplicitFieldDevice (rx_ps.h:283-285;
+ * rxPBDSPH::CalImplicitField -> CalColorField, rx_sph_pbd.cpp:2024-2108;
+ * on the GPU pbdsphCalDensityInGrid / sphCalDensityInGrid,
+ * rx_pbdsph_kernel.cu:1220-1299, rx_sph_kernel.cu:1038-1085): the density
+ * sum_j m W_poly6(|x - x_j|) of the current particles at the nodes of an
+ * n[0] x n[1] x n[2] lattice, node (i, j, k) at minp + (i, j, k) d, stored
+ * at out[k n0 n1 + j n0 + i] (host or device float array per `where`);
+ * nodes outside the simulation range (the box grown by 1 %, as the
+ * reference's Initialize sets it) read 0.  The field a marching-cubes mesher
+ * consumes (rx_mc_kernel.cu).  Synchronises. */
+int fsph_density_grid(fsph_ctx *ctx, const int *n, const double *minp, const double *d, float *out, int where);
+
 /* ---- fields without moving the particles (UpdateWithoutPosAndVel) ---- */
 /* rxSPH_GPU::UpdateWithoutPosAndVel (rx_sph_gpu.cpp:925-1060; the pure
  * virtual of rx_ps.h:254): a step's field evaluation without its position

@@ -278,6 +278,23 @@ public:
         return p;
     }
 
+    /* -- density on a lattice for meshing (rx_ps.h:280-285) ------------- */
+    /* hF[k n0 n1 + j n0 + i] = density at minp + (i, j, k) d (host array) */
+    virtual void CalImplicitField(int n[3], Vec3 minp, Vec3 d, RXREAL *hF) {
+        m_status = fsph_density_grid(m_ctx, n, minp.data, d.data, hF, FSPH_HOST);
+    }
+    /* the same into a device array */
+    virtual void CalImplicitFieldDevice(int n[3], Vec3 minp, Vec3 d, RXREAL *dF) {
+        m_status = fsph_density_grid(m_ctx, n, minp.data, d.data, dF, FSPH_DEVICE);
+    }
+    virtual double GetImplicit(double x, double y, double z) {
+        int n[3] = {1, 1, 1};
+        float v = 0.0f;
+        const double p[3] = {x, y, z}, one[3] = {1.0, 1.0, 1.0};
+        m_status = fsph_density_grid(m_ctx, n, p, one, &v, FSPH_HOST);
+        return v;
+    }
+
     /* -- scene set-up (rx_ps.cpp:66-261) --------------------------------- */
     void Reset(rxParticleConfig config) {
         if (!m_ctx) return;

@@ -66,6 +66,7 @@ def orc_lib() -> ctypes.CDLL:
         L.fsph_orc_finalize_ext.argtypes = [vp, vp, vp, vp, cf, vp, vp]
         L.fsph_orc_set_obstacles.argtypes = [vp, vp, ci]
         L.fsph_orc_project.argtypes = [vp, vp, ci, vp]
+        L.fsph_orc_density_grid.argtypes = [vp, vp, vp, vp, vp]
         L.fsph_orc_neighbors.argtypes = [vp, vp, vp, vp, ctypes.c_longlong]
         L.fsph_orc_neighbors.restype = ctypes.c_longlong
         L.fsph_orc_pbf_lambda.argtypes = [vp, vp, vp, vp]
@@ -135,6 +136,15 @@ class Oracle:
         rec = [[0.0, *c, *e, *a, 0.0] for c, e, a in boxes] + [[1.0, *c, 0, 0, 0, 0, 0, 0, r] for c, r in spheres]
         arr = np.ascontiguousarray(rec, dtype=np.float64).reshape(-1, 11)
         self.L.fsph_orc_set_obstacles(self.h, _vp(arr), arr.shape[0])
+
+    def density_grid(self, n, minp, d):
+        """The density field of the current positions on an n[0] x n[1] x n[2]
+        lattice from minp with spacing d (CalImplicitField); (n[2], n[1], n[0])."""
+        nn = np.ascontiguousarray(n, dtype=np.int32)
+        out = np.zeros(int(np.prod(nn)), np.float32)
+        self.L.fsph_orc_density_grid(self.h, _vp(nn), _vp(np.ascontiguousarray(minp, np.float64)),
+                                     _vp(np.ascontiguousarray(d, np.float64)), _vp(out))
+        return out.reshape(nn[2], nn[1], nn[0])
 
     def project(self, pos4):
         """The solid projection (obstacles, then the box walls) of the given points."""
@@ -237,6 +247,7 @@ def ref_lib() -> ctypes.CDLL | None:
         L.fsph_ref_pbf_dp.argtypes = [vp, vp, vp, ci, cf, vp]
         L.fsph_ref_pbf_predict.argtypes = [vp, cf, vp, vp, vp, vp]
         L.fsph_ref_sph_forces.argtypes = [vp, vp, vp, vp]
+        L.fsph_ref_pbf_density_grid.argtypes = [vp, vp, ci, vp, vp, vp, vp]
         L.fsph_ref_kernel.restype = cd
         L.fsph_ref_kernel.argtypes = [ci, cd, cd]
         L.fsph_ref_kernel_coef.restype = cd
@@ -333,6 +344,17 @@ class RefSolver:
         dp = np.zeros((self.n, 4), np.float32)
         self.L.fsph_ref_pbf_dp(self.h, _vp(pos4), _vp(lam), self.n, dt, _vp(dp))
         return dp
+
+    def density_grid(self, pos4, n, minp, d):
+        """rxPBDSPH::CalImplicitField of the given particles on an n[0] x n[1] x n[2]
+        lattice from minp with spacing d; returns (n[2], n[1], n[0])."""
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        nn = np.ascontiguousarray(n, dtype=np.int32)
+        out = np.zeros(int(np.prod(nn)), np.float32)
+        self.L.fsph_ref_pbf_density_grid(self.h, _vp(pos4), pos4.shape[0], _vp(nn),
+                                         _vp(np.ascontiguousarray(minp, np.float64)),
+                                         _vp(np.ascontiguousarray(d, np.float64)), _vp(out))
+        return out.reshape(nn[2], nn[1], nn[0])
 
     def sph_forces(self):
         d = np.zeros(self.n, np.float32)

@@ -664,6 +664,74 @@ struct Solver {
         vel.swap(vnew);
     }
 
+    /* The density field on a lattice for meshing (rxPBDSPH::CalImplicitField
+     * -> GetImplicit -> CalColorField, rx_sph_pbd.cpp:2024-2108): node (i, j, k)
+     * at minp + (i, j, k) d (double), 0 outside the simulation range (the
+     * box grown by 1 %, rx_sph_pbd.cpp:188-196), else sum_j m W(r_j) over the
+     * particles with fl(|x - x_j|^2) <= fl(h h), r_j = fl(sqrt(Dist2)),
+     * accumulated in T; out[k nx ny + j nx + i]. */
+    void density_grid(const int nn[3], const double minp[3], const double dd[3], float *out) const {
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            const double size = P.box_max[a] - P.box_min[a];
+            lo[a] = P.box_min[a] - 0.5 * 0.01 * size;
+            hi[a] = lo[a] + size * (1.0 + 0.01);
+        }
+        const T hT = (T)P.h;
+        const T h2 = hT * hT;
+        const double cw = (double)P.h * 1.0001;
+        int g[3];
+        for (int a = 0; a < 3; ++a) g[a] = std::max(1, (int)std::floor((hi[a] - lo[a]) / cw) + 1);
+        const size_t C = (size_t)g[0] * g[1] * g[2];
+        std::vector<int> cnt(C + 1, 0), cellOf(n), order(n);
+        auto cell3 = [&](const double x[3], int c[3]) {
+            for (int a = 0; a < 3; ++a) c[a] = std::min(std::max((int)std::floor((x[a] - lo[a]) / cw), 0), g[a] - 1);
+        };
+        for (int i = 0; i < n; ++i) {
+            double x[3] = {(double)pos[4 * (size_t)i], (double)pos[4 * (size_t)i + 1], (double)pos[4 * (size_t)i + 2]};
+            int c[3];
+            cell3(x, c);
+            cellOf[i] = (int)(((size_t)c[2] * g[1] + c[1]) * g[0] + c[0]);
+            cnt[cellOf[i] + 1]++;
+        }
+        for (size_t c = 0; c < C; ++c) cnt[c + 1] += cnt[c];
+        {
+            std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+            for (int i = 0; i < n; ++i) order[fill[cellOf[i]]++] = i;
+        }
+        const double m = (double)(T)P.mass;
+        const long long tot = (long long)nn[0] * nn[1] * nn[2];
+#pragma omp parallel for schedule(static)
+        for (long long t = 0; t < tot; ++t) {
+            const int i = (int)(t % nn[0]), j = (int)((t / nn[0]) % nn[1]), k = (int)(t / ((long long)nn[0] * nn[1]));
+            const double x[3] = {minp[0] + i * dd[0], minp[1] + j * dd[1], minp[2] + k * dd[2]};
+            T c = 0;
+            bool inside = true;
+            for (int a = 0; a < 3; ++a) inside = inside && x[a] >= lo[a] && x[a] <= hi[a];
+            if (inside) {
+                int cc[3];
+                cell3(x, cc);
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            const int z = cc[2] + dz, y = cc[1] + dy, xx = cc[0] + dx;
+                            if (xx < 0 || y < 0 || z < 0 || xx >= g[0] || y >= g[1] || z >= g[2]) continue;
+                            const size_t cell = ((size_t)z * g[1] + y) * g[0] + xx;
+                            for (int s = cnt[cell]; s < cnt[cell + 1]; ++s) {
+                                const int q = order[s];
+                                const V3 dv = v3(x[0], x[1], x[2]) - at(pos, q);
+                                const T d2 = (T)dot(dv, dv);
+                                if (d2 <= h2) {
+                                    const T r = (T)std::sqrt((double)d2);
+                                    acc_add(c, m * K.W((double)r));
+                                }
+                            }
+                        }
+            }
+            out[t] = (float)c;
+        }
+    }
+
     /* ---------------- WCSPH ---------------- */
     /* p = k (rho - rho0); a_i = -sum m (p_i/rho_i^2 + p_j/rho_j^2) gradW
      *   + mu sum m (v_j - v_i)/rho_j lapW + g (rx_sph_cpu.cpp:558-656). */
@@ -829,6 +897,11 @@ void fsph_orc_sph_step(fsph_orc *o, float dt) { ORC_DISPATCH(o, S->sph_step(dt))
 void fsph_orc_set_obstacles(fsph_orc *o, const double *rec, int n) {
     if (o->prec) set_obstacles((Solver<double> *)o->s, rec, n);
     else set_obstacles((Solver<float> *)o->s, rec, n);
+}
+
+/* rxPBDSPH::CalImplicitField of the current positions (see Solver::density_grid). */
+void fsph_orc_density_grid(fsph_orc *o, const int *nn, const double *minp, const double *d, float *out) {
+    ORC_DISPATCH(o, S->density_grid(nn, minp, d, out));
 }
 
 /* The solid projection (obstacles, then the box walls) of n points. */

@@ -152,7 +152,8 @@ def extract() -> bool:
               r"^void rxPBDSPH::calPositionCorrection", r"^RXREAL rxPBDSPH::calRestDensity",
               r"^int rxPBDSPH::calCollisionSolid", r"^void rxPBDSPH::integrate",
               r"^void rxPBDSPH::GetNearestNeighbors\(int", r"^void rxPBDSPH::GetNearestNeighbors\(Vec3",
-              r"^void rxPBDSPH::SetParticlesToCell\(RXREAL", r"^void rxPBDSPH::SetParticlesToCell\(void"]:
+              r"^void rxPBDSPH::SetParticlesToCell\(RXREAL", r"^void rxPBDSPH::SetParticlesToCell\(void",
+              r"^double rxPBDSPH::GetImplicit", r"^void rxPBDSPH::CalImplicitField\(", r"^double rxPBDSPH::CalColorField"]:
         parts.append(_block(pbd, a))
     parts.append('#line 1 "rx_sph_cpu.cpp"\n')
     for a in [r"^void rxSPH::Initialize", r"^bool rxSPH::Update", r"^void rxSPH::calDensity",

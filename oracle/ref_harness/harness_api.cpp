@@ -168,6 +168,18 @@ long long fsph_ref_neighbors(void *p, const float *pos4, int n, int *offsets, in
     return t;
 }
 
+/* The density field on a lattice (rxPBDSPH::CalImplicitField -> CalColorField,
+ * rx_sph_pbd.cpp:2024-2108) of the given particles: node (i, j, k) at
+ * minp + (i, j, k) d, out[k nx ny + j nx + i]. */
+void fsph_ref_pbf_density_grid(void *p, const float *pos4, int n, const int *nn, const double *minp,
+                               const double *d, float *out) {
+    rxPBDSPH *s = (rxPBDSPH *)p;
+    set_particles(s, n, pos4, nullptr);
+    s->m_pNNGrid->SetObjectToCell(s->m_hPos, n);
+    int dims[3] = {nn[0], nn[1], nn[2]};
+    s->CalImplicitField(dims, Vec3(minp[0], minp[1], minp[2]), Vec3(d[0], d[1], d[2]), out);
+}
+
 /* One lambda pass (rxPBDSPH::calScalingFactor) on the given predicted positions. */
 void fsph_ref_pbf_lambda(void *p, const float *pos4, int n, float dt, float *dens, float *scl) {
     rxPBDSPH *s = (rxPBDSPH *)p;

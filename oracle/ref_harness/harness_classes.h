@@ -116,6 +116,9 @@ public:
     void GetNearestNeighbors(int idx, RXREAL *p, vector<rxNeigh> &neighs, RXREAL h = -1.0);
     void SetParticlesToCell(void);
     void SetParticlesToCell(RXREAL *prts, int n, RXREAL h);
+    double GetImplicit(double x, double y, double z);
+    void CalImplicitField(int n[3], Vec3 minp, Vec3 d, RXREAL *hF);
+    double CalColorField(double x, double y, double z);
 };
 
 class rxSPH : public fsphRefBase {

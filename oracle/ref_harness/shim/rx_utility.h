@@ -48,6 +48,8 @@ inline Vec3 operator-(const Vec3 &a, const Vec3 &b) { return Vec3(a[0] - b[0], a
 inline Vec3 operator-(const Vec3 &a, double s) { return Vec3(a[0] - s, a[1] - s, a[2] - s); }
 inline Vec3 operator*(const Vec3 &a, double s) { return Vec3(a[0] * s, a[1] * s, a[2] * s); }
 inline Vec3 operator*(double s, const Vec3 &a) { return Vec3(a[0] * s, a[1] * s, a[2] * s); }
+/* element-wise product, as the reference's vector class (rx_sph_pbd.cpp:2045) */
+inline Vec3 operator*(const Vec3 &a, const Vec3 &b) { return Vec3(a[0] * b[0], a[1] * b[1], a[2] * b[2]); }
 inline Vec3 operator/(const Vec3 &a, double s) { return Vec3(a[0] / s, a[1] / s, a[2] / s); }
 inline double norm2(const Vec3 &a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
 inline double norm(const Vec3 &a) { return sqrt(norm2(a)); }

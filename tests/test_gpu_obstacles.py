@@ -106,3 +106,4 @@ def test_moving_sphere_obstacle(gpu):
         ps.SetSphereObstacle((0.0, 0.0, 0.0), 0.01)
     ps.ClearObstacles()
     ps.Update(0.0016)
+

@@ -149,7 +149,8 @@ EXPORTS = [
     "fsph_pbf_eval_correction", "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_time_pass",
     "fsph_pbf_eval_lambda_noalloc", "fsph_neighbors_ex", "fsph_step_fields",
     "fsph_set_box_obstacle", "fsph_set_sphere_obstacle", "fsph_move_sphere_obstacle", "fsph_get_sphere_obstacle_pos",
-    "fsph_clear_obstacles", "fsph_num_obstacles", "fsph_density_grid",
+    "fsph_clear_obstacles", "fsph_num_obstacles", "fsph_density_grid", "fsph_num_active", "fsph_add_delete_region",
+    "fsph_clear_delete_regions", "fsph_add_inlet_line", "fsph_clear_inlets", "fsph_emit_inlets",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
     "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
     "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
@@ -204,6 +205,13 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_clear_obstacles.argtypes = [c_void_p]
     L.fsph_num_obstacles.argtypes = [c_void_p]
     L.fsph_density_grid.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+    L.fsph_num_active.argtypes = [c_void_p]
+    L.fsph_add_delete_region.argtypes = [c_void_p, c_void_p, c_void_p]
+    L.fsph_clear_delete_regions.argtypes = [c_void_p]
+    L.fsph_add_inlet_line.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int,
+                                      ctypes.c_double]
+    L.fsph_clear_inlets.argtypes = [c_void_p]
+    L.fsph_emit_inlets.argtypes = [c_void_p, c_int, P(c_int)]
     L.fsph_time_pass.argtypes = [c_void_p, c_int, c_int, P(c_float)]
     L.fsph_mlp_create.argtypes = [P(c_void_p)]
     L.fsph_mlp_destroy.argtypes = [c_void_p]
@@ -246,7 +254,8 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
                  "fsph_pbf_eval_xsph_vorticity", "fsph_sph_eval_forces", "fsph_params_from_env",
                  "fsph_neighbors_ex", "fsph_step_fields", "fsph_set_box_obstacle", "fsph_set_sphere_obstacle",
                  "fsph_move_sphere_obstacle", "fsph_get_sphere_obstacle_pos", "fsph_clear_obstacles",
-                 "fsph_num_obstacles", "fsph_density_grid"]:
+                 "fsph_num_obstacles", "fsph_density_grid", "fsph_num_active", "fsph_add_delete_region",
+                 "fsph_clear_delete_regions", "fsph_add_inlet_line", "fsph_clear_inlets", "fsph_emit_inlets"]:
         getattr(L, name).restype = c_int
     return L
 

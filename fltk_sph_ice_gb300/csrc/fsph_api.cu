@@ -94,6 +94,19 @@ struct fsph_ctx {
     unsigned int *b_id = nullptr, *b_key = nullptr, *b_rank = nullptr;
     unsigned int *b_count = nullptr, *b_cell = nullptr;
     unsigned char *b_near = nullptr;
+    /* dynamic particle count: slots [0, n_active) of the home set take part
+     * in the steps, [n_active, n) are deleted particles (attribute -1)
+     * parked at the reference's far point */
+    int n_active = 0;
+    unsigned int *part_scan = nullptr, *part_bsum = nullptr;
+    struct Inlet {
+        double pos1[3], pos2[3], vel[3], up[3], spacing;
+        int accum, span;
+    };
+    std::vector<Inlet> inlets;
+    int inlet_start = -1;
+    std::vector<float4> del_regions; /* (lo, hi) pairs */
+    float4 *del_dev = nullptr;
     /* analytic obstacles: boxes first, then spheres, as uploaded */
     std::vector<Obstacle> boxes, spheres;
     Obstacle *obs_dev = nullptr;
@@ -234,6 +247,8 @@ void free_particles(fsph_ctx *c) {
     cudaFree(c->xb); cudaFree(c->acc); cudaFree(c->vort); cudaFree(c->dens); cudaFree(c->pres);
     cudaFree(c->key); cudaFree(c->rank); cudaFree(c->perm); cudaFree(c->epart); cudaFree(c->dpart);
     cudaFree(c->res_id); c->res_id = nullptr;
+    cudaFree(c->part_scan); cudaFree(c->part_bsum);
+    c->part_scan = c->part_bsum = nullptr;
     cudaFree(c->nl.list); cudaFree(c->nl.cnt); cudaFree(c->nl.cellb);
     c->nl = NbrLists{};
     cudaFree(c->xpred); cudaFree(c->dstep); cudaFree(c->dwarm); cudaFree(c->tmp4); cudaFree(c->feat);
@@ -335,6 +350,8 @@ int alloc_particles(fsph_ctx *c, int cap) {
     FSPH_TRY(dalloc(c, &c->dens, n)); FSPH_TRY(dalloc(c, &c->pres, n));
     FSPH_TRY(dalloc(c, &c->key, n)); FSPH_TRY(dalloc(c, &c->rank, n)); FSPH_TRY(dalloc(c, &c->perm, n));
     FSPH_TRY(dalloc(c, &c->res_id, n));
+    FSPH_TRY(dalloc(c, &c->part_scan, n + 1));
+    FSPH_TRY(dalloc(c, &c->part_bsum, scan_blocks((unsigned int)n)));
     FSPH_TRY(dalloc(c, &c->nl.list, n * kListMax)); FSPH_TRY(dalloc(c, &c->nl.cnt, n));
     FSPH_TRY(dalloc(c, &c->nl.cellb, n));
     FSPH_TRY(dalloc(c, &c->xpred, n)); FSPH_TRY(dalloc(c, &c->dstep, n)); FSPH_TRY(dalloc(c, &c->dwarm, n));
@@ -700,9 +717,84 @@ int load_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int
         FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, b, c->stream));
     }
     FSPH_CUDA(c, cudaMemsetAsync(c->warm_valid, 0, sizeof(unsigned int), c->stream));
-    if (n != c->n) c->graph_valid = false;
+    if (n != c->n_active) c->graph_valid = false;
     c->n = n;
+    c->n_active = n;
     return check_launch(c);
+}
+
+/* Bring the home set to particle order (slot d = particle d), as the
+ * setters need it; the last step's results keep its slot order in res_id. */
+int home_to_particle_order(fsph_ctx *c) {
+    if (c->home_identity) return FSPH_OK;
+    cudaStream_t s = c->stream;
+    const int n = c->n;
+    launch_unsort4(n, c->set[0].id, c->set[0].pos, c->set[1].pos, 0, s);
+    launch_unsort4(n, c->set[0].id, c->set[0].vel, c->set[1].vel, 0, s);
+    launch_unsort1(n, c->set[0].id, c->set[0].attr, c->set[1].attr, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    /* the warm-start history (step corrections, features) follows the particles */
+    launch_unsort4(n, c->set[0].id, c->dstep, c->tmp4, 0, s);
+    FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, c->tmp4, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    if (!c->res_in_res_id) {
+        /* the last step's other results (density, lambda, forces, ...) stay
+         * in its slot order, which res_id keeps for the getters */
+        FSPH_CUDA(c, cudaMemcpyAsync(c->res_id, c->set[0].id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        c->res_in_res_id = true;
+    }
+    {
+        float4 *tf = reinterpret_cast<float4 *>(c->nl.list); /* lists are rebuilt by every step */
+        launch_unsort_rows(n, c->set[0].id, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->feat, tf, (size_t)n * kFeatures * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    launch_iota(n, c->set[0].id, s);
+    c->home_identity = true;
+    return check_launch(c);
+}
+
+/* Stable partition of the home set: particles with attribute != -1 first
+ * (they take part in the steps), deleted ones after; n_active follows.
+ * Synchronises. */
+int repartition(fsph_ctx *c) {
+    const int n = c->n;
+    cudaStream_t s = c->stream;
+    if (n > 0) {
+        if (!c->res_in_res_id) {
+            FSPH_CUDA(c, cudaMemcpyAsync(c->res_id, c->set[0].id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+            c->res_in_res_id = true;
+        }
+        launch_mark_active(n, c->set[0].attr, c->key, s);
+        launch_scan(c->key, c->part_scan, c->part_bsum, (unsigned int)n, s);
+        launch_partition_perm(n, c->part_scan, c->perm, s);
+        Gather g{};
+        g.n4 = 3; g.n1 = 2;
+        g.src4[0] = c->set[0].pos; g.dst4[0] = c->set[1].pos;
+        g.src4[1] = c->set[0].vel; g.dst4[1] = c->set[1].vel;
+        g.src4[2] = c->dstep; g.dst4[2] = c->tmp4;
+        g.src1[0] = c->set[0].id; g.dst1[0] = c->set[1].id;
+        g.src1[1] = c->set[0].attr; g.dst1[1] = c->set[1].attr;
+        launch_gather(n, c->perm, g, nullptr, s);
+        float4 *tf = reinterpret_cast<float4 *>(c->nl.list);
+        launch_gather_rows(n, c->perm, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, c->tmp4, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].id, c->set[1].id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->feat, tf, (size_t)n * kFeatures * 4, cudaMemcpyDeviceToDevice, s));
+        unsigned int na = 0;
+        FSPH_CUDA(c, cudaMemcpyAsync(&na, c->part_scan + n, 4, cudaMemcpyDeviceToHost, s));
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
+        FSPH_TRY(check_launch(c));
+        if ((int)na != c->n_active) c->graph_valid = false;
+        c->n_active = (int)na;
+        c->home_identity = false;
+    } else {
+        c->n_active = 0;
+    }
+    return FSPH_OK;
 }
 
 /* Build the grid on device positions x (length n, current slot order) and
@@ -879,6 +971,7 @@ int fsph_destroy(fsph_ctx *c) {
     cudaFree(c->warm_valid);
     cudaFree(c->mlp_dev);
     cudaFree(c->obs_dev);
+    cudaFree(c->del_dev);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->s2) cudaStreamDestroy(c->s2);
     if (c->s3) cudaStreamDestroy(c->s3);
@@ -899,14 +992,20 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
         if (c->n > p->max_particles) return fail(c, FSPH_INVALID_ARG, "max_particles below the current particle count");
         /* keep the particles across the reallocation */
         std::vector<float4> hp((size_t)c->n), hv((size_t)c->n);
+        std::vector<int> ha((size_t)c->n);
         if (c->n) {
             FSPH_TRY(fsph_get_array(c, FSPH_POSITION, hp.data(), FSPH_HOST, nullptr));
             FSPH_TRY(fsph_get_array(c, FSPH_VELOCITY, hv.data(), FSPH_HOST, nullptr));
+            FSPH_TRY(fsph_get_array(c, FSPH_ATTRIBUTE, ha.data(), FSPH_HOST, nullptr));
         }
         int n = c->n;
         FSPH_TRY(alloc_particles(c, p->max_particles));
         c->n = 0;
         FSPH_TRY(load_particles(c, (const float *)hp.data(), (const float *)hv.data(), n, FSPH_HOST));
+        if (n) {
+            FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, ha.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+            FSPH_TRY(repartition(c));
+        }
     }
     FSPH_TRY(alloc_grid(c));
     FSPH_TRY(boundary_build(c)); /* the boundary's cell table follows the grid */
@@ -951,28 +1050,7 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
     int n = c->n;
     /* bring the home arrays to particle order (once after a step), then
      * overwrite the range */
-    if (!c->home_identity) {
-        launch_unsort4(n, c->set[0].id, c->set[0].pos, c->set[1].pos, 0, s);
-        launch_unsort4(n, c->set[0].id, c->set[0].vel, c->set[1].vel, 0, s);
-        launch_unsort1(n, c->set[0].id, c->set[0].attr, c->set[1].attr, s);
-        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos, c->set[1].pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
-        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel, c->set[1].vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
-        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, c->set[1].attr, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-        /* the warm-start history (step corrections, features) follows the particles */
-        launch_unsort4(n, c->set[0].id, c->dstep, c->tmp4, 0, s);
-        FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, c->tmp4, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
-        /* the last step's other results (density, lambda, forces, ...) stay
-         * in its slot order, which res_id keeps for the getters */
-        FSPH_CUDA(c, cudaMemcpyAsync(c->res_id, c->set[0].id, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-        c->res_in_res_id = true;
-        {
-            float4 *tf = reinterpret_cast<float4 *>(c->nl.list); /* lists are rebuilt by every step */
-            launch_unsort_rows(n, c->set[0].id, reinterpret_cast<const float4 *>(c->feat), tf, kFeatures / 4, s);
-            FSPH_CUDA(c, cudaMemcpyAsync(c->feat, tf, (size_t)n * kFeatures * 4, cudaMemcpyDeviceToDevice, s));
-        }
-        launch_iota(n, c->set[0].id, s);
-        c->home_identity = true;
-    }
+    FSPH_TRY(home_to_particle_order(c));
     cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (type == FSPH_POSITION || type == FSPH_VELOCITY) {
         /* staged and checked before it replaces anything: a range with a
@@ -992,6 +1070,8 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
     }
     FSPH_TRY(check_launch(c));
     FSPH_CUDA(c, cudaStreamSynchronize(s));
+    /* an attribute of -1 deletes a particle, another value revives one */
+    if (type == FSPH_ATTRIBUTE) FSPH_TRY(repartition(c));
     return FSPH_OK;
 }
 
@@ -999,6 +1079,10 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
     if (!c) return FSPH_INVALID_ARG;
     if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
+    if (c->n_active <= 0) { /* every particle deleted: nothing moves */
+        if (stats) std::memset(stats, 0, sizeof(*stats));
+        return FSPH_OK;
+    }
     cudaStream_t user = (cudaStream_t)stream;
     cudaEvent_t ev = nullptr;
     if (user && user != c->stream) {
@@ -1009,26 +1093,33 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
     }
     if (c->P.solver == FSPH_SOLVER_PBF && c->P.warm_start == 1 && !c->model_loaded)
         return fail(c, FSPH_UNSUPPORTED, "warm_start = 1 needs a network (fsph_set_warm_start_model)");
-    DevParams p = dev_for(c, c->n, dt);
+    DevParams p = dev_for(c, c->n_active, dt);
     c->dp = p;
     c->home_identity = false; /* the step leaves the home set in cell order */
     c->res_in_res_id = false;
     c->last_step_graph = c->P.use_graph != 0;
     if (c->P.solver == FSPH_SOLVER_WCSPH) {
         if (c->P.use_graph) {
-            if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n) FSPH_TRY(build_sph_graph(c, p));
+            if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n_active) FSPH_TRY(build_sph_graph(c, p));
             FSPH_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
         } else {
             FSPH_TRY(sph_step(c, p));
         }
     } else if (c->P.use_graph) {
-        if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n) FSPH_TRY(build_pbf_graph(c, p));
+        if (!c->graph_valid || c->graph_dt != dt || c->graph_n != c->n_active) FSPH_TRY(build_pbf_graph(c, p));
         FSPH_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
     } else {
         FSPH_TRY(pbf_step_eager(c, p));
     }
     FSPH_TRY(check_launch(c));
     FSPH_CUDA(c, cudaMemcpyAsync(c->ctl_host, c->ctl, sizeof(DevCtl), cudaMemcpyDeviceToHost, c->stream));
+    if (!c->del_regions.empty()) {
+        /* deletion regions (checkDeletePB after the position update,
+         * rx_sph_gpu.cpp:875-890): the deleted particles leave the active part */
+        launch_delete_regions(c->n_active, c->set[0].pos, c->set[0].vel, c->set[0].attr, c->del_dev,
+                              (int)(c->del_regions.size() / 2), c->stream);
+        FSPH_TRY(repartition(c));
+    }
     if (ev) {
         FSPH_CUDA(c, cudaEventRecord(ev, c->stream));
         FSPH_CUDA(c, cudaStreamWaitEvent(user, ev, 0));
@@ -1251,7 +1342,7 @@ int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const doub
     if (tot > (1ll << 31)) return fail(c, FSPH_INVALID_ARG, "more than 2^31 lattice nodes");
     cudaStream_t s = c->stream;
     float *dout = where == FSPH_DEVICE ? out : nullptr;
-    if (c->n == 0) { /* no particles: an empty field */
+    if (c->n_active == 0) { /* no particles: an empty field */
         if (where == FSPH_HOST) std::memset(out, 0, (size_t)tot * sizeof(float));
         else FSPH_CUDA(c, cudaMemsetAsync(out, 0, (size_t)tot * sizeof(float), s));
         FSPH_CUDA(c, cudaStreamSynchronize(s));
@@ -1264,7 +1355,7 @@ int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const doub
         lo[a] = c->P.box_min[a] - 0.5 * 0.01 * size;
         hi[a] = lo[a] + size * (1.0 + 0.01);
     }
-    DevParams p = dev_for(c, c->n, 1.0f);
+    DevParams p = dev_for(c, c->n_active, 1.0f); /* the deleted particles are parked far away */
     FSPH_TRY(build_on(c, p, c->set[0].pos));
     if (!dout) FSPH_CUDA(c, cudaMallocAsync((void **)&dout, (size_t)tot * sizeof(float), s));
     launch_density_grid(p, c->cell_start, c->set[1].pos, nn, minp, d, lo, hi, dout, s);
@@ -1279,11 +1370,11 @@ int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const doub
 
 int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {
     if (!c) return FSPH_INVALID_ARG;
-    if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
+    if (c->n_active <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
     cudaStream_t user = (cudaStream_t)stream;
     if (user && user != c->stream) FSPH_CUDA(c, cudaStreamSynchronize(user));
-    DevParams p = dev_for(c, c->n, dt);
+    DevParams p = dev_for(c, c->n_active, dt);
     cudaStream_t s = c->stream;
     FSPH_CUDA(c, cudaStreamSynchronize(s));
     /* results keep the sorted order of this evaluation (res_id); the
@@ -1441,13 +1532,146 @@ int fsph_clear_obstacles(fsph_ctx *c) {
 
 int fsph_num_obstacles(const fsph_ctx *c) { return c ? (int)(c->boxes.size() + c->spheres.size()) : -1; }
 
+int fsph_num_active(const fsph_ctx *c) { return c ? c->n_active : -1; }
+
+int fsph_add_delete_region(fsph_ctx *c, const double *lo, const double *hi) {
+    if (!c || !lo || !hi) return FSPH_INVALID_ARG;
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(lo[a]) || !std::isfinite(hi[a])) return fail(c, FSPH_INVALID_ARG, "region: finite corners");
+    if (c->del_regions.size() >= 2 * 64) return fail(c, FSPH_INVALID_ARG, "at most 64 deletion regions");
+    c->del_regions.push_back(make_float4((float)lo[0], (float)lo[1], (float)lo[2], 0.0f));
+    c->del_regions.push_back(make_float4((float)hi[0], (float)hi[1], (float)hi[2], 0.0f));
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!c->del_dev) FSPH_CUDA(c, cudaMalloc((void **)&c->del_dev, 2 * 64 * sizeof(float4)));
+    FSPH_CUDA(c, cudaMemcpy(c->del_dev, c->del_regions.data(), c->del_regions.size() * sizeof(float4),
+                            cudaMemcpyHostToDevice));
+    return FSPH_OK;
+}
+
+int fsph_clear_delete_regions(fsph_ctx *c) {
+    if (!c) return FSPH_INVALID_ARG;
+    c->del_regions.clear();
+    return FSPH_OK;
+}
+
+int fsph_add_inlet_line(fsph_ctx *c, const double *pos1, const double *pos2, const double *vel, const double *up,
+                        int accum, int span, double spacing) {
+    if (!c || !pos1 || !pos2 || !vel || !up) return FSPH_INVALID_ARG;
+    if (accum < 1 || span < 0 || !(spacing >= 0.0)) return fail(c, FSPH_INVALID_ARG, "inlet: accum >= 1, span >= 0");
+    fsph_ctx::Inlet q;
+    for (int a = 0; a < 3; ++a) {
+        q.pos1[a] = pos1[a]; q.pos2[a] = pos2[a]; q.vel[a] = vel[a]; q.up[a] = up[a];
+        if (!std::isfinite(pos1[a]) || !std::isfinite(pos2[a]) || !std::isfinite(vel[a]) || !std::isfinite(up[a]))
+            return fail(c, FSPH_INVALID_ARG, "inlet: finite vectors");
+    }
+    q.accum = accum; q.span = span; q.spacing = spacing;
+    c->inlets.push_back(q);
+    return (int)c->inlets.size();
+}
+
+int fsph_clear_inlets(fsph_ctx *c) {
+    if (!c) return FSPH_INVALID_ARG;
+    c->inlets.clear();
+    c->inlet_start = -1;
+    return FSPH_OK;
+}
+
+namespace {
+/* U[0, 1) from (seed, index): the SplitMix64 finaliser */
+double inlet_uniform(unsigned long long seed, unsigned long long idx) {
+    unsigned long long z = seed * 0x9E3779B97F4A7C15ull + idx * 0xD1B54A32D192ED03ull + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+}  // namespace
+
+int fsph_emit_inlets(fsph_ctx *c, int step, int *emitted) {
+    if (!c) return FSPH_INVALID_ARG;
+    if (emitted) *emitted = 0;
+    if (c->inlets.empty()) return FSPH_OK;
+    /* the particles of every line due at this step, in the reference's
+     * placement (addParticles, rx_ps.cpp:444-520): n = l / r along the line,
+     * at (i + 1/2) l / n from pos1, jitter 0.01 of the spacing, accum rows
+     * stacked along up by spacing * (l / n); attribute = the line's index */
+    std::vector<float4> px, pv;
+    std::vector<int> pa;
+    const double r = (double)c->P.particle_radius;
+    for (size_t li = 0; li < c->inlets.size(); ++li) {
+        const fsph_ctx::Inlet &q = c->inlets[li];
+        if (!(q.span > 0 && step % q.span == 0)) continue;
+        double rel[3], l = 0.0;
+        for (int a = 0; a < 3; ++a) { rel[a] = q.pos2[a] - q.pos1[a]; l += rel[a] * rel[a]; }
+        l = std::sqrt(l);
+        const int n = (int)(l / r);
+        if (n <= 0 || !(l > 0.0)) continue;
+        const double spacing = l / n, jitter = spacing * 0.01;
+        double p1[3] = {q.pos1[0], q.pos1[1], q.pos1[2]};
+        const unsigned long long seed = (unsigned long long)(li + 1) * 1000003ull + (unsigned long long)step;
+        for (int j = 0; j < q.accum; ++j) {
+            for (int i = 0; i < n; ++i) {
+                float x[3];
+                for (int a = 0; a < 3; ++a) {
+                    const double u = inlet_uniform(seed, 3ull * (px.size()) + (unsigned long long)a);
+                    x[a] = (float)(p1[a] + rel[a] / l * (i + 0.5) * spacing + (u * 2.0 - 1.0) * jitter);
+                }
+                px.push_back(make_float4(x[0], x[1], x[2], 0.0f));
+                pv.push_back(make_float4((float)q.vel[0], (float)q.vel[1], (float)q.vel[2], 0.0f));
+                pa.push_back((int)li);
+            }
+            for (int a = 0; a < 3; ++a) p1[a] += q.up[a] * q.spacing * spacing;
+        }
+    }
+    const int count = (int)px.size();
+    if (count == 0) return FSPH_OK;
+    /* the new particles go at the inlet index, after the existing ones at
+     * first, wrapping to 0 past max_particles (rx_ps.cpp:466-505) */
+    FSPH_TRY(home_to_particle_order(c));
+    cudaStream_t s = c->stream;
+    int index = c->inlet_start < 0 ? c->n : c->inlet_start;
+    const int n_old = c->n;
+    int n = c->n, done = 0;
+    bool over = false;
+    while (done < count) {
+        if (index >= c->cap) { index = 0; over = true; }
+        const int run = std::min(count - done, c->cap - index);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].pos + index, px.data() + done, (size_t)run * 16, cudaMemcpyHostToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].vel + index, pv.data() + done, (size_t)run * 16, cudaMemcpyHostToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr + index, pa.data() + done, (size_t)run * 4, cudaMemcpyHostToDevice, s));
+        FSPH_CUDA(c, cudaMemsetAsync(c->dstep + index, 0, (size_t)run * 16, s));
+        FSPH_CUDA(c, cudaMemsetAsync(c->feat + (size_t)index * kFeatures, 0, (size_t)run * kFeatures * 4, s));
+        if (index + run > n) { /* new slots: their ids continue the particle order */
+            launch_iota(index + run, c->set[0].id, s);
+            n = index + run;
+        }
+        index += run;
+        done += run;
+    }
+    if (over) n = c->cap;
+    if (c->res_in_res_id && n > n_old) {
+        /* the results' slot map covers the new particles too (they have no
+         * results yet): slot d -> particle d, so it stays a permutation */
+        launch_iota(n, c->perm, s);
+        FSPH_CUDA(c, cudaMemcpyAsync(c->res_id + n_old, c->perm + n_old, (size_t)(n - n_old) * 4,
+                                     cudaMemcpyDeviceToDevice, s));
+    }
+    c->n = n;
+    c->inlet_start = index;
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    FSPH_TRY(check_launch(c));
+    FSPH_TRY(repartition(c));
+    if (emitted) *emitted = count;
+    return FSPH_OK;
+}
+
 int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
     if (!c || !avg_ms || reps <= 0) return FSPH_INVALID_ARG;
-    if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
+    if (c->n_active <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     const bool sph_pass = pass == FSPH_PASS_SPH_DENSITY || pass == FSPH_PASS_SPH_FORCE;
     if (sph_pass != (c->P.solver == FSPH_SOLVER_WCSPH))
         return fail(c, FSPH_UNSUPPORTED, "this pass belongs to the other solver");
-    DevParams p = dev_for(c, c->n, c->dp.dt > 0.0f ? c->dp.dt : 1e-3f);
+    DevParams p = dev_for(c, c->n_active, c->dp.dt > 0.0f ? c->dp.dt : 1e-3f);
     cudaStream_t s = c->stream;
     if (sph_pass) {
         /* the state of a WCSPH step before its passes: grid on x, sorted x, v */

@@ -741,6 +741,53 @@ __global__ void k_nb_fill(DevParams p, const unsigned int *__restrict__ cell_sta
 }
 
 /* ======================================================================== */
+/* deletion regions and the active / parked partition                       */
+/* ======================================================================== */
+
+/* Particles strictly inside a region [lo, hi] (checkDeletePB,
+ * rx_pbdsph_kernel.cu:1171-1187) are deleted: attribute -1, parked at the
+ * reference's far point (0, 0, 1e6) with zero velocity. */
+__global__ void k_delete_regions(int n, float4 *__restrict__ pos, float4 *__restrict__ vel,
+                                 unsigned int *__restrict__ attr, const float4 *__restrict__ reg, int nreg) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n || attr[d] == 0xffffffffu) return;
+    const float4 x = pos[d];
+    for (int r = 0; r < nreg; ++r) {
+        const float4 lo = reg[2 * r], hi = reg[2 * r + 1];
+        if (x.x > lo.x && x.x < hi.x && x.y > lo.y && x.y < hi.y && x.z > lo.z && x.z < hi.z) {
+            pos[d] = make_float4(0.0f, 0.0f, 1e6f, 0.0f);
+            vel[d] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            attr[d] = 0xffffffffu;
+            return;
+        }
+    }
+}
+
+/* keep[d] = 1 for a particle that takes part in the steps (attribute != -1) */
+__global__ void k_mark_active(int n, const unsigned int *__restrict__ attr, unsigned int *__restrict__ keep) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < n) keep[d] = attr[d] != 0xffffffffu ? 1u : 0u;
+}
+
+/* stable partition, active slots first: perm[new slot] = old slot, from the
+ * exclusive scan of the keep flags (scan[n] = the active count) */
+__global__ void k_partition_perm(int n, const unsigned int *__restrict__ scan, unsigned int *__restrict__ perm) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    const unsigned int s = scan[d], keep = scan[d + 1] - s, nk = scan[n];
+    perm[keep ? s : nk + ((unsigned int)d - s)] = (unsigned int)d;
+}
+
+/* rows of k4 float4 per slot: dst[d] = src[perm[d]] */
+__global__ void k_gather_rows(int n, const unsigned int *__restrict__ perm, const float4 *__restrict__ src,
+                              float4 *__restrict__ dst, int k4) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * k4) return;
+    const long long d = t / k4, c = t % k4;
+    dst[t] = src[(long long)perm[d] * k4 + c];
+}
+
+/* ======================================================================== */
 /* density on a lattice (for meshing)                                       */
 /* ======================================================================== */
 
@@ -1016,6 +1063,19 @@ void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const f
 void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
                     const unsigned int *offsets, int *out, float *d2out, cudaStream_t s) {
     k_nb_fill<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, id, offsets, out, d2out);
+}
+void launch_delete_regions(int n, float4 *pos, float4 *vel, unsigned int *attr, const float4 *reg, int nreg,
+                           cudaStream_t s) {
+    if (n > 0 && nreg > 0) k_delete_regions<<<blocks_for(n), kBlock, 0, s>>>(n, pos, vel, attr, reg, nreg);
+}
+void launch_mark_active(int n, const unsigned int *attr, unsigned int *keep, cudaStream_t s) {
+    if (n > 0) k_mark_active<<<blocks_for(n), kBlock, 0, s>>>(n, attr, keep);
+}
+void launch_partition_perm(int n, const unsigned int *scan, unsigned int *perm, cudaStream_t s) {
+    if (n > 0) k_partition_perm<<<blocks_for(n), kBlock, 0, s>>>(n, scan, perm);
+}
+void launch_gather_rows(int n, const unsigned int *perm, const float4 *src, float4 *dst, int k4, cudaStream_t s) {
+    if (n > 0) k_gather_rows<<<blocks_for((long long)n * k4), kBlock, 0, s>>>(n, perm, src, dst, k4);
 }
 void launch_density_grid(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const int nn[3],
                          const double minp[3], const double d[3], const double lo[3], const double hi[3], float *out,

@@ -128,6 +128,14 @@ void launch_nb_count(const DevParams &p, const unsigned int *cell_start, const f
 void launch_nb_fill(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const unsigned int *id,
                     const unsigned int *offsets, int *out, float *d2out, cudaStream_t s);
 
+/* ---- deletion regions and the active / parked partition ---- */
+/* reg: nreg pairs (lo, hi) of float4 */
+void launch_delete_regions(int n, float4 *pos, float4 *vel, unsigned int *attr, const float4 *reg, int nreg,
+                           cudaStream_t s);
+void launch_mark_active(int n, const unsigned int *attr, unsigned int *keep, cudaStream_t s);
+void launch_partition_perm(int n, const unsigned int *scan, unsigned int *perm, cudaStream_t s);
+void launch_gather_rows(int n, const unsigned int *perm, const float4 *src, float4 *dst, int k4, cudaStream_t s);
+
 /* ---- density on a lattice (CalImplicitField) ---- */
 void launch_density_grid(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const int nn[3],
                          const double minp[3], const double d[3], const double lo[3], const double hi[3], float *out,

@@ -149,10 +149,40 @@ class rxParticleSystemBase:
 
     # -- step ------------------------------------------------------------
     def Update(self, dt: float, step: int = 0, stats: bool = True) -> bool:
-        """rxParticleSystemBase::Update (rx_ps.h:254): advance one step."""
+        """rxParticleSystemBase::Update (rx_ps.h:254): the inlet lines due at
+        `step` emit their particles (rx_sph_pbd_gpu.cpp:795-815), then one step."""
+        if getattr(self, "_inlets", 0):
+            self._check(self.L.fsph_emit_inlets(self._ctx, int(step), None), "fsph_emit_inlets")
         st = self.L.fsph_step(self._ctx, float(dt), None, ctypes.byref(self.last_stats) if stats else None)
         self._check(st, "fsph_step")
         return True
+
+    # -- dynamic particle count: inlets and deletion regions ---------------
+    def AddLine(self, pos1, pos2, vel, up, accum: int, span: int, spacing: float) -> int:
+        """An inlet line (rxInletLine / AddLine, rx_ps.h:41-49, rx_ps.cpp:432)."""
+        d = lambda v: np.ascontiguousarray(v, dtype=np.float64)  # noqa: E731
+        a, b, v, u = d(pos1), d(pos2), d(vel), d(up)
+        k = self.L.fsph_add_inlet_line(self._ctx, _ptr(a), _ptr(b), _ptr(v), _ptr(u), int(accum), int(span),
+                                       float(spacing))
+        if k <= 0:
+            self._check(k if k else abi.INVALID_ARG, "fsph_add_inlet_line")
+        self._inlets = k
+        return k
+
+    def EmitInlets(self, step: int) -> int:
+        """The particles of the inlet lines due at `step`; returns how many."""
+        n = ctypes.c_int(0)
+        self._check(self.L.fsph_emit_inlets(self._ctx, int(step), ctypes.byref(n)), "fsph_emit_inlets")
+        return n.value
+
+    def AddDeleteRegion(self, lo, hi):
+        """Particles strictly inside [lo, hi] at the end of a step are deleted
+        (attribute -1, parked far away; env.delete_region, rx_sph.h:125-126)."""
+        a, b = np.ascontiguousarray(lo, np.float64), np.ascontiguousarray(hi, np.float64)
+        self._check(self.L.fsph_add_delete_region(self._ctx, _ptr(a), _ptr(b)), "fsph_add_delete_region")
+
+    def GetNumActiveParticles(self) -> int:
+        return int(self.L.fsph_num_active(self._ctx))
 
     def Sync(self):
         self._check(self.L.fsph_sync(self._ctx), "fsph_sync")

@@ -230,6 +230,35 @@ int fsph_neighbors(fsph_ctx *ctx, int *offsets, int *indices, long long cap, lon
 int fsph_neighbors_ex(fsph_ctx *ctx, const float *pos4, int n, float radius, int where, int *offsets,
                       int *indices, float *dist2, long long cap, long long *total);
 
+/* ---- dynamic particle count: inlets and deletion regions ---- */
+/* A deleted particle keeps its index: attribute -1, parked at (0, 0, 1e6)
+ * with zero velocity (checkDeletePB, rx_pbdsph_kernel.cu:1171-1187), and
+ * takes no further part in the steps; fsph_num_particles counts it,
+ * fsph_num_active does not.  Writing an attribute of -1 through
+ * fsph_set_array deletes a particle the same way, another value revives it. */
+int fsph_num_active(const fsph_ctx *ctx);
+/* Particles strictly inside [lo, hi] at the end of a step are deleted (the
+ * reference applies its regions after the position update,
+ * rx_sph_gpu.cpp:875-890; env.delete_region, rx_sph.h:125-126).  At most 64. */
+int fsph_add_delete_region(fsph_ctx *ctx, const double *lo, const double *hi);
+int fsph_clear_delete_regions(fsph_ctx *ctx);
+/* An inlet line (rxInletLine / AddLine, rx_ps.h:41-49, rx_ps.cpp:432-436):
+ * when fsph_emit_inlets is called for a step with step % span == 0, the
+ * line adds accum rows of n = |pos2 - pos1| / r particles (r the particle
+ * radius), spaced l / n along it from (i + 1/2) l / n, jittered by 0.01 of
+ * that spacing, rows stacked along `up` by spacing * (l / n), with velocity
+ * vel and attribute = the line's index (addParticles, rx_ps.cpp:444-520).
+ * Returns the number of lines (> 0) or a negative status. */
+int fsph_add_inlet_line(fsph_ctx *ctx, const double *pos1, const double *pos2, const double *vel,
+                        const double *up, int accum, int span, double spacing);
+int fsph_clear_inlets(fsph_ctx *ctx);
+/* Emit the particles of the lines due at `step` (rxPBDSPH_GPU::Update,
+ * rx_sph_pbd_gpu.cpp:795-815, before the step): after the existing
+ * particles at first, then from where the last emission ended, wrapping to
+ * index 0 past max_particles as the reference does.  *emitted (optional)
+ * receives the count.  Synchronises. */
+int fsph_emit_inlets(fsph_ctx *ctx, int step, int *emitted);
+
 /* ---- density on a lattice, for surface meshing ---- */
 /* CalImplicitField / CalImplicitFieldDevice (rx_ps.h:283-285;
  * rxPBDSPH::CalImplicitField -> CalColorField, rx_sph_pbd.cpp:2024-2108;

@@ -74,6 +74,16 @@ struct Vec3 {
 };
 inline Vec3 operator*(double s, const Vec3 &a) { return a * s; }
 
+/* Inlet line (rx_ps.h:41-49). */
+struct rxInletLine {
+    Vec3 pos1, pos2;  /* end points */
+    Vec3 vel;         /* velocity of the added particles */
+    Vec3 up;          /* direction the rows pile up in */
+    int accum;        /* rows per emission */
+    int span;         /* steps between emissions */
+    double spacing;   /* row spacing, in particle spacings */
+};
+
 /* Neighbour record (rx_nnsearch.h:59-64). */
 struct rxNeigh {
     int Idx;
@@ -186,6 +196,9 @@ public:
         if (m_status != FSPH_OK) return;
         p.gravity[1] = m_gravity_y;
         create(p);
+        /* the deletion regions of the environment (rx_sph_pbd_gpu.cpp:264-271) */
+        for (int i = 0; m_ctx && i < env.use_delete_region && i < rxSPHEnviroment::MAX_DELETE_REGIONS; ++i)
+            fsph_add_delete_region(m_ctx, env.delete_region[i][0].data, env.delete_region[i][1].data);
     }
 
     bool IsInitialized() const { return m_ctx != nullptr; }
@@ -254,6 +267,23 @@ public:
         m_flags_dirty = true;
     }
     bool IsUseVorticity(void) const { return m_use_vorticity; }
+
+    /* -- inlets and deleted particles (rx_ps.h:304; rx_ps.cpp:432-520) ---- */
+    int AddLine(rxInletLine line) {
+        const int k = fsph_add_inlet_line(m_ctx, line.pos1.data, line.pos2.data, line.vel.data, line.up.data,
+                                          line.accum, line.span, line.spacing);
+        if (k > 0) m_inlets = k;
+        else m_status = k;
+        return k;
+    }
+    /* the particles that take part in the steps (deleted ones excluded) */
+    int GetNumActiveParticles() const { return m_ctx ? fsph_num_active(m_ctx) : 0; }
+    /* particles strictly inside [lo, hi] at the end of a step are deleted */
+    template <class V1, class V2>
+    void AddDeleteRegion(const V1 &lo, const V2 &hi) {
+        const Vec3 a(lo), b(hi);
+        m_status = fsph_add_delete_region(m_ctx, a.data, b.data);
+    }
 
     /* -- analytic obstacles (rx_ps.h:266-272; fsph_set_box_obstacle) ----- */
     template <class V1, class V2, class V3, class V4>
@@ -397,7 +427,12 @@ public:
 
 protected:
     /* -- step ---------------------------------------------------------- */
-    bool update_impl(RXREAL dt) {
+    bool update_impl(RXREAL dt, int step) {
+        /* the inlet lines due at this step first (rx_sph_pbd_gpu.cpp:795-815) */
+        if (m_ctx && m_inlets) {
+            m_status = fsph_emit_inlets(m_ctx, step, nullptr);
+            if (m_status != FSPH_OK) return false;
+        }
         if (!m_ctx || fsph_num_particles(m_ctx) == 0) return false;
         sync_flags();
         m_status = fsph_step(m_ctx, dt, nullptr, &m_stats);
@@ -442,6 +477,7 @@ protected:
     bool m_use_vorticity = false;
     bool m_artificial_pressure = true;
     bool m_flags_dirty = false;
+    int m_inlets = 0;
     uint64_t m_seed = 1;
 
     void create(const fsph_params &p) {
@@ -550,10 +586,7 @@ protected:
 class rxFsphSolver : public rxParticleSystemBase {
 public:
     using rxParticleSystemBase::rxParticleSystemBase;
-    bool Update(RXREAL dt, int step = 0) override {
-        (void)step;
-        return update_impl(dt);
-    }
+    bool Update(RXREAL dt, int step = 0) override { return update_impl(dt, step); }
     bool UpdateWithoutPosAndVel(RXREAL dt, int step = 0) override {
         (void)step;
         return fields_impl(dt);

@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_lambda(DevParams
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     float4 *pp = par ? ppos1 : ppos0;
     float e1 = 0.f, e2 = 0.f, em = 0.f;
-#if FSPH_PERSIST
+#if FSPH_PERSIST_LAMBDA
     /* persistent warps: warp w takes the 32-slot chunks w, w + W, ... in a
      * fixed order (the error sums stay deterministic) */
     const int lane = threadIdx.x & 31;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_correction(DevPa
     const float4 *__restrict__ src = par ? ppos1 : ppos0;
     float4 *__restrict__ dst = par ? ppos0 : ppos1;
     float disp2 = 0.f;
-#if FSPH_PERSIST
+#if FSPH_PERSIST_CORRECTION
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * 32 < p.n; c += nw) {
@@ -954,21 +954,25 @@ void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const f
 }
 /* blocks of a constraint-pass launch: one per kPassBlock slots, or (with
  * persistent warps) the resident blocks of the whole GPU, at most that */
-static unsigned int pass_blocks(int n, const void *kernel) {
+static unsigned int pass_blocks(int n, const void *kernel, bool persistent) {
     unsigned int b = blocks_for(n, kPassBlock);
-#if FSPH_PERSIST
-    static int resident = 0;
-    if (resident == 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kPassBlock, 0);
-        resident = std::max(1, sms * std::max(per, 1));
+    if (persistent) {
+        /* resident blocks of each pass kernel, looked up once */
+        static const void *known[4] = {nullptr, nullptr, nullptr, nullptr};
+        static int resident[4] = {0, 0, 0, 0};
+        int k = 0;
+        while (k < 4 && known[k] && known[k] != kernel) ++k;
+        if (k == 4) k = 3;
+        if (known[k] != kernel) {
+            int dev = 0, sms = 0, per = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kPassBlock, 0);
+            resident[k] = std::max(1, sms * std::max(per, 1));
+            known[k] = kernel;
+        }
+        b = std::min(b, (unsigned int)resident[k]);
     }
-    b = std::min(b, (unsigned int)resident);
-#else
-    (void)kernel;
-#endif
     return b;
 }
 
@@ -976,7 +980,7 @@ void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *p
                    DevCtl *ctl, ErrPartial *part, unsigned long long while_handle, int use_graph,
                    const NbrLists &nl, cudaStream_t s) {
     auto k = p.compensated ? k_lambda<true> : k_lambda<false>;
-    k<<<pass_blocks(p.n, (const void *)k), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
+    k<<<pass_blocks(p.n, (const void *)k, FSPH_PERSIST_LAMBDA != 0), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, dens, ctl, part,
                                          (cudaGraphConditionalHandle)while_handle, use_graph,
                                          p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
 }
@@ -989,7 +993,7 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
                        const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,
                        unsigned long long if_handle2, int use_graph, float4 *dp_out, const NbrLists &nl,
                        cudaStream_t s) {
-    k_correction<<<pass_blocks(p.n, (const void *)k_correction), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb,
+    k_correction<<<pass_blocks(p.n, (const void *)k_correction, FSPH_PERSIST_CORRECTION != 0), kPassBlock, 0, s>>>(p, cell_start, ppos0, ppos1, xb,
                                                                                     ctl, part,
                                                     (cudaGraphConditionalHandle)if_handle,
                                                     (cudaGraphConditionalHandle)if_handle2, use_graph, dp_out,

@@ -44,10 +44,18 @@ constexpr int kBatch = FSPH_KBATCH;
 #ifndef FSPH_FOLD
 #define FSPH_FOLD 0
 #endif
-/* FSPH_PERSIST 1: the single-scene constraint passes run as many blocks as
- * are resident on the GPU, each warp taking 32-slot chunks round-robin */
-#ifndef FSPH_PERSIST
-#define FSPH_PERSIST 0
+/* FSPH_PERSIST_LAMBDA / FSPH_PERSIST_CORRECTION 1: that single-scene
+ * constraint pass runs as many blocks as are resident on the GPU, each warp
+ * taking 32-slot chunks round-robin (FSPH_PERSIST sets both) */
+#ifdef FSPH_PERSIST
+#define FSPH_PERSIST_LAMBDA FSPH_PERSIST
+#define FSPH_PERSIST_CORRECTION FSPH_PERSIST
+#endif
+#ifndef FSPH_PERSIST_LAMBDA
+#define FSPH_PERSIST_LAMBDA 0
+#endif
+#ifndef FSPH_PERSIST_CORRECTION
+#define FSPH_PERSIST_CORRECTION 0
 #endif
 
 /* Neighbour-list loads do not allocate in L1 (ld.global.nc.L1::no_allocate):

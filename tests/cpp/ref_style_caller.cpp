@@ -10,6 +10,7 @@
  *
  *   ref_style_caller out.dat steps
  */
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -24,6 +25,11 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "usage: %s out.dat steps\n", argv[0]);
         return 2;
     }
+    const auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) { /* phase times on stderr */
+        std::fprintf(stderr, "%s %.3f s\n", what,
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    };
     rxParticleSystemBase *m_pPS = new RXSPH(true);
 
     // InitSPH: the scene's environment, then Initialize
@@ -45,6 +51,7 @@ int main(int argc, char **argv) {
         return 1;
     }
     const double m_fDt = sph_env.dt;
+    lap("initialized");
     m_pPS->ToggleUseVorticity(0);
     m_pPS->Reset(rxParticleSystemBase::RX_CONFIG_NONE);
 
@@ -54,6 +61,7 @@ int main(int argc, char **argv) {
     m_pPS->AddBox(-1, cen, Vec3(0.08, 0.08, 0.08), Vec3(0.0), pr * 2.0f);
     const int n0 = m_pPS->GetNumParticles();
     if (n0 <= 0) { std::fprintf(stderr, "AddBox placed no particles\n"); return 1; }
+    lap("scene placed");
 
     // StepPS
     const int steps = std::atoi(argv[2]);
@@ -69,6 +77,7 @@ int main(int argc, char **argv) {
         }
     }
 
+    lap("stepped");
     // neighbour lists of the current positions
     m_pPS->SetParticlesToCell();
     const std::vector<std::vector<rxNeigh> > &nb = ((RXSPH *)m_pPS)->GetNeights();
@@ -77,7 +86,7 @@ int main(int argc, char **argv) {
     for (const std::vector<rxNeigh> &row : nb)
         for (const rxNeigh &q : row) {
             ++total;
-            worst = std::fmax(worst, std::fabs((double)q.Dist * q.Dist - q.Dist2));
+            worst = std::fmax(worst, std::fabs((double)q.Dist * q.Dist - q.Dist2) / std::fmax(q.Dist2, 1e-30f));
         }
 
     // the fields of a step without moving the particles
@@ -92,6 +101,7 @@ int main(int argc, char **argv) {
         rmax = std::fmax(rmax, (double)rho[i]);
     }
 
+    lap("neighbours and fields");
     // the particle file
     if (!m_pPS->OutputParticles(argv[1])) { std::fprintf(stderr, "OutputParticles failed\n"); return 1; }
     std::printf("particles %d max %d neighbours %zu dist_check %.3e unmoved %d density %.3f %.3f dim %.3f %.3f %.3f\n",

@@ -76,11 +76,30 @@ def assert_sets_equal(off_a, idx_a, off_b, idx_b):
         f"{len(np.unique(ra[ca != cb]))} particles with different neighbour sets"
 
 
-def assert_step_equal(gpu, ref, x0g, x0r, what):
+def density_sensitivity(x, dx, p):
+    """sum_j m |dW/dr(r_ij)| (dx_i + dx_j) per particle (FP64, over the
+    neighbours within h): how far densities move when the particles move by
+    dx, the bound on what a difference in the state a step starts from
+    carries into its densities."""
+    n = x.shape[0]
+    o = oracle.Oracle(p, n, threads=4)
+    off, idx = o.neighbors(np.ascontiguousarray(x, np.float32))
+    rows = np.repeat(np.arange(n), np.diff(off))
+    h = float(np.float32(p.h))
+    aw = 315.0 / (64.0 * np.pi * h ** 9)
+    d = x[rows, :3].astype(np.float64) - x[idx, :3].astype(np.float64)
+    r = np.sqrt((d * d).sum(1))
+    wp = 6.0 * aw * r * np.maximum(h * h - r * r, 0.0) ** 2
+    return np.bincount(rows, weights=float(np.float32(p.mass)) * wp * (dx[rows] + dx[idx]), minlength=n)
+
+
+def assert_step_equal(gpu, ref, x0g, x0r, what, p=None):
     """One step's results from the two sides' start positions x0g / x0r
     (equal for a first step, else apart by what earlier steps left): the
     position change (element-wise, with one storage ulp of each position and
-    the start difference), velocity (the same over dt) and density."""
+    the start difference), velocity (the same over dt) and density
+    (element-wise 1e-5, plus, after a first step, what the position
+    differences carry: density_sensitivity)."""
     xg, xr = gpu.GetArrayVBO(abi.RX_POSITION)[:, :3], ref.get("pos")[:, :3]
     x0g = np.asarray(x0g, np.float64)[:, :3]
     x0r = np.asarray(x0r, np.float64)[:, :3]
@@ -89,7 +108,20 @@ def assert_step_equal(gpu, ref, x0g, x0r, what):
     vg, vr = gpu.GetArrayVBO(abi.RX_VELOCITY)[:, :3], ref.get("vel")[:, :3]
     assert_close(vg, vr, f"{what}: velocity", atol=carried / PBF_DT)
     dg, dr = gpu.GetArrayVBO(abi.RX_DENSITY), ref.get("dens")
-    assert_close(dg, dr, f"{what}: density", etol=1e-5, floor=0.0)
+    atol = None
+    if p is not None and not np.array_equal(x0g, x0r):
+        dx = np.maximum(np.linalg.norm(xg - xr.astype(np.float64), axis=1), np.linalg.norm(x0g - x0r, axis=1))
+        atol = 2.0 * density_sensitivity(xr, dx, p)
+    assert_close(dg, dr, f"{what}: density", etol=1e-5, floor=0.0, atol=atol)
+
+
+def ref_mean_error(ref, p):
+    """The reference's two-sided mean density error from its own densities,
+    summed in double: its loop sums it in float (dens_var, rx_sph_pbd.cpp:
+    447-453), which at 1 M terms of ~0.2 is off by ~5e-4 relative (the
+    float sum reproduces the reported g_fEta bit for bit)."""
+    r0 = float(np.float32(p.rest_dens))
+    return float(np.mean(np.abs(ref.get("dens").astype(np.float64) - r0) / r0))
 
 
 EPS32 = float(np.finfo(np.float32).eps)
@@ -154,10 +186,11 @@ def steps_vs_reference(p, pos, vel, nsteps, what):
     for k in range(nsteps):
         x0g, x0r = g.GetArrayVBO(abi.RX_POSITION), r.get("pos")
         g.Update(PBF_DT)
-        it, eta = r.update(PBF_DT)
+        it, _ = r.update(PBF_DT)
+        eta = ref_mean_error(r, p)
         assert g.last_stats.iterations == 4 and it == 4
-        assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-4 * eta, (g.last_stats.density_error_two_sided, eta)
-        assert_step_equal(g, r, x0g, x0r, f"{what} step {k + 1}")
+        assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-5 * eta, (g.last_stats.density_error_two_sided, eta)
+        assert_step_equal(g, r, x0g, x0r, f"{what} step {k + 1}", p)
     g.close()
 
 
@@ -254,7 +287,8 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
     base = reference_setup(sc.params)
     r = oracle.RefSolver(base, sc.n, "pbf")
     r.set(x, v)
-    it, eta = r.update(PBF_DT)
+    it, _ = r.update(PBF_DT)
+    eta = ref_mean_error(r, base)
     assert it == 4
     for skin, rebuilds in ((0.1, False), (0.005, True)):
         p = abi.FsphParams.from_buffer_copy(base)
@@ -265,7 +299,7 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
         assert g.last_stats.iterations == 4
         if rebuilds:
             assert g.last_stats.grid_builds > 1, g.last_stats.grid_builds
-        assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-4 * eta
+        assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-5 * eta
         assert_step_equal(g, r, x, x, f"1M, skin {skin}")
         g.close()
 

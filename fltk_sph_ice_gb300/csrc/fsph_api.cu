@@ -19,8 +19,11 @@
  *   - no GL buffers and no CPU neighbour mirror (rx_sph_pbd_gpu.cpp:962-1011).
  */
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,6 +39,26 @@ using namespace fsph;
 
 namespace {
 const double kPi = 3.14159265358979323846;
+
+/* NVTX range for the duration of a scope (seen by ncu / Nsight; free when
+ * no tool is attached) */
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
+/* device-allocation fault injection (test hook, process-wide): an
+ * allocation larger than g_alloc_max_bytes (>= 0), or the allocation
+ * numbered g_alloc_fail_at (counted from the last fsph_set_alloc_fault),
+ * returns FSPH_OOM without calling cudaMalloc */
+std::atomic<long long> g_alloc_max_bytes{-1};
+std::atomic<long long> g_alloc_fail_at{-1};
+std::atomic<long long> g_alloc_count{0};
+bool alloc_faulted(size_t bytes) {
+    const long long k = g_alloc_count.fetch_add(1);
+    const long long mx = g_alloc_max_bytes.load();
+    return (mx >= 0 && (long long)bytes > mx) || k == g_alloc_fail_at.load();
+}
 }
 
 struct BufSet {
@@ -113,6 +136,13 @@ struct fsph_ctx {
     int nobs_dev = 0;
     bool last_step_graph = false;
     bool stats_pending = false;
+    /* per-step JSON-lines record (fsph_set_step_log) */
+    FILE *log = nullptr;
+    long long steps_done = 0;
+    /* set when a reallocation failed part-way: the buffers are incomplete
+     * and every call that touches them is refused until fsph_set_params
+     * reallocates successfully */
+    bool broken = false;
     std::string err;
 };
 
@@ -137,6 +167,13 @@ int fail(fsph_ctx *c, int st, const std::string &msg) {
     if (c) c->err = msg;
     return st;
 }
+
+#define FSPH_USABLE(c)                                                                                       \
+    do {                                                                                                     \
+        if (!(c)) return FSPH_INVALID_ARG;                                                                   \
+        if ((c)->broken)                                                                                     \
+            return fail((c), FSPH_OOM, "buffers lost in a failed reallocation; call fsph_set_params again"); \
+    } while (0)
 
 /* ---------------- parameters ---------------- */
 
@@ -234,6 +271,7 @@ template <class T>
 int dalloc(fsph_ctx *c, T **p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
+    if (alloc_faulted(count * sizeof(T))) return fail(c, FSPH_OOM, "device allocation refused (injected fault)");
     FSPH_CUDA(c, cudaMalloc((void **)p, count * sizeof(T)));
     return FSPH_OK;
 }
@@ -531,7 +569,12 @@ void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
 
 int pbf_step_eager(fsph_ctx *c, const DevParams &p) {
     cudaStream_t s = c->stream;
-    int it = enqueue_pbf_pre(c, p, s);
+    int it;
+    {
+        NvtxRange r("pbf_predict_and_grid");
+        it = enqueue_pbf_pre(c, p, s);
+    }
+    NvtxRange r("pbf_constraint_loop");
     for (int k = 0;; ++k) {
         launch_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->dens, c->ctl, c->epart, 0ull, 0, c->nl, s);
         launch_boundary_lambda(p, c->cell_start, c->ppos[0], c->ppos[1], c->ctl, c->b_stat, c->b_lam, s);
@@ -758,6 +801,7 @@ int home_to_particle_order(fsph_ctx *c) {
  * (they take part in the steps), deleted ones after; n_active follows.
  * Synchronises. */
 int repartition(fsph_ctx *c) {
+    NvtxRange range("fsph_repartition");
     const int n = c->n;
     cudaStream_t s = c->stream;
     if (n > 0) {
@@ -960,6 +1004,7 @@ int fsph_create(const fsph_params *params, fsph_ctx **out) {
 int fsph_destroy(fsph_ctx *c) {
     if (!c) return FSPH_INVALID_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->log) std::fclose(c->log);
     drop_graph(c);
     free_particles(c);
     free_grid(c);
@@ -985,11 +1030,14 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
     int st = validate(*p, why);
     if (st != FSPH_OK) return fail(c, st, why);
     FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
-    int old_cap = c->P.max_particles;
+    const bool rebuild = c->broken; /* a failed reallocation lost the particles */
+    if (rebuild) c->n = c->n_active = 0;
+    if (!rebuild && p->max_particles != c->P.max_particles && c->n > p->max_particles)
+        return fail(c, FSPH_INVALID_ARG, "max_particles below the current particle count");
+    const int old_cap = c->P.max_particles;
     c->P = *p;
     drop_graph(c);
-    if (p->max_particles != old_cap) {
-        if (c->n > p->max_particles) return fail(c, FSPH_INVALID_ARG, "max_particles below the current particle count");
+    if (rebuild || p->max_particles != old_cap) {
         /* keep the particles across the reallocation */
         std::vector<float4> hp((size_t)c->n), hv((size_t)c->n);
         std::vector<int> ha((size_t)c->n);
@@ -999,6 +1047,7 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
             FSPH_TRY(fsph_get_array(c, FSPH_ATTRIBUTE, ha.data(), FSPH_HOST, nullptr));
         }
         int n = c->n;
+        c->broken = true; /* until every buffer is in place again */
         FSPH_TRY(alloc_particles(c, p->max_particles));
         c->n = 0;
         FSPH_TRY(load_particles(c, (const float *)hp.data(), (const float *)hv.data(), n, FSPH_HOST));
@@ -1007,9 +1056,11 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
             FSPH_TRY(repartition(c));
         }
     }
+    c->broken = true;
     FSPH_TRY(alloc_grid(c));
     FSPH_TRY(boundary_build(c)); /* the boundary's cell table follows the grid */
     FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->broken = false;
     return FSPH_OK;
 }
 
@@ -1023,6 +1074,7 @@ int fsph_num_particles(const fsph_ctx *c) { return c ? c->n : -1; }
 
 int fsph_set_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n, int where) {
     if (!c) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (n < 0 || n > c->cap) return fail(c, FSPH_INVALID_ARG, "particle count outside [0, max_particles]");
     if (n > 0 && !pos4) return fail(c, FSPH_INVALID_ARG, "null positions");
     if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
@@ -1042,6 +1094,7 @@ int fsph_set_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n,
 
 int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count, int where) {
     if (!c || !data) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (start < 0 || count < 0 || count > c->n - start) return fail(c, FSPH_INVALID_ARG, "range outside [0, n)");
     if (type != FSPH_POSITION && type != FSPH_VELOCITY && type != FSPH_ATTRIBUTE)
         return fail(c, FSPH_INVALID_ARG, "settable arrays: POSITION, VELOCITY, ATTRIBUTE");
@@ -1077,6 +1130,13 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
 
 int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
     if (!c) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
+    NvtxRange range("fsph_step");
+    if (c->log && !stats) { /* the record needs the stats of every step */
+        fsph_step_stats own;
+        return fsph_step(c, dt, stream, &own);
+    }
+    const auto t_start = std::chrono::steady_clock::now();
     if (c->n <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
     if (c->n_active <= 0) { /* every particle deleted: nothing moves */
@@ -1125,11 +1185,41 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
         FSPH_CUDA(c, cudaStreamWaitEvent(user, ev, 0));
         cudaEventDestroy(ev);
     }
+    ++c->steps_done;
     if (stats) {
         FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
         fill_stats(c, stats);
+        if (c->log) {
+            const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+            std::fprintf(c->log,
+                         "{\"step\": %lld, \"solver\": \"%s\", \"dt\": %.9g, \"n\": %d, \"n_active\": %d, "
+                         "\"iterations\": %d, \"grid_builds\": %d, \"density_error\": %.9g, "
+                         "\"density_error_one_sided\": %.9g, \"density_error_two_sided\": %.9g, "
+                         "\"density_error_max\": %.9g, \"status\": \"%s\", \"host_ms\": %.4f}\n",
+                         c->steps_done - 1, c->P.solver == FSPH_SOLVER_PBF ? "pbf" : "wcsph", (double)dt, c->n,
+                         c->n_active, stats->iterations, stats->grid_builds, (double)stats->density_error,
+                         (double)stats->density_error_one_sided, (double)stats->density_error_two_sided,
+                         (double)stats->density_error_max, fsph_status_string(stats->status), ms);
+            std::fflush(c->log);
+        }
         if (stats->status == FSPH_NAN_DETECTED) return fail(c, FSPH_NAN_DETECTED, "NaN in density or position");
     }
+    return FSPH_OK;
+}
+
+int fsph_set_step_log(fsph_ctx *c, const char *path) {
+    if (!c) return FSPH_INVALID_ARG;
+    if (c->log) { std::fclose(c->log); c->log = nullptr; }
+    if (!path || !*path) return FSPH_OK;
+    c->log = std::fopen(path, "a");
+    if (!c->log) return fail(c, FSPH_INVALID_ARG, std::string("cannot open ") + path);
+    return FSPH_OK;
+}
+
+int fsph_set_alloc_fault(long long max_bytes, long long fail_at) {
+    g_alloc_max_bytes = max_bytes;
+    g_alloc_fail_at = fail_at;
+    g_alloc_count = 0;
     return FSPH_OK;
 }
 
@@ -1148,6 +1238,7 @@ int fsph_sync(fsph_ctx *c) {
 
 int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
     if (!c || !dst) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
     int n = c->n;
     if (n == 0) return FSPH_OK;
@@ -1242,6 +1333,7 @@ const void *fsph_device_ptr(fsph_ctx *c, int type) {
 int fsph_neighbors_ex(fsph_ctx *c, const float *pos4, int n, float radius, int where, int *offsets, int *indices,
                       float *dist2, long long cap, long long *total) {
     if (!c || !offsets || !total) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     *total = 0;
     if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
     const bool given = pos4 != nullptr;
@@ -1334,6 +1426,7 @@ int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long 
 
 int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const double *d, float *out, int where) {
     if (!c || !nn || !minp || !d || !out) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
     for (int a = 0; a < 3; ++a)
         if (nn[a] <= 0 || !std::isfinite(minp[a]) || !std::isfinite(d[a]))
@@ -1370,6 +1463,7 @@ int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const doub
 
 int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {
     if (!c) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (c->n_active <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
     cudaStream_t user = (cudaStream_t)stream;
@@ -1423,6 +1517,7 @@ int fsph_set_warm_start_model(fsph_ctx *c, const float *blob) {
 
 int fsph_set_boundary(fsph_ctx *c, const float *bpos4, int nb, int where) {
     if (!c || nb < 0 || (nb > 0 && !bpos4)) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
     if (nb > 0 && c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "boundary particles: PBF only");
     FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1444,11 +1539,14 @@ int fsph_set_boundary(fsph_ctx *c, const float *bpos4, int nb, int where) {
         return fail(c, FSPH_NAN_DETECTED, "non-finite boundary position");
     }
     c->nb = nb;
-    return boundary_build(c);
+    const int st = boundary_build(c);
+    if (st != FSPH_OK) free_boundary(c);
+    return st;
 }
 
 int fsph_get_boundary(fsph_ctx *c, int which, float *dst) {
     if (!c || !dst) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     const int nb = c->nb;
     if (nb == 0) return FSPH_OK;
     cudaStream_t s = c->stream;
@@ -1589,6 +1687,8 @@ double inlet_uniform(unsigned long long seed, unsigned long long idx) {
 
 int fsph_emit_inlets(fsph_ctx *c, int step, int *emitted) {
     if (!c) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
+    NvtxRange range("fsph_emit_inlets");
     if (emitted) *emitted = 0;
     if (c->inlets.empty()) return FSPH_OK;
     /* the particles of every line due at this step, in the reference's
@@ -1667,6 +1767,7 @@ int fsph_emit_inlets(fsph_ctx *c, int step, int *emitted) {
 
 int fsph_time_pass(fsph_ctx *c, int pass, int reps, float *avg_ms) {
     if (!c || !avg_ms || reps <= 0) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (c->n_active <= 0) return fail(c, FSPH_INVALID_ARG, "no particles");
     const bool sph_pass = pass == FSPH_PASS_SPH_DENSITY || pass == FSPH_PASS_SPH_FORCE;
     if (sph_pass != (c->P.solver == FSPH_SOLVER_WCSPH))
@@ -1787,6 +1888,7 @@ int fsph_pbf_eval_correction(fsph_ctx *c, const float *pos4, const float *lambda
 int fsph_pbf_eval_xsph_vorticity(fsph_ctx *c, const float *pos4, const float *vel4, const float *dens, int n,
                                  float dt, float *vel_out4, float *vort4) {
     if (!c || !pos4 || !vel4 || !dens || !vel_out4 || !vort4) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     if (c->P.solver != FSPH_SOLVER_PBF) return fail(c, FSPH_UNSUPPORTED, "XSPH / vorticity: PBF only");
     if (!(dt > 0.0f) || !std::isfinite(dt)) return fail(c, FSPH_INVALID_ARG, "dt must be positive and finite");
     FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
@@ -1826,6 +1928,7 @@ int fsph_pbf_eval_xsph_vorticity(fsph_ctx *c, const float *pos4, const float *ve
 int fsph_sph_eval_forces(fsph_ctx *c, const float *pos4, const float *vel4, int n, float *dens, float *pres,
                          float *acc4) {
     if (!c || !pos4 || !dens || !pres || !acc4) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
     FSPH_TRY(fsph_set_particles(c, pos4, vel4, n, FSPH_HOST));
     if (n == 0) return FSPH_OK;
     DevParams p = dev_for(c, n, 1.0f);

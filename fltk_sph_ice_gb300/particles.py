@@ -184,6 +184,10 @@ class rxParticleSystemBase:
     def GetNumActiveParticles(self) -> int:
         return int(self.L.fsph_num_active(self._ctx))
 
+    def SetStepLog(self, path: str | None):
+        """Append one JSON line per step to `path` (None stops the log)."""
+        self._check(self.L.fsph_set_step_log(self._ctx, path.encode() if path else None), "fsph_set_step_log")
+
     def Sync(self):
         self._check(self.L.fsph_sync(self._ctx), "fsph_sync")
 

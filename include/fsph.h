@@ -417,6 +417,20 @@ int fsph_mlp_train(fsph_mlp *m, const float *x, const float *t, int n, int batch
 /* Install a trained blob (host) as the context's warm-start network. */
 int fsph_set_warm_start_model(fsph_ctx *ctx, const float *blob);
 
+/* ---- records and test hooks ---- */
+/* Append one JSON line per step to `path` (NULL or "" stops): step number,
+ * solver, dt, particle counts, iterations, grid builds, the three density
+ * errors, status and the host-timed step in ms.  While a log is open every
+ * step waits for its stats.  The reference's per-step figures were the
+ * globals g_iIterations / g_fEta (rx_sph_pbd.cpp:461-462) and RXTIMER prints. */
+int fsph_set_step_log(fsph_ctx *ctx, const char *path);
+/* Device-allocation fault injection, process-wide, for testing the error
+ * paths: allocations larger than max_bytes (>= 0) and the allocation
+ * numbered fail_at (0 = the next one; < 0 never) fail with FSPH_OOM without
+ * calling cudaMalloc.  fsph_set_alloc_fault(-1, -1) switches it off.
+ * No counterpart in the reference. */
+int fsph_set_alloc_fault(long long max_bytes, long long fail_at);
+
 /* ---- measurement ---- */
 typedef enum fsph_pass {
     FSPH_PASS_LAMBDA = 0,      /* one lambda pass (density + constraint + error reduction) */

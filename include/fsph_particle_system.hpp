@@ -421,6 +421,11 @@ public:
     int GetIterations() const { return m_stats.iterations; }
     float GetDensityError() const { return m_stats.density_error; }
     const fsph_step_stats &GetStepStats() const { return m_stats; }
+    /* one JSON line per step appended to `path` (nullptr stops) */
+    bool SetStepLog(const char *path) {
+        m_status = m_ctx ? fsph_set_step_log(m_ctx, path) : FSPH_NOT_INITIALIZED;
+        return m_status == FSPH_OK;
+    }
     fsph_ctx *Context() { return m_ctx; }
 
     static constexpr float kDefaultVorticityEps = 1e-4f;

@@ -1424,6 +1424,76 @@ int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long 
     return fsph_neighbors_ex(c, nullptr, 0, 0.0f, FSPH_HOST, offsets, indices, nullptr, cap, total);
 }
 
+/* The reference's neighbour-search grid over the simulation range (the box
+ * grown by 1 %, rx_sph_pbd.cpp:188-196): cw = L_max / 2^round(log2(L_max/h))
+ * for both; the CPU grid (rxNNGrid::Setup, rx_nnsearch.h:174-199) rounds each
+ * axis count to a power of two, the GPU grid (setupCells,
+ * rx_sph_pbd_gpu.cpp:1986-2011) takes floor(L_axis / cw) + 1.  The same
+ * double operations in the same order, so the same bits. */
+int reference_grid(const fsph_params &P, int rule, double org[3], double &cw, int g[3]) {
+    double lo[3], hi[3], ws[3];
+    for (int a = 0; a < 3; ++a) {
+        const double size = P.box_max[a] - P.box_min[a];
+        lo[a] = P.box_min[a] - 0.5 * 0.01 * size;
+        hi[a] = lo[a] + size * (1.0 + 0.01);
+    }
+    for (int a = 0; a < 3; ++a) ws[a] = hi[a] - lo[a];
+    const double h = (double)P.h;
+    const double max_axis = std::max(ws[0], std::max(ws[1], ws[2]));
+    const int d = (int)(std::log(max_axis / h) / std::log(2.0) + 0.5);
+    const int m = (int)(std::pow(2.0, (double)d) + 0.5);
+    if (m <= 0) return FSPH_INVALID_ARG;
+    cw = max_axis / m;
+    for (int a = 0; a < 3; ++a) {
+        org[a] = lo[a];
+        if (rule == 0) {
+            const int da = (int)(std::log(ws[a] / cw) / std::log(2.0) + 0.5);
+            g[a] = (int)(std::pow(2.0, (double)da) + 0.5);
+        } else {
+            g[a] = (int)(ws[a] / cw) + 1;
+        }
+        if (g[a] < 1) return FSPH_INVALID_ARG;
+    }
+    if ((double)g[0] * g[1] * g[2] > 4294967295.0) return FSPH_INVALID_ARG;
+    return FSPH_OK;
+}
+
+int fsph_reference_cell_hash(fsph_ctx *c, int rule, const float *pos4, int n, int where, unsigned int *hash,
+                             int *grid, double *cell_width) {
+    if (!c || n < 0 || (n > 0 && (!pos4 || !hash))) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
+    if (rule != 0 && rule != 1) return fail(c, FSPH_INVALID_ARG, "rule: 0 (CPU grid) or 1 (GPU grid)");
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    double org[3], cw;
+    int g[3];
+    if (reference_grid(c->P, rule, org, cw, g) != FSPH_OK)
+        return fail(c, FSPH_INVALID_ARG, "degenerate reference grid for this box and h");
+    if (grid) std::memcpy(grid, g, sizeof(g));
+    if (cell_width) *cell_width = cw;
+    if (n == 0) return FSPH_OK;
+    cudaStream_t s = c->stream;
+    const float4 *dpos = reinterpret_cast<const float4 *>(pos4);
+    unsigned int *dout = hash;
+    float4 *tpos = nullptr;
+    if (where == FSPH_HOST) {
+        FSPH_CUDA(c, cudaMallocAsync((void **)&tpos, (size_t)n * sizeof(float4), s));
+        FSPH_CUDA(c, cudaMallocAsync((void **)&dout, (size_t)n * sizeof(unsigned int), s));
+        FSPH_CUDA(c, cudaMemcpyAsync(tpos, pos4, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, s));
+        dpos = tpos;
+    }
+    launch_reference_cells(n, dpos, rule, org, cw, g, dout, s);
+    cudaError_t e = cudaGetLastError();
+    if (where == FSPH_HOST) {
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(hash, dout, (size_t)n * sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(tpos, s);
+        cudaFreeAsync(dout, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(c, FSPH_CUDA_ERROR, std::string("reference cell hash: ") + cudaGetErrorString(e));
+    return FSPH_OK;
+}
+
 int fsph_density_grid(fsph_ctx *c, const int *nn, const double *minp, const double *d, float *out, int where) {
     if (!c || !nn || !minp || !d || !out) return FSPH_INVALID_ARG;
     FSPH_USABLE(c);

@@ -1090,6 +1090,41 @@ void launch_density_grid(const DevParams &p, const unsigned int *cell_start, con
                                                       make_double3(d[0], d[1], d[2]), make_double3(lo[0], lo[1], lo[2]),
                                                       make_double3(hi[0], hi[1], hi[2]), out);
 }
+/* The reference's cell hash of each position (z Gy Gx + y Gx + x):
+ * rule 0 = its CPU grid (rxNNGrid::CalGridHash(Vec3), rx_nnsearch.h:590-599:
+ * (p - min) / cw in double, truncated to int, clamped to [0, G-1]);
+ * rule 1 = its GPU grid (calcGridPos / calcGridHash, rx_cu_common.cu:121-144:
+ * floor((p - origin) / cw) in float, clamped). */
+__global__ void __launch_bounds__(kBlock) k_reference_cells(int n, const float4 *__restrict__ pos, int rule,
+                                                            double3 org, double cw, int gx, int gy, int gz,
+                                                            unsigned int *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 x = pos[i];
+    int c[3];
+    const int g[3] = {gx, gy, gz};
+    const float xf[3] = {x.x, x.y, x.z};
+    const double o[3] = {org.x, org.y, org.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        int k;
+        if (rule == 0) {
+            k = (int)__ddiv_rn((double)xf[a] - o[a], cw);
+        } else {
+            k = (int)floorf(__fdiv_rn(__fsub_rn(xf[a], (float)o[a]), (float)cw));
+        }
+        c[a] = k < 0 ? 0 : (k >= g[a] ? g[a] - 1 : k);
+    }
+    out[i] = ((unsigned int)c[2] * (unsigned int)gy + (unsigned int)c[1]) * (unsigned int)gx + (unsigned int)c[0];
+}
+
+void launch_reference_cells(int n, const float4 *pos, int rule, const double org[3], double cw, const int g[3],
+                            unsigned int *out, cudaStream_t s) {
+    if (n > 0)
+        k_reference_cells<<<blocks_for(n), kBlock, 0, s>>>(n, pos, rule, make_double3(org[0], org[1], org[2]), cw,
+                                                          g[0], g[1], g[2], out);
+}
+
 void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s) {
     k_unsort4<<<blocks_for(n), kBlock, 0, s>>>(n, id, src, dst, zero_w);
 }

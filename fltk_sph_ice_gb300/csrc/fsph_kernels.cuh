@@ -141,6 +141,10 @@ void launch_density_grid(const DevParams &p, const unsigned int *cell_start, con
                          const double minp[3], const double d[3], const double lo[3], const double hi[3], float *out,
                          cudaStream_t s);
 
+/* ---- the reference's cell hash (rule 0: its CPU grid, 1: its GPU grid) ---- */
+void launch_reference_cells(int n, const float4 *pos, int rule, const double org[3], double cw, const int g[3],
+                            unsigned int *out, cudaStream_t s);
+
 /* ---- particle order <-> device order ---- */
 void launch_unsort4(int n, const unsigned int *id, const float4 *src, float4 *dst, int zero_w, cudaStream_t s);
 void launch_unsort1(int n, const unsigned int *id, const unsigned int *src, unsigned int *dst, cudaStream_t s);

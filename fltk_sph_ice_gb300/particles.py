@@ -228,6 +228,18 @@ class rxParticleSystemBase:
         return off, idx[:total.value]
 
     # -- density on a lattice (rx_ps.h:283-285) ----------------------------
+    def CalGridHash(self, pos, rule: int = 0):
+        """The reference's cell hash of each position: rule 0 = its CPU grid
+        (rxNNGrid::CalGridHash), 1 = its GPU grid (calcGridPos /
+        calcGridHash).  Returns (hash uint32[n], grid dims (3,), cell width)."""
+        p4 = _as4(pos)
+        out = np.zeros(p4.shape[0], np.uint32)
+        g = np.zeros(3, np.int32)
+        cw = ctypes.c_double()
+        self._check(self.L.fsph_reference_cell_hash(self._ctx, int(rule), _ptr(p4), p4.shape[0], abi.HOST, _ptr(out),
+                                                    _ptr(g), ctypes.byref(cw)), "fsph_reference_cell_hash")
+        return out, g, cw.value
+
     def CalImplicitField(self, n, minp, d) -> np.ndarray:
         """The density field of the current particles on an n[0] x n[1] x n[2]
         lattice from minp with spacing d (CalImplicitField, rx_sph_pbd.cpp:2036):

@@ -259,6 +259,21 @@ int fsph_clear_inlets(fsph_ctx *ctx);
  * receives the count.  Synchronises. */
 int fsph_emit_inlets(fsph_ctx *ctx, int step, int *emitted);
 
+/* ---- the reference's cell indices ---- */
+/* The reference's cell hash z*Gy*Gx + y*Gx + x of each of n positions
+ * (float4 stride), for parity of cell indices: rule 0 = the reference's CPU
+ * grid (rxNNGrid::Setup / CalGridHash(Vec3), rx_nnsearch.h:174-199, 590-599:
+ * power-of-two axis counts, (p - min) / cw in double truncated), rule 1 =
+ * its GPU grid (setupCells, rx_sph_pbd_gpu.cpp:1986-2011, and calcGridPos /
+ * calcGridHash, rx_cu_common.cu:121-144: floor(L/cw) + 1 cells per axis,
+ * float floor); both over the box grown by 1 % (rx_sph_pbd.cpp:188-196) with
+ * the context's h, cell coordinates clamped to [0, G-1].  grid[3] and
+ * cell_width (either may be NULL) receive the geometry.  This context's own
+ * grid is a different, padded one (cell width h(1 + cell_skin)); the
+ * neighbour sets do not depend on the grid. */
+int fsph_reference_cell_hash(fsph_ctx *ctx, int rule, const float *pos4, int n, int where, unsigned int *hash,
+                             int *grid, double *cell_width);
+
 /* ---- density on a lattice, for surface meshing ---- */
 /* CalImplicitField / CalImplicitFieldDevice (rx_ps.h:283-285;
  * rxPBDSPH::CalImplicitField -> CalColorField, rx_sph_pbd.cpp:2024-2108;

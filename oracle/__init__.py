@@ -248,6 +248,8 @@ def ref_lib() -> ctypes.CDLL | None:
         L.fsph_ref_pbf_predict.argtypes = [vp, cf, vp, vp, vp, vp]
         L.fsph_ref_sph_forces.argtypes = [vp, vp, vp, vp]
         L.fsph_ref_pbf_density_grid.argtypes = [vp, vp, ci, vp, vp, vp, vp]
+        L.fsph_ref_cell_hash.argtypes = [vp, vp, ci, vp]
+        L.fsph_ref_cell_hash.restype = ctypes.c_longlong
         L.fsph_ref_kernel.restype = cd
         L.fsph_ref_kernel.argtypes = [ci, cd, cd]
         L.fsph_ref_kernel_coef.restype = cd
@@ -320,6 +322,14 @@ class RefSolver:
             return it, float(eta[0])
         self.L.fsph_ref_sph_update(self.h, dt)
         return None
+
+    def cell_hash(self, pos4):
+        """rxNNGrid::CalGridHash(Vec3) of each position on the reference's CPU
+        grid, and that grid's cell count."""
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        out = np.zeros(pos4.shape[0], np.uint32)
+        cells = self.L.fsph_ref_cell_hash(self.h, _vp(pos4), pos4.shape[0], _vp(out))
+        return out, int(cells)
 
     def neighbors(self, pos4):
         pos4 = np.ascontiguousarray(pos4, dtype=np.float32)

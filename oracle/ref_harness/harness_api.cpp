@@ -180,6 +180,15 @@ void fsph_ref_pbf_density_grid(void *p, const float *pos4, int n, const int *nn,
     s->CalImplicitField(dims, Vec3(minp[0], minp[1], minp[2]), Vec3(d[0], d[1], d[2]), out);
 }
 
+/* rxNNGrid::CalGridHash(Vec3) of the reference's CPU grid for each position,
+ * and the grid's cell count. */
+long long fsph_ref_cell_hash(void *p, const float *pos4, int n, unsigned int *out) {
+    rxPBDSPH *s = (rxPBDSPH *)p;
+    for (int i = 0; i < n; ++i)
+        out[i] = s->m_pNNGrid->CalGridHash(Vec3(pos4[4 * i + 0], pos4[4 * i + 1], pos4[4 * i + 2]));
+    return (long long)s->m_pNNGrid->GetCellData().uNumCells;
+}
+
 /* One lambda pass (rxPBDSPH::calScalingFactor) on the given predicted positions. */
 void fsph_ref_pbf_lambda(void *p, const float *pos4, int n, float dt, float *dens, float *scl) {
     rxPBDSPH *s = (rxPBDSPH *)p;

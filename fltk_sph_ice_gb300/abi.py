@@ -83,7 +83,8 @@ class FsphParams(ctypes.Structure):
         ("walk_cells", ctypes.c_int),
         ("collect_features", ctypes.c_int),
         ("compensated_density", ctypes.c_int),
-        ("reserved", ctypes.c_int * 3),
+        ("grid_sort", ctypes.c_int),
+        ("reserved", ctypes.c_int * 2),
     ]
 
     def to_dict(self) -> dict:

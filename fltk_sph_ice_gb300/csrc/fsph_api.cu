@@ -143,6 +143,7 @@ struct fsph_ctx {
      * and every call that touches them is refused until fsph_set_params
      * reallocates successfully */
     bool broken = false;
+    RadixBufs radix; /* grid_sort 1 */
     std::string err;
 };
 
@@ -199,6 +200,7 @@ int validate(const fsph_params &p, std::string &why) {
     }
     if (p.cell_skin < 0.0f || p.cell_skin > 1.0f) { why = "cell_skin must lie in [0, 1]"; return FSPH_INVALID_ARG; }
     if (p.warm_start < 0 || p.warm_start > 1) { why = "warm_start must be 0 or 1"; return FSPH_INVALID_ARG; }
+    if (p.grid_sort < 0 || p.grid_sort > 1) { why = "grid_sort must be 0 or 1"; return FSPH_INVALID_ARG; }
     return FSPH_OK;
 }
 
@@ -297,6 +299,9 @@ void free_particles(fsph_ctx *c) {
     c->key = c->rank = c->perm = nullptr;
     c->epart = nullptr;
     c->dpart = nullptr;
+    cudaFree(c->radix.k0); cudaFree(c->radix.k1);
+    cudaFree(c->radix.hist); cudaFree(c->radix.offs); cudaFree(c->radix.bsum);
+    c->radix = RadixBufs{};
 }
 
 void free_grid(fsph_ctx *c) {
@@ -396,6 +401,12 @@ int alloc_particles(fsph_ctx *c, int cap) {
     FSPH_TRY(dalloc(c, &c->tmp4, n)); FSPH_TRY(dalloc(c, &c->feat, n * kFeatures));
     FSPH_CUDA(c, cudaMemsetAsync(c->dstep, 0, n * sizeof(float4), c->stream));
     FSPH_CUDA(c, cudaMemsetAsync(c->feat, 0, n * kFeatures * sizeof(float), c->stream));
+    {
+        const size_t nt = radix_tiles((int)n), nh = nt * 256;
+        FSPH_TRY(dalloc(c, &c->radix.k0, n)); FSPH_TRY(dalloc(c, &c->radix.k1, n));
+        FSPH_TRY(dalloc(c, &c->radix.hist, nh)); FSPH_TRY(dalloc(c, &c->radix.offs, nh + 1)); /* + the total */
+        FSPH_TRY(dalloc(c, &c->radix.bsum, scan_blocks((unsigned int)nh)));
+    }
     FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n, kPassBlock)));
     FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n, kPassBlock)));
     for (int k = 0; k < 2; ++k) {
@@ -469,11 +480,18 @@ int boundary_build(fsph_ctx *c) {
 
 /* ---------------- building blocks of a step ---------------- */
 
-/* counting sort of the slots of x (device order) by cell: leaves perm */
+/* perm = the slots in (cell, previous slot) order, from the hashed cells:
+ * the counting sort (grid_sort 0) or the LSD radix sort (grid_sort 1) */
+void sort_cells(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
+    if (c->P.grid_sort == 1) launch_radix_sort_cells(p.n, c->key, c->ncells, c->radix, c->perm, s);
+    else launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+}
+
+/* sort of the slots of x (device order) by cell: leaves perm */
 void enqueue_sort(fsph_ctx *c, const DevParams &p, const float4 *x, cudaStream_t s) {
     launch_hash(p, x, c->key, c->rank, c->count, s);
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
-    launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+    sort_cells(c, p, s);
 }
 
 /* the grid rebuild used inside the loop and after it (positions = current x*) */
@@ -481,7 +499,7 @@ void enqueue_rebuild(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
     BufSet &I = c->set[it], &O = c->set[1 - it];
     launch_hash_parity(p, c->ppos[0], c->ppos[1], c->ctl, c->key, c->rank, c->count, s);
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
-    launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+    sort_cells(c, p, s);
     const bool ws = c->P.warm_start != 0 || c->P.collect_features != 0;
     float *t_lam = reinterpret_cast<float *>(c->rank); /* free once the scatter has run */
     launch_rebuild_gather(p.n, c->perm, c->ctl, I.pos, c->ppos[0], c->ppos[1], I.id, I.attr, c->dens, O.pos, O.vel,
@@ -530,7 +548,7 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     launch_predict_hash(p, c->set[src].pos, c->set[src].vel, acc, c->ppos[1], c->key, c->rank, c->count, dw,
                         ws ? c->tmp4 : nullptr, s);
     launch_scan(c->count, c->cell_start, c->block_sums, c->ncells, s);
-    launch_scatter_sort(p, c->key, c->rank, c->cell_start, c->perm, c->ncells, s);
+    sort_cells(c, p, s);
     Gather g{};
     g.n4 = ws ? 4 : 3; g.n1 = 3;
     g.src4[0] = c->set[src].pos; g.dst4[0] = c->set[it].pos;

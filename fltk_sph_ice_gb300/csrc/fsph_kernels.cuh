@@ -141,6 +141,18 @@ void launch_density_grid(const DevParams &p, const unsigned int *cell_start, con
                          const double minp[3], const double d[3], const double lo[3], const double hi[3], float *out,
                          cudaStream_t s);
 
+/* ---- grid sort as an LSD radix sort of (cell << 32 | slot) keys ---- */
+struct RadixBufs {
+    unsigned long long *k0 = nullptr, *k1 = nullptr; /* n keys each (ping-pong) */
+    unsigned int *hist = nullptr, *offs = nullptr;   /* 256 x tiles (offs: + 1 for the scan's total) */
+    unsigned int *bsum = nullptr;                    /* scan_blocks(256 x tiles) */
+};
+unsigned int radix_tiles(int n);
+int radix_passes(unsigned int ncells);
+/* perm[d] = the previous slot of the d-th key in (cell, slot) order */
+void launch_radix_sort_cells(int n, const unsigned int *cell, unsigned int ncells, const RadixBufs &b,
+                             unsigned int *perm, cudaStream_t s);
+
 /* ---- the reference's cell hash (rule 0: its CPU grid, 1: its GPU grid) ---- */
 void launch_reference_cells(int n, const float4 *pos, int rule, const double org[3], double cw, const int g[3],
                             unsigned int *out, cudaStream_t s);

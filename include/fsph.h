@@ -126,7 +126,11 @@ typedef struct fsph_params {
     int collect_features;    /* 1: compute FSPH_FEATURES / FSPH_STEP_CORRECTION every step even
                                 without a warm start (training-data collection) */
     int compensated_density; /* 1: Kahan-compensated FP32 density sums in the lambda pass */
-    int reserved[3];
+    int grid_sort;           /* order of the slots by cell at each grid build, both giving the
+                                order of the 64-bit key (cell << 32 | previous slot):
+                                0: counting sort (atomic ranks, then each cell's slots sorted);
+                                1: LSD radix sort of the 64-bit keys, 8 cell bits per pass */
+    int reserved[2];
 } fsph_params;
 
 /* Scene description in the reference's own terms (rxSPHEnviroment). */

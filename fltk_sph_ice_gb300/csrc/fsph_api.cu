@@ -1581,6 +1581,158 @@ int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {
     return FSPH_OK;
 }
 
+/* ---- state file: everything a step reads, in device order ---- */
+extern "C++" {
+namespace {
+const char kStateMagic[8] = {'F', 'S', 'P', 'H', 'S', 'T', 'A', 'T'};
+const int kStateVersion = 1;
+
+struct StateHeader {
+    char magic[8];
+    int version, params_size, n, n_active, nb, inlet_start;
+    int n_inlets, n_del, n_boxes, n_spheres;
+    int home_identity, model_loaded, model_nbr;
+    unsigned int warm_valid;
+    int mlp_bytes, features;
+    long long steps_done;
+};
+
+template <class T>
+bool put(std::FILE *f, const T *v, size_t count) { return count == 0 || std::fwrite(v, sizeof(T), count, f) == count; }
+template <class T>
+bool get(std::FILE *f, T *v, size_t count) { return count == 0 || std::fread(v, sizeof(T), count, f) == count; }
+
+/* device array <-> file through a host buffer */
+template <class T>
+int put_dev(fsph_ctx *c, std::FILE *f, const T *d, size_t count) {
+    std::vector<T> h(count);
+    if (count) FSPH_CUDA(c, cudaMemcpy(h.data(), d, count * sizeof(T), cudaMemcpyDeviceToHost));
+    return put(f, h.data(), count) ? FSPH_OK : fail(c, FSPH_INVALID_ARG, "state file: write failed");
+}
+template <class T>
+int get_dev(fsph_ctx *c, std::FILE *f, T *d, size_t count) {
+    std::vector<T> h(count);
+    if (!get(f, h.data(), count)) return fail(c, FSPH_INVALID_ARG, "state file: truncated");
+    if (count) FSPH_CUDA(c, cudaMemcpy(d, h.data(), count * sizeof(T), cudaMemcpyHostToDevice));
+    return FSPH_OK;
+}
+struct FileCloser {
+    std::FILE *f;
+    ~FileCloser() { if (f) std::fclose(f); }
+};
+}  // namespace
+}  // extern "C++"
+
+int fsph_save_state(fsph_ctx *c, const char *path) {
+    if (!c || !path) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    FileCloser fc{std::fopen(path, "wb")};
+    if (!fc.f) return fail(c, FSPH_INVALID_ARG, std::string("cannot write ") + path);
+    StateHeader h{};
+    std::memcpy(h.magic, kStateMagic, 8);
+    h.version = kStateVersion;
+    h.params_size = (int)sizeof(fsph_params);
+    h.n = c->n; h.n_active = c->n_active; h.nb = c->nb; h.inlet_start = c->inlet_start;
+    h.n_inlets = (int)c->inlets.size(); h.n_del = (int)c->del_regions.size();
+    h.n_boxes = (int)c->boxes.size(); h.n_spheres = (int)c->spheres.size();
+    h.home_identity = c->home_identity ? 1 : 0;
+    h.model_loaded = c->model_loaded ? 1 : 0;
+    h.model_nbr = c->model_nbr ? 1 : 0;
+    FSPH_CUDA(c, cudaMemcpy(&h.warm_valid, c->warm_valid, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+    h.mlp_bytes = (int)sizeof(MlpDev);
+    h.features = kFeatures;
+    h.steps_done = c->steps_done;
+    bool ok = put(fc.f, &h, 1) && put(fc.f, &c->P, 1) && put(fc.f, c->inlets.data(), c->inlets.size()) &&
+              put(fc.f, c->del_regions.data(), c->del_regions.size()) && put(fc.f, c->boxes.data(), c->boxes.size()) &&
+              put(fc.f, c->spheres.data(), c->spheres.size());
+    if (!ok) return fail(c, FSPH_INVALID_ARG, "state file: write failed");
+    const size_t n = (size_t)c->n;
+    FSPH_TRY(put_dev(c, fc.f, c->set[0].pos, n));
+    FSPH_TRY(put_dev(c, fc.f, c->set[0].vel, n));
+    FSPH_TRY(put_dev(c, fc.f, c->set[0].id, n));
+    FSPH_TRY(put_dev(c, fc.f, c->set[0].attr, n));
+    FSPH_TRY(put_dev(c, fc.f, c->dstep, n));
+    FSPH_TRY(put_dev(c, fc.f, c->feat, n * kFeatures));
+    FSPH_TRY(put_dev(c, fc.f, c->b_in, (size_t)c->nb));
+    if (c->model_loaded)
+        FSPH_TRY(put_dev(c, fc.f, reinterpret_cast<const unsigned char *>(c->mlp_dev), sizeof(MlpDev)));
+    if (std::fflush(fc.f) != 0) return fail(c, FSPH_INVALID_ARG, "state file: write failed");
+    return FSPH_OK;
+}
+
+int fsph_load_state(fsph_ctx *c, const char *path) {
+    if (!c || !path) return FSPH_INVALID_ARG;
+    FileCloser fc{std::fopen(path, "rb")};
+    if (!fc.f) return fail(c, FSPH_INVALID_ARG, std::string("cannot read ") + path);
+    StateHeader h{};
+    if (!get(fc.f, &h, 1) || std::memcmp(h.magic, kStateMagic, 8) != 0)
+        return fail(c, FSPH_INVALID_ARG, "not a state file");
+    if (h.version != kStateVersion || h.params_size != (int)sizeof(fsph_params) || h.mlp_bytes != (int)sizeof(MlpDev) ||
+        h.features != kFeatures)
+        return fail(c, FSPH_INVALID_ARG, "state file of another version or build");
+    fsph_params P{};
+    if (!get(fc.f, &P, 1)) return fail(c, FSPH_INVALID_ARG, "state file: truncated");
+    if (h.n < 0 || h.n > P.max_particles || h.n_active < 0 || h.n_active > h.n || h.nb < 0 || h.n_inlets < 0 ||
+        h.n_del < 0 || h.n_boxes < 0 || h.n_boxes > kMaxBoxObstacles || h.n_spheres < 0 ||
+        h.n_spheres > kMaxSphereObstacles || (h.n_del & 1) || h.n_del > 2 * 64 || h.n_inlets > 4096)
+        return fail(c, FSPH_INVALID_ARG, "state file: inconsistent counts");
+    if (P.solver != c->P.solver) return fail(c, FSPH_INVALID_ARG, "state file of the other solver");
+    std::vector<fsph_ctx::Inlet> inlets((size_t)h.n_inlets);
+    std::vector<float4> del((size_t)h.n_del);
+    std::vector<Obstacle> boxes((size_t)h.n_boxes), spheres((size_t)h.n_spheres);
+    if (!get(fc.f, inlets.data(), inlets.size()) || !get(fc.f, del.data(), del.size()) ||
+        !get(fc.f, boxes.data(), boxes.size()) || !get(fc.f, spheres.data(), spheres.size()))
+        return fail(c, FSPH_INVALID_ARG, "state file: truncated");
+    /* the particle arrays are read into host buffers first, so a bad file
+     * leaves the context as it was */
+    const size_t n = (size_t)h.n;
+    std::vector<float4> pos(n), vel(n), dstep(n), bpos((size_t)h.nb);
+    std::vector<unsigned int> id(n), attr(n);
+    std::vector<float> feat(n * kFeatures);
+    std::vector<unsigned char> mlp(h.model_loaded ? sizeof(MlpDev) : 0);
+    if (!get(fc.f, pos.data(), n) || !get(fc.f, vel.data(), n) || !get(fc.f, id.data(), n) ||
+        !get(fc.f, attr.data(), n) || !get(fc.f, dstep.data(), n) || !get(fc.f, feat.data(), feat.size()) ||
+        !get(fc.f, bpos.data(), bpos.size()) || !get(fc.f, mlp.data(), mlp.size()))
+        return fail(c, FSPH_INVALID_ARG, "state file: truncated");
+    std::vector<unsigned char> seen(n, 0);
+    for (size_t k = 0; k < n; ++k) {
+        if (id[k] >= n || seen[id[k]]) return fail(c, FSPH_INVALID_ARG, "state file: particle order is not a permutation");
+        seen[id[k]] = 1;
+    }
+    FSPH_TRY(fsph_set_params(c, &P));
+    FSPH_TRY(fsph_set_boundary(c, h.nb ? reinterpret_cast<const float *>(bpos.data()) : nullptr, h.nb, FSPH_HOST));
+    FSPH_TRY(load_particles(c, reinterpret_cast<const float *>(pos.data()), reinterpret_cast<const float *>(vel.data()),
+                            h.n, FSPH_HOST));
+    cudaStream_t s = c->stream;
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].id, id.data(), n * 4, cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr, attr.data(), n * 4, cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->dstep, dstep.data(), n * 16, cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->feat, feat.data(), feat.size() * 4, cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaMemcpyAsync(c->warm_valid, &h.warm_valid, sizeof(unsigned int), cudaMemcpyHostToDevice, s));
+    if (h.model_loaded) FSPH_CUDA(c, cudaMemcpyAsync(c->mlp_dev, mlp.data(), mlp.size(), cudaMemcpyHostToDevice, s));
+    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    c->model_loaded = h.model_loaded != 0;
+    c->model_nbr = h.model_nbr != 0;
+    c->home_identity = h.home_identity != 0;
+    c->res_in_res_id = false;
+    c->n_active = h.n_active;
+    c->inlets = inlets;
+    c->inlet_start = h.inlet_start;
+    c->del_regions = del;
+    c->boxes = boxes;
+    c->spheres = spheres;
+    c->steps_done = h.steps_done;
+    drop_graph(c);
+    FSPH_TRY(upload_obstacles(c));
+    if (!c->del_regions.empty()) { /* the table fsph_add_delete_region keeps: 64 regions */
+        if (!c->del_dev) FSPH_CUDA(c, cudaMalloc((void **)&c->del_dev, 2 * 64 * sizeof(float4)));
+        FSPH_CUDA(c, cudaMemcpy(c->del_dev, c->del_regions.data(), c->del_regions.size() * sizeof(float4),
+                                cudaMemcpyHostToDevice));
+    }
+    return FSPH_OK;
+}
+
 int fsph_set_warm_start_model(fsph_ctx *c, const float *blob) {
     if (!c || !blob) return FSPH_INVALID_ARG;
     for (int k = 0; k < FSPH_MLP_BLOB_SIZE; ++k)

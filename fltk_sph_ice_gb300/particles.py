@@ -10,6 +10,8 @@ the library's status and message; nothing here computes physics.
 from __future__ import annotations
 
 import ctypes
+import json
+import os
 
 import numpy as np
 
@@ -183,6 +185,59 @@ class rxParticleSystemBase:
 
     def GetNumActiveParticles(self) -> int:
         return int(self.L.fsph_num_active(self._ctx))
+
+    def SaveState(self, path: str):
+        """The exact device state (fsph_save_state): resuming from it with
+        LoadState steps bit-identically to continuing."""
+        self._check(self.L.fsph_save_state(self._ctx, os.fsencode(path)), "fsph_save_state")
+
+    def LoadState(self, path: str):
+        self._check(self.L.fsph_load_state(self._ctx, os.fsencode(path)), "fsph_load_state")
+
+    def OutputParticles(self, path: str):
+        """The reference's particle file (rx_ps.cpp:581-612): uint32 N, N x 3
+        float32 positions, N x 3 float32 velocities."""
+        x = self.GetArrayVBO(abi.RX_POSITION)[:, :3]
+        v = self.GetArrayVBO(abi.RX_VELOCITY)[:, :3]
+        with open(path, "wb") as f:
+            f.write(np.uint32(x.shape[0]).tobytes())
+            f.write(np.ascontiguousarray(x, np.float32).tobytes())
+            f.write(np.ascontiguousarray(v, np.float32).tobytes())
+
+    def InputParticles(self, path: str):
+        """rx_ps.cpp:614-644: the positions (and velocities, when present) of
+        a particle file replace the current particles."""
+        raw = open(path, "rb").read()
+        n = int(np.frombuffer(raw[:4], np.uint32)[0])
+        body = np.frombuffer(raw[4:], np.float32)
+        if body.size < 3 * n:
+            raise ValueError("particle file truncated")
+        x = body[:3 * n].reshape(n, 3)
+        v = body[3 * n:6 * n].reshape(n, 3) if body.size >= 6 * n else None
+        self.Set(x, v)
+
+    def SaveCheckpoint(self, path: str, seed: int | None = None):
+        """Particle file at `path`, exact state at path + '.state', JSON
+        sidecar at path + '.json' (parameters, counts, the scene seed)."""
+        self.OutputParticles(path)
+        self.SaveState(path + ".state")
+        side = {"format": "fsph checkpoint 1", "params": self.GetParams().to_dict(), "seed": seed,
+                "particles": self.GetNumParticles(), "active": self.GetNumActiveParticles(),
+                "state": os.path.basename(path) + ".state",
+                "jitter": "inlet jitter is counter-based on (line, step); no generator state"}
+        with open(path + ".json", "w") as f:
+            json.dump(side, f, indent=1)
+
+    def LoadCheckpoint(self, path: str):
+        """Resume from SaveCheckpoint's files; returns the sidecar's seed."""
+        with open(path + ".json") as f:
+            side = json.load(f)
+        st = path + ".state"
+        if os.path.isfile(st):
+            self.LoadState(st)
+        else:
+            self.InputParticles(path)
+        return side.get("seed")
 
     def SetStepLog(self, path: str | None):
         """Append one JSON line per step to `path` (None stops the log)."""

@@ -436,6 +436,24 @@ int fsph_mlp_train(fsph_mlp *m, const float *x, const float *t, int n, int batch
 /* Install a trained blob (host) as the context's warm-start network. */
 int fsph_set_warm_start_model(fsph_ctx *ctx, const float *blob);
 
+/* ---- checkpoint / resume ---- */
+/* Write everything a step reads to `path`, in device order, so that
+ * fsph_load_state into a context of the same solver resumes bit-identically
+ * to continuing without the checkpoint: the parameters, the particles'
+ * positions, velocities, attributes and slot order, the warm-start history
+ * and network, the boundary particles, obstacles, inlet lines (with the
+ * ring index of the next emission), deletion regions and the step count.
+ * The inlet jitter is a counter-based function of (line, step), so no
+ * random-generator state exists to save.  The reference's checkpoint is the
+ * particle file alone (OutputParticles / InputParticles, rx_ps.cpp:581-644:
+ * uint32 N, positions, velocities), which fsph_particle_system.hpp writes
+ * beside this file.  The per-step fields (density, lambda, forces) are not
+ * saved: the next step recomputes them.  A file of another build version or
+ * a truncated file is rejected with FSPH_INVALID_ARG before the context is
+ * changed.  Synchronises. */
+int fsph_save_state(fsph_ctx *ctx, const char *path);
+int fsph_load_state(fsph_ctx *ctx, const char *path);
+
 /* ---- records and test hooks ---- */
 /* Append one JSON line per step to `path` (NULL or "" stops): step number,
  * solver, dt, particle counts, iterations, grid builds, the three density

@@ -41,6 +41,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -415,6 +416,56 @@ public:
         if (ok && std::fread(v3.data(), sizeof(float), v3.size(), f) != v3.size()) std::fill(v3.begin(), v3.end(), 0.0f);
         std::fclose(f);
         return ok && Set(p3, v3) ? 1 : 0;
+    }
+
+    /* Checkpoint: the reference's particle file at fn (OutputParticles), the
+     * exact device state at fn + ".state" (fsph_save_state) and a JSON
+     * sidecar at fn + ".json" with the parameters and the placement RNG
+     * seed (the AddBox / AddSphere / AddLine jitter counter).  LoadCheckpoint
+     * resumes bit-identically to continuing without the checkpoint; without
+     * the ".state" file it falls back to the particle file (the seed is
+     * still restored).  Return 1 on success, 0 on failure. */
+    int SaveCheckpoint(const std::string &fn) {
+        if (!m_ctx || !OutputParticles(fn)) return 0;
+        m_status = fsph_save_state(m_ctx, (fn + ".state").c_str());
+        if (m_status != FSPH_OK) return 0;
+        const fsph_params p = params();
+        FILE *f = std::fopen((fn + ".json").c_str(), "w");
+        if (!f) return 0;
+        std::fprintf(f,
+                     "{\"format\": \"fsph checkpoint 1\", \"solver\": %d, \"particles\": %d, "
+                     "\"active\": %d, \"max_particles\": %d, \"seed\": %llu, \"inlets\": %d, "
+                     "\"h\": %.9g, \"mass\": %.9g, \"rest_dens\": %.9g, \"dt_note\": \"dt is an Update argument\", "
+                     "\"box_min\": [%.17g, %.17g, %.17g], \"box_max\": [%.17g, %.17g, %.17g], "
+                     "\"state\": \"%s.state\"}\n",
+                     p.solver, GetNumParticles(), GetNumActiveParticles(), p.max_particles,
+                     (unsigned long long)m_seed, m_inlets, (double)p.h, (double)p.mass, (double)p.rest_dens,
+                     p.box_min[0], p.box_min[1], p.box_min[2], p.box_max[0], p.box_max[1], p.box_max[2], fn.c_str());
+        const bool ok = std::fclose(f) == 0;
+        return ok ? 1 : 0;
+    }
+    int LoadCheckpoint(const std::string &fn) {
+        if (!m_ctx) return 0;
+        FILE *f = std::fopen((fn + ".json").c_str(), "r");
+        if (f) { /* the seed and the inlet count from the sidecar */
+            char buf[4096];
+            const size_t k = std::fread(buf, 1, sizeof(buf) - 1, f);
+            std::fclose(f);
+            buf[k] = 0;
+            const char *q = std::strstr(buf, "\"seed\": ");
+            if (q) m_seed = std::strtoull(q + 8, nullptr, 10);
+            q = std::strstr(buf, "\"inlets\": ");
+            if (q) m_inlets = (int)std::strtol(q + 10, nullptr, 10);
+        }
+        m_status = fsph_load_state(m_ctx, (fn + ".state").c_str());
+        if (m_status == FSPH_OK) {
+            const fsph_params p = params();
+            m_use_vorticity = p.vort_eps != 0.0f;
+            m_artificial_pressure = p.use_ap != 0;
+            m_gravity_y = p.gravity[1];
+            return 1;
+        }
+        return InputParticles(fn);
     }
 
     /* g_iIterations / g_fEta of the last step (rx_sph_pbd.cpp:461-462) */

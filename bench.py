@@ -565,6 +565,8 @@ def gpu_arm(args):
         cfg = {"workload": WORKLOAD, "particles": n, "block": list(BLOCK), "dt": sc.dt, "eta_one_sided": 1e-3,
                "constraint": "unilateral (clamped C >= 0)", "method": method_of(meta),
                "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
+               "not_converged_steps": warm["not_converged_steps"], "status": warm["status"],
+               "meets_criterion": warm["not_converged_steps"] == 0,
                "grid_builds_per_step": warm["grid_builds"], "cell_skin": round(float(sc.params.cell_skin), 3),
                "model": {"samples": meta.get("samples"), "rollouts": meta.get("rollouts"),
                          "output_damping": meta.get("output_damping")},
@@ -921,7 +923,7 @@ def large_arm(args):
                 raise RuntimeError(L.fsph_last_error(ps.handle).decode())
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        iters, errs, kern = [], [], 0
+        iters, errs, kern, unconv = [], [], 0, 0
         if dist:
             dist.barrier()
         for k in range(args.steps):
@@ -935,11 +937,13 @@ def large_arm(args):
             iters.append(stats.iterations)
             errs.append(stats.density_error_one_sided)
             kern += stats.kernels
+            unconv += int(stats.status == abi.NOT_CONVERGED)
         tot_s = sum(a.elapsed_time(c) for a, c in ev) / 1000.0
         value, tot_s = replica_rate(sc.n, args.steps, tot_s, dist)
         ps.close()
         return {"value": value, "ms_per_step": 1000.0 * tot_s / args.steps, "mean_iterations": float(np.mean(iters)),
-                "max_error": float(np.max(errs)), "kernels": kern}
+                "max_error": float(np.max(errs)), "kernels": kern, "not_converged_steps": unconv,
+                "status": "FSPH_NOT_CONVERGED" if unconv else "FSPH_OK"}
 
     with ClockSampler(local) as clk:
         plain = leg(False) if not args.no_plain else None
@@ -952,10 +956,13 @@ def large_arm(args):
                "block": [256, 256, 256], "dt": sc.dt, "eta_one_sided": 1e-3, "compensated_density": True,
                "constraint": "unilateral (clamped C >= 0)", "method": method_of(meta),
                "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
+               "not_converged_steps": warm["not_converged_steps"], "status": warm["status"],
+               "meets_criterion": warm["not_converged_steps"] == 0,
                "preroll_steps": LARGE_PREROLL, "l2": "256 MiB flush between timed steps",
                "parallelism": f"replicas x{world}", "fp64_error_per_step": fp64}
         if plain:
-            cfg["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "mean_iterations", "max_error")}
+            cfg["plain"] = {k: plain[k] for k in ("value", "ms_per_step", "mean_iterations", "max_error",
+                                                  "not_converged_steps", "status")}
             cfg["speedup_vs_plain"] = warm["value"] / plain["value"]
         line = {
             "metric": LARGE_METRIC, "value": warm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,

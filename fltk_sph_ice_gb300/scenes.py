@@ -231,16 +231,18 @@ def batched_scenes(count: int = 256, seed: int = 4, n_lo: int = 2048, n_hi: int 
     return out
 
 
-def box_surface(lo, side: float, spacing: float) -> np.ndarray:
+def box_surface(lo, side: float, spacing: float, layers: int = 1) -> np.ndarray:
     """Particles on the surface of the axis-aligned cube [lo, lo + side]^3: the
     lattice points of an m^3 grid (m = side / spacing, rounded) that lie on
     the cube's faces, each once -- the role of rxSolid::GenerateParticlesOnSurf
-    for a box (rx_sph_pbd.cpp:180, spacing 1.2 r there)."""
+    for a box (rx_sph_pbd.cpp:180, spacing 1.2 r there).  layers > 1 keeps
+    every lattice point within layers - 1 spacings of a face (a solid shell)."""
     m = max(1, int(round(side / spacing)))
     s = side / m
     g = np.arange(m + 1)
     x, y, z = np.meshgrid(g, g, g, indexing="ij")
-    on = (x == 0) | (x == m) | (y == 0) | (y == m) | (z == 0) | (z == m)
+    depth = np.minimum.reduce([x, m - x, y, m - y, z, m - z])
+    on = depth < max(1, int(layers))
     pts = np.stack([x[on], y[on], z[on]], axis=1).astype(np.float64) * s + np.asarray(lo, np.float64)
     out = np.zeros((pts.shape[0], 4), np.float32)
     out[:, :3] = pts
@@ -254,14 +256,17 @@ def pbf_obstacle_drop(n_side: int = 256, h: float = H_DEFAULT, seed: int = 5) ->
     proportions, scaled so the block fits at the stated h: box L^3 with L =
     2.6 block sides, obstacle side 0.15 L at the centre, block centred in x and
     z one h above it (so the impact starts within a few steps).  Obstacle
-    surface particles at spacing 1.2 r (r = h / 4), as the reference samples
-    solids."""
+    particles at spacing 1.2 r (r = h / 4), the reference's surface spacing
+    for solids, in a shell of 10 layers (3 h thick): 1.48M boundary particles
+    at n_side = 256, the stated ~1.5M.  Only the outer layers meet the fluid
+    (within h); the deeper ones give the outer layers the boundary volume
+    psi_b of a solid rather than of a sheet."""
     s = 0.5 * h
     B = n_side * s
     L = 2.6 * B
     ob_side = 0.15 * L
     ob_lo = [0.5 * (L - ob_side)] * 3
-    bnd = box_surface(ob_lo, ob_side, 1.2 * 0.25 * h)
+    bnd = box_surface(ob_lo, ob_side, 1.2 * 0.25 * h, layers=10)
     o = [0.5 * (L - B) + 0.5 * s, ob_lo[1] + ob_side + h + 0.5 * s, 0.5 * (L - B) + 0.5 * s]
     pos = lattice_block(o, (n_side, n_side, n_side), s, 0.01 * h, seed, 0)
     p = pbf_params(h, [0, 0, 0], [L, L, L], pos.shape[0])

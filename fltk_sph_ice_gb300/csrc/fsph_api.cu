@@ -134,6 +134,15 @@ struct fsph_ctx {
     std::vector<Obstacle> boxes, spheres;
     Obstacle *obs_dev = nullptr;
     int nobs_dev = 0;
+    /* triangle-mesh obstacles: vertices (x, y, z floats) and triangles (3
+     * vertex indices) as given, and their device copies with the cell table */
+    std::vector<float> poly_v;
+    std::vector<int> poly_t;
+    float4 *poly_vrts = nullptr;
+    int4 *poly_tris = nullptr;
+    unsigned int *poly_start = nullptr, *poly_end = nullptr, *poly_idx = nullptr;
+    PolyTable poly{};
+    int ntri_dev = 0;
     bool last_step_graph = false;
     bool stats_pending = false;
     /* per-step JSON-lines record (fsph_set_step_log) */
@@ -337,6 +346,8 @@ DevParams dev_for(const fsph_ctx *c, int n, float dt) {
     attach_boundary(c, p);
     p.nobs = c->nobs_dev;
     p.obs = c->obs_dev;
+    p.ntri = c->ntri_dev;
+    p.poly = c->poly;
     return p;
 }
 
@@ -370,6 +381,176 @@ int upload_obstacles(fsph_ctx *c) {
         c->nobs_dev = (int)all.size();
         c->graph_valid = false;
     }
+    return FSPH_OK;
+}
+
+/* The reference's neighbour-search grid over the simulation range (the box
+ * grown by 1 %, rx_sph_pbd.cpp:188-196): cw = L_max / 2^round(log2(L_max/h))
+ * for both; the CPU grid (rxNNGrid::Setup, rx_nnsearch.h:174-199) rounds each
+ * axis count to a power of two, the GPU grid (setupCells,
+ * rx_sph_pbd_gpu.cpp:1986-2011) takes floor(L_axis / cw) + 1.  The same
+ * double operations in the same order, so the same bits. */
+int reference_grid(const fsph_params &P, int rule, double org[3], double &cw, int g[3]) {
+    double lo[3], hi[3], ws[3];
+    for (int a = 0; a < 3; ++a) {
+        const double size = P.box_max[a] - P.box_min[a];
+        lo[a] = P.box_min[a] - 0.5 * 0.01 * size;
+        hi[a] = lo[a] + size * (1.0 + 0.01);
+    }
+    for (int a = 0; a < 3; ++a) ws[a] = hi[a] - lo[a];
+    const double h = (double)P.h;
+    const double max_axis = std::max(ws[0], std::max(ws[1], ws[2]));
+    const int d = (int)(std::log(max_axis / h) / std::log(2.0) + 0.5);
+    const int m = (int)(std::pow(2.0, (double)d) + 0.5);
+    if (m <= 0) return FSPH_INVALID_ARG;
+    cw = max_axis / m;
+    for (int a = 0; a < 3; ++a) {
+        org[a] = lo[a];
+        if (rule == 0) {
+            const int da = (int)(std::log(ws[a] / cw) / std::log(2.0) + 0.5);
+            g[a] = (int)(std::pow(2.0, (double)da) + 0.5);
+        } else {
+            g[a] = (int)(ws[a] / cw) + 1;
+        }
+        if (g[a] < 1) return FSPH_INVALID_ARG;
+    }
+    if ((double)g[0] * g[1] * g[2] > 4294967295.0) return FSPH_INVALID_ARG;
+    return FSPH_OK;
+}
+
+/* ---- triangle-mesh obstacles: the cell table ---- */
+
+/* Triangle against the axis-aligned cube [-0.5, 0.5]^3 by separating axes
+ * (Akenine-Moeller, "Fast 3D Triangle-Box Overlap Testing", 2001): the three
+ * box normals, the triangle's normal and the nine edge cross products.  The
+ * reference uses the Green-Hatch test (RXFunc::polygon_intersects_cube) for
+ * the same question; the two differ only for triangles that touch a cell
+ * without entering it. */
+bool tri_cube_overlap(const double v[3][3]) {
+    const double hb = 0.5;
+    for (int a = 0; a < 3; ++a) { /* box normals: the triangle's extent */
+        const double mn = std::min(v[0][a], std::min(v[1][a], v[2][a]));
+        const double mx = std::max(v[0][a], std::max(v[1][a], v[2][a]));
+        if (mn > hb || mx < -hb) return false;
+    }
+    double e[3][3];
+    for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) e[k][a] = v[(k + 1) % 3][a] - v[k][a];
+    for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) { /* axis = unit vector a x edge k */
+            double ax[3] = {0.0, 0.0, 0.0};
+            const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+            ax[a1] = -e[k][a2];
+            ax[a2] = e[k][a1];
+            double mn = 1e300, mx = -1e300;
+            for (int j = 0; j < 3; ++j) {
+                const double q = ax[0] * v[j][0] + ax[1] * v[j][1] + ax[2] * v[j][2];
+                mn = std::min(mn, q);
+                mx = std::max(mx, q);
+            }
+            const double rad = hb * (std::fabs(ax[0]) + std::fabs(ax[1]) + std::fabs(ax[2]));
+            if (mn > rad || mx < -rad) return false;
+        }
+    double nrm[3] = {e[0][1] * e[1][2] - e[0][2] * e[1][1], e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                     e[0][0] * e[1][1] - e[0][1] * e[1][0]};
+    const double dpl = nrm[0] * v[0][0] + nrm[1] * v[0][1] + nrm[2] * v[0][2];
+    const double rad = hb * (std::fabs(nrm[0]) + std::fabs(nrm[1]) + std::fabs(nrm[2]));
+    return std::fabs(dpl) <= rad;
+}
+
+void free_polygons(fsph_ctx *c) {
+    cudaFree(c->poly_vrts); cudaFree(c->poly_tris);
+    cudaFree(c->poly_start); cudaFree(c->poly_end); cudaFree(c->poly_idx);
+    c->poly_vrts = nullptr; c->poly_tris = nullptr;
+    c->poly_start = c->poly_end = c->poly_idx = nullptr;
+    c->poly = PolyTable{};
+    c->ntri_dev = 0;
+}
+
+/* Bin the triangles into the cells of the reference's GPU grid they
+ * intersect (setPolysToCell, rx_sph_pbd_gpu.cpp:2051-2200: each triangle's
+ * bounding box of cells, (b - origin) / cw truncated and clamped, each cell
+ * tested against the triangle), a cell's triangles in ascending index as
+ * its stable sort leaves them, and upload the mesh and the table.  The
+ * reference never closes the last non-empty cell of its table (its loop
+ * compares with the particle count), which drops that cell's triangles;
+ * here every cell is closed. */
+int polygons_upload(fsph_ctx *c) {
+    FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
+    free_polygons(c);
+    c->graph_valid = false;
+    const int nv = (int)c->poly_v.size() / 3, nt = (int)c->poly_t.size() / 3;
+    if (nt == 0) return FSPH_OK;
+    double org[3], cwd;
+    int g[3];
+    if (reference_grid(c->P, 1, org, cwd, g) != FSPH_OK)
+        return fail(c, FSPH_INVALID_ARG, "degenerate grid for this box and h");
+    const float cwf = (float)cwd;
+    const double len = (double)cwf;
+    const unsigned int ncell = (unsigned int)g[0] * (unsigned int)g[1] * (unsigned int)g[2];
+    std::vector<std::pair<unsigned int, unsigned int>> hits; /* (cell, triangle) */
+    for (int i = 0; i < nt; ++i) {
+        double V[3][3];
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 3; ++a) V[j][a] = (double)c->poly_v[3 * (size_t)c->poly_t[3 * i + j] + a];
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            const double bmin = std::min(V[0][a], std::min(V[1][a], V[2][a])) - org[a];
+            const double bmax = std::max(V[0][a], std::max(V[1][a], V[2][a])) - org[a];
+            const double fl = bmin / len, fh = bmax / len;
+            lo[a] = fl < 0.0 ? (int)std::max(fl, -1.0) : (int)std::min(fl, (double)g[a]);
+            hi[a] = fh < 0.0 ? (int)std::max(fh, -1.0) : (int)std::min(fh, (double)g[a]);
+            lo[a] = std::min(std::max(lo[a], 0), g[a] - 1);
+            hi[a] = std::min(std::max(hi[a], 0), g[a] - 1);
+        }
+        for (int x = lo[0]; x <= hi[0]; ++x)
+            for (int y = lo[1]; y <= hi[1]; ++y)
+                for (int z = lo[2]; z <= hi[2]; ++z) {
+                    const double cen[3] = {org[0] + (x + 0.5) * len, org[1] + (y + 0.5) * len,
+                                           org[2] + (z + 0.5) * len};
+                    double vc[3][3];
+                    for (int j = 0; j < 3; ++j)
+                        for (int a = 0; a < 3; ++a) vc[j][a] = (V[j][a] - cen[a]) / len;
+                    if (tri_cube_overlap(vc))
+                        hits.push_back({((unsigned int)z * (unsigned int)g[1] + (unsigned int)y) * (unsigned int)g[0] +
+                                            (unsigned int)x,
+                                        (unsigned int)i});
+                }
+    }
+    std::stable_sort(hits.begin(), hits.end(),
+                     [](const std::pair<unsigned int, unsigned int> &a, const std::pair<unsigned int, unsigned int> &b) {
+                         return a.first < b.first;
+                     });
+    std::vector<unsigned int> start(ncell, 0xffffffffu), end(ncell, 0u), idx(std::max<size_t>(hits.size(), 1), 0u);
+    for (size_t k = 0; k < hits.size(); ++k) {
+        idx[k] = hits[k].second;
+        if (k == 0 || hits[k].first != hits[k - 1].first) start[hits[k].first] = (unsigned int)k;
+        end[hits[k].first] = (unsigned int)k + 1;
+    }
+    std::vector<float4> hv((size_t)nv);
+    for (int v = 0; v < nv; ++v) hv[v] = make_float4(c->poly_v[3 * v], c->poly_v[3 * v + 1], c->poly_v[3 * v + 2], 0.0f);
+    std::vector<int4> ht((size_t)nt);
+    for (int t = 0; t < nt; ++t) ht[t] = make_int4(c->poly_t[3 * t], c->poly_t[3 * t + 1], c->poly_t[3 * t + 2], 0);
+    FSPH_TRY(dalloc(c, &c->poly_vrts, (size_t)nv));
+    FSPH_TRY(dalloc(c, &c->poly_tris, (size_t)nt));
+    FSPH_TRY(dalloc(c, &c->poly_start, (size_t)ncell));
+    FSPH_TRY(dalloc(c, &c->poly_end, (size_t)ncell));
+    FSPH_TRY(dalloc(c, &c->poly_idx, idx.size()));
+    FSPH_CUDA(c, cudaMemcpy(c->poly_vrts, hv.data(), hv.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    FSPH_CUDA(c, cudaMemcpy(c->poly_tris, ht.data(), ht.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    FSPH_CUDA(c, cudaMemcpy(c->poly_start, start.data(), start.size() * 4, cudaMemcpyHostToDevice));
+    FSPH_CUDA(c, cudaMemcpy(c->poly_end, end.data(), end.size() * 4, cudaMemcpyHostToDevice));
+    FSPH_CUDA(c, cudaMemcpy(c->poly_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice));
+    PolyTable &t = c->poly;
+    t.vrts = c->poly_vrts;
+    t.tris = c->poly_tris;
+    t.start = c->poly_start;
+    t.end = c->poly_end;
+    t.idx = c->poly_idx;
+    t.org = make_float3((float)org[0], (float)org[1], (float)org[2]);
+    t.cw = cwf;
+    t.gx = g[0]; t.gy = g[1]; t.gz = g[2];
+    c->ntri_dev = nt;
     return FSPH_OK;
 }
 
@@ -1035,6 +1216,7 @@ int fsph_destroy(fsph_ctx *c) {
     cudaFree(c->mlp_dev);
     cudaFree(c->obs_dev);
     cudaFree(c->del_dev);
+    free_polygons(c);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->s2) cudaStreamDestroy(c->s2);
     if (c->s3) cudaStreamDestroy(c->s3);
@@ -1077,6 +1259,7 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
     c->broken = true;
     FSPH_TRY(alloc_grid(c));
     FSPH_TRY(boundary_build(c)); /* the boundary's cell table follows the grid */
+    if (!c->poly_t.empty()) FSPH_TRY(polygons_upload(c)); /* so does the triangles' */
     FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
     c->broken = false;
     return FSPH_OK;
@@ -1442,40 +1625,6 @@ int fsph_neighbors(fsph_ctx *c, int *offsets, int *indices, long long cap, long 
     return fsph_neighbors_ex(c, nullptr, 0, 0.0f, FSPH_HOST, offsets, indices, nullptr, cap, total);
 }
 
-/* The reference's neighbour-search grid over the simulation range (the box
- * grown by 1 %, rx_sph_pbd.cpp:188-196): cw = L_max / 2^round(log2(L_max/h))
- * for both; the CPU grid (rxNNGrid::Setup, rx_nnsearch.h:174-199) rounds each
- * axis count to a power of two, the GPU grid (setupCells,
- * rx_sph_pbd_gpu.cpp:1986-2011) takes floor(L_axis / cw) + 1.  The same
- * double operations in the same order, so the same bits. */
-int reference_grid(const fsph_params &P, int rule, double org[3], double &cw, int g[3]) {
-    double lo[3], hi[3], ws[3];
-    for (int a = 0; a < 3; ++a) {
-        const double size = P.box_max[a] - P.box_min[a];
-        lo[a] = P.box_min[a] - 0.5 * 0.01 * size;
-        hi[a] = lo[a] + size * (1.0 + 0.01);
-    }
-    for (int a = 0; a < 3; ++a) ws[a] = hi[a] - lo[a];
-    const double h = (double)P.h;
-    const double max_axis = std::max(ws[0], std::max(ws[1], ws[2]));
-    const int d = (int)(std::log(max_axis / h) / std::log(2.0) + 0.5);
-    const int m = (int)(std::pow(2.0, (double)d) + 0.5);
-    if (m <= 0) return FSPH_INVALID_ARG;
-    cw = max_axis / m;
-    for (int a = 0; a < 3; ++a) {
-        org[a] = lo[a];
-        if (rule == 0) {
-            const int da = (int)(std::log(ws[a] / cw) / std::log(2.0) + 0.5);
-            g[a] = (int)(std::pow(2.0, (double)da) + 0.5);
-        } else {
-            g[a] = (int)(ws[a] / cw) + 1;
-        }
-        if (g[a] < 1) return FSPH_INVALID_ARG;
-    }
-    if ((double)g[0] * g[1] * g[2] > 4294967295.0) return FSPH_INVALID_ARG;
-    return FSPH_OK;
-}
-
 int fsph_reference_cell_hash(fsph_ctx *c, int rule, const float *pos4, int n, int where, unsigned int *hash,
                              int *grid, double *cell_width) {
     if (!c || n < 0 || (n > 0 && (!pos4 || !hash))) return FSPH_INVALID_ARG;
@@ -1585,7 +1734,7 @@ int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {
 extern "C++" {
 namespace {
 const char kStateMagic[8] = {'F', 'S', 'P', 'H', 'S', 'T', 'A', 'T'};
-const int kStateVersion = 1;
+const int kStateVersion = 2;
 
 struct StateHeader {
     char magic[8];
@@ -1595,6 +1744,7 @@ struct StateHeader {
     unsigned int warm_valid;
     int mlp_bytes, features;
     long long steps_done;
+    int poly_nv, poly_nt;
 };
 
 template <class T>
@@ -1643,9 +1793,12 @@ int fsph_save_state(fsph_ctx *c, const char *path) {
     h.mlp_bytes = (int)sizeof(MlpDev);
     h.features = kFeatures;
     h.steps_done = c->steps_done;
+    h.poly_nv = (int)(c->poly_v.size() / 3);
+    h.poly_nt = (int)(c->poly_t.size() / 3);
     bool ok = put(fc.f, &h, 1) && put(fc.f, &c->P, 1) && put(fc.f, c->inlets.data(), c->inlets.size()) &&
               put(fc.f, c->del_regions.data(), c->del_regions.size()) && put(fc.f, c->boxes.data(), c->boxes.size()) &&
-              put(fc.f, c->spheres.data(), c->spheres.size());
+              put(fc.f, c->spheres.data(), c->spheres.size()) && put(fc.f, c->poly_v.data(), c->poly_v.size()) &&
+              put(fc.f, c->poly_t.data(), c->poly_t.size());
     if (!ok) return fail(c, FSPH_INVALID_ARG, "state file: write failed");
     const size_t n = (size_t)c->n;
     FSPH_TRY(put_dev(c, fc.f, c->set[0].pos, n));
@@ -1675,15 +1828,21 @@ int fsph_load_state(fsph_ctx *c, const char *path) {
     if (!get(fc.f, &P, 1)) return fail(c, FSPH_INVALID_ARG, "state file: truncated");
     if (h.n < 0 || h.n > P.max_particles || h.n_active < 0 || h.n_active > h.n || h.nb < 0 || h.n_inlets < 0 ||
         h.n_del < 0 || h.n_boxes < 0 || h.n_boxes > kMaxBoxObstacles || h.n_spheres < 0 ||
-        h.n_spheres > kMaxSphereObstacles || (h.n_del & 1) || h.n_del > 2 * 64 || h.n_inlets > 4096)
+        h.n_spheres > kMaxSphereObstacles || (h.n_del & 1) || h.n_del > 2 * 64 || h.n_inlets > 4096 ||
+        h.poly_nv < 0 || h.poly_nv > (1 << 24) || h.poly_nt < 0 || h.poly_nt > (1 << 24))
         return fail(c, FSPH_INVALID_ARG, "state file: inconsistent counts");
     if (P.solver != c->P.solver) return fail(c, FSPH_INVALID_ARG, "state file of the other solver");
     std::vector<fsph_ctx::Inlet> inlets((size_t)h.n_inlets);
     std::vector<float4> del((size_t)h.n_del);
     std::vector<Obstacle> boxes((size_t)h.n_boxes), spheres((size_t)h.n_spheres);
+    std::vector<float> poly_v(3 * (size_t)h.poly_nv);
+    std::vector<int> poly_t(3 * (size_t)h.poly_nt);
     if (!get(fc.f, inlets.data(), inlets.size()) || !get(fc.f, del.data(), del.size()) ||
-        !get(fc.f, boxes.data(), boxes.size()) || !get(fc.f, spheres.data(), spheres.size()))
+        !get(fc.f, boxes.data(), boxes.size()) || !get(fc.f, spheres.data(), spheres.size()) ||
+        !get(fc.f, poly_v.data(), poly_v.size()) || !get(fc.f, poly_t.data(), poly_t.size()))
         return fail(c, FSPH_INVALID_ARG, "state file: truncated");
+    for (int k : poly_t)
+        if (k < 0 || k >= h.poly_nv) return fail(c, FSPH_INVALID_ARG, "state file: triangle vertex outside the mesh");
     /* the particle arrays are read into host buffers first, so a bad file
      * leaves the context as it was */
     const size_t n = (size_t)h.n;
@@ -1723,8 +1882,11 @@ int fsph_load_state(fsph_ctx *c, const char *path) {
     c->boxes = boxes;
     c->spheres = spheres;
     c->steps_done = h.steps_done;
+    c->poly_v = poly_v;
+    c->poly_t = poly_t;
     drop_graph(c);
     FSPH_TRY(upload_obstacles(c));
+    FSPH_TRY(polygons_upload(c));
     if (!c->del_regions.empty()) { /* the table fsph_add_delete_region keeps: 64 regions */
         if (!c->del_dev) FSPH_CUDA(c, cudaMalloc((void **)&c->del_dev, 2 * 64 * sizeof(float4)));
         FSPH_CUDA(c, cudaMemcpy(c->del_dev, c->del_regions.data(), c->del_regions.size() * sizeof(float4),
@@ -1869,6 +2031,67 @@ int fsph_clear_obstacles(fsph_ctx *c) {
 }
 
 int fsph_num_obstacles(const fsph_ctx *c) { return c ? (int)(c->boxes.size() + c->spheres.size()) : -1; }
+
+int fsph_set_polygon_obstacle(fsph_ctx *c, const double *vrts, int nv, const int *tris, int nt, const double *vel) {
+    if (!c || nv < 0 || nt < 0 || (nv > 0 && !vrts) || (nt > 0 && !tris)) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
+    (void)vel; /* the reference keeps it unused (its PolyVel lines are commented out) */
+    if (nt == 0) return FSPH_OK;
+    const long long base = (long long)c->poly_v.size() / 3;
+    if (base + nv > (1ll << 24) || (long long)c->poly_t.size() / 3 + nt > (1ll << 24))
+        return fail(c, FSPH_INVALID_ARG, "at most 2^24 obstacle vertices and triangles");
+    for (long long k = 0; k < 3ll * nv; ++k)
+        if (!std::isfinite(vrts[k])) return fail(c, FSPH_INVALID_ARG, "polygon obstacle: non-finite vertex");
+    for (long long k = 0; k < 3ll * nt; ++k)
+        if (tris[k] < 0 || tris[k] >= nv) return fail(c, FSPH_INVALID_ARG, "polygon obstacle: vertex index outside [0, nv)");
+    for (long long k = 0; k < 3ll * nv; ++k) c->poly_v.push_back((float)vrts[k]);
+    for (long long k = 0; k < 3ll * nt; ++k) c->poly_t.push_back((int)(tris[k] + base));
+    const int st = polygons_upload(c);
+    if (st != FSPH_OK) { /* leave no half-added mesh */
+        c->poly_v.resize((size_t)base * 3);
+        c->poly_t.resize(c->poly_t.size() - 3 * (size_t)nt);
+        polygons_upload(c);
+    }
+    return st;
+}
+
+int fsph_clear_polygon_obstacles(fsph_ctx *c) {
+    if (!c) return FSPH_INVALID_ARG;
+    c->poly_v.clear();
+    c->poly_t.clear();
+    return polygons_upload(c);
+}
+
+int fsph_num_polygon_triangles(const fsph_ctx *c) { return c ? (int)(c->poly_t.size() / 3) : -1; }
+
+int fsph_polygon_collide(fsph_ctx *c, const float *x0_4, float *x1_4, float *v4, int n, float dt, int where) {
+    if (!c || n < 0 || (n > 0 && (!x0_4 || !x1_4 || !v4))) return FSPH_INVALID_ARG;
+    FSPH_USABLE(c);
+    if (where != FSPH_HOST && where != FSPH_DEVICE) return fail(c, FSPH_INVALID_ARG, "where");
+    if (n == 0 || c->ntri_dev == 0) return FSPH_OK;
+    cudaStream_t s = c->stream;
+    const size_t b = (size_t)n * sizeof(float4);
+    const float4 *d0 = reinterpret_cast<const float4 *>(x0_4);
+    float4 *d1 = reinterpret_cast<float4 *>(x1_4), *dv = reinterpret_cast<float4 *>(v4);
+    float4 *tmp = nullptr;
+    if (where == FSPH_HOST) {
+        FSPH_CUDA(c, cudaMallocAsync((void **)&tmp, 3 * b, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(tmp, x0_4, b, cudaMemcpyHostToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(tmp + n, x1_4, b, cudaMemcpyHostToDevice, s));
+        FSPH_CUDA(c, cudaMemcpyAsync(tmp + 2 * (size_t)n, v4, b, cudaMemcpyHostToDevice, s));
+        d0 = tmp; d1 = tmp + n; dv = tmp + 2 * (size_t)n;
+    }
+    launch_polygon_collide(dev_for(c, n, dt), n, d0, d1, dv, s);
+    cudaError_t e = cudaGetLastError();
+    if (where == FSPH_HOST) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(x1_4, d1, b, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(v4, dv, b, cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(tmp, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(c, FSPH_CUDA_ERROR, std::string("polygon collision: ") + cudaGetErrorString(e));
+    return FSPH_OK;
+}
 
 int fsph_num_active(const fsph_ctx *c) { return c ? c->n_active : -1; }
 

@@ -35,6 +35,20 @@ struct Obstacle {
     float4 inv[3];           /* box: rows of its inverse */
 };
 
+/* Triangle-mesh obstacles (SetPolygonObstacle, rx_ps.h:268): the triangles
+ * binned into the cells of the reference's GPU grid (setupCells,
+ * rx_sph_pbd_gpu.cpp:1986-2011) that they intersect, as setPolysToCell does
+ * (rx_sph_pbd_gpu.cpp:2051-2200); cell c holds idx[start[c], end[c]),
+ * start[c] = 0xffffffff when empty. */
+struct PolyTable {
+    const float4 *vrts;
+    const int4 *tris;
+    const unsigned int *start, *end, *idx;
+    float3 org;                 /* the grid's origin and cell width, as floats */
+    float cw;
+    int gx, gy, gz;
+};
+
 /* Launch-time constants of one solver; passed by value to every kernel. */
 struct DevParams {
     int n;
@@ -67,6 +81,9 @@ struct DevParams {
     /* analytic obstacles (nobs = 0: none) */
     int nobs;
     const Obstacle *obs;
+    /* triangle-mesh obstacles (ntri = 0: none) */
+    int ntri;
+    PolyTable poly;
 };
 
 /* Neighbour lists: up to kListMax entries per particle, transposed (entry
@@ -206,6 +223,111 @@ __device__ inline float3 obstacle_project(float3 x, const DevParams &p) {
     }
     return x;
 }
+/* ---- triangle-mesh obstacles: the reference's GPU rule ---- */
+/* IEEE single-precision operations with no fused multiply-add, so that the
+ * rule can be restated bit for bit on the CPU; the reference's own build lets
+ * the compiler fuse and normalises with an approximate rsqrtf, so it may
+ * differ in the last bits. */
+__device__ inline float3 psub(float3 a, float3 b) {
+    return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ inline float3 padd(float3 a, float3 b) {
+    return make_float3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+__device__ inline float3 pscale(float3 a, float s) {
+    return make_float3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s));
+}
+__device__ inline float pdot(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ inline float3 pcross(float3 a, float3 b) {
+    return make_float3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)),
+                       __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+                       __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ inline float plength(float3 a) { return __fsqrt_rn(pdot(a, a)); }
+__device__ inline float3 pnormalize(float3 a) {
+    const float l = plength(a);
+    return make_float3(__fdiv_rn(a.x, l), __fdiv_rn(a.y, l), __fdiv_rn(a.z, l));
+}
+
+/* intersectSegmentTriangle (rx_cu_common.cu:891-975): 1 when the segment
+ * P0 -> P1 enters the triangle from its front side (I = the crossing point,
+ * n = the unit normal), 0 when not, 2 when it lies in the triangle's plane,
+ * -1 for a degenerate triangle.  The reference lets a zero-area triangle
+ * through its zero-vector test as NaN and reports a hit at a NaN point;
+ * here it is -1. */
+__device__ inline int seg_triangle(float3 P0, float3 P1, float3 V0, float3 V1, float3 V2, float3 &I, float3 &n) {
+    const float3 u = psub(V1, V0), v = psub(V2, V0);
+    const float3 c = pcross(u, v);
+    if (pdot(c, c) == 0.0f) return -1;
+    n = pnormalize(c);
+    if (fabsf(n.x) < 1.0e-10 && fabsf(n.y) < 1.0e-10 && fabsf(n.z) < 1.0e-10) return -1;
+    const float3 dir = psub(P1, P0);
+    const float a = pdot(n, psub(P0, V0));
+    const float b = pdot(n, dir);
+    if ((double)fabsf(b) < 1e-10) return a == 0.0f ? 2 : 0;
+    const float r = __fdiv_rn(-a, b);
+    if (r < 0.0f || fabsf(a) > fabsf(b) || b > 0.0f) return 0;
+    I = padd(P0, pscale(dir, r));
+    const float uu = pdot(u, u), uv = pdot(u, v), vv = pdot(v, v);
+    const float3 w = psub(I, V0);
+    const float wu = pdot(w, u), wv = pdot(w, v);
+    const float D = __fsub_rn(__fmul_rn(uv, uv), __fmul_rn(uu, vv));
+    const float sp = __fdiv_rn(__fsub_rn(__fmul_rn(uv, wv), __fmul_rn(vv, wu)), D);
+    if (sp < 0.0f || sp > 1.0f) return 0;
+    const float tp = __fdiv_rn(__fsub_rn(__fmul_rn(uv, wu), __fmul_rn(uu, wv)), D);
+    if (tp < 0.0f || __fadd_rn(sp, tp) > 1.0f) return 0;
+    return 1;
+}
+
+/* calCollisionPolygonPB (rx_pbdsph_kernel.cu:916-936) with the reference's
+ * restitution 0 (rx_sph_pbd_gpu.cpp:103): on a hit, x1 moves back to the
+ * crossing point plus the reflected velocity over the remaining part of
+ * the step, and v loses its component into the triangle. */
+__device__ inline void polygon_hit(float3 x0, float3 &x1, float3 &v, float3 V0, float3 V1, float3 V2, float dt) {
+    float3 cp, n;
+    if (seg_triangle(x0, x1, V0, V1, V2, cp, n) != 1) return;
+    const float d = plength(psub(x1, cp));
+    n = pnormalize(n);
+    const float3 vr = pscale(pscale(n, -1.0f), pdot(n, v));
+    const float l = plength(psub(x1, x0));
+    x1 = padd(cp, pscale(vr, __fdiv_rn(__fmul_rn(dt, d), l)));
+    v = padd(v, vr);
+}
+
+/* calcGridPos / calcGridHash of the reference's GPU grid (float floor, clamped). */
+__device__ inline unsigned int poly_cell(float3 x, const PolyTable &t) {
+    int c[3];
+    const float xs[3] = {x.x, x.y, x.z}, os[3] = {t.org.x, t.org.y, t.org.z};
+    const int g[3] = {t.gx, t.gy, t.gz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float f = floorf(__fdiv_rn(__fsub_rn(xs[a], os[a]), t.cw));
+        const int k = f != f ? 0 : (int)fminf(fmaxf(f, -1.0f), (float)g[a]);
+        c[a] = k < 0 ? 0 : (k >= g[a] ? g[a] - 1 : k);
+    }
+    return ((unsigned int)c[2] * (unsigned int)t.gy + (unsigned int)c[1]) * (unsigned int)t.gx + (unsigned int)c[0];
+}
+
+/* The segment x0 -> x1 (with velocity v) against the triangles of the cells
+ * of x0 and of x1, in that order, both visited even when they are the same
+ * cell (pbdsphIntegrateWithPolygon, rx_pbdsph_kernel.cu:985-1030). */
+__device__ inline void polygon_collide(float3 x0, float3 &x1, float3 &v, float dt, const DevParams &p) {
+    const PolyTable &t = p.poly;
+    const unsigned int cells[2] = {poly_cell(x0, t), poly_cell(x1, t)};
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        const unsigned int s = t.start[cells[k]];
+        if (s == 0xffffffffu) continue;
+        const unsigned int e = t.end[cells[k]];
+        for (unsigned int j = s; j < e; ++j) {
+            const int4 tri = t.tris[t.idx[j]];
+            polygon_hit(x0, x1, v, f3(t.vrts[tri.x]), f3(t.vrts[tri.y]), f3(t.vrts[tri.z]), dt);
+        }
+    }
+}
+
 /* obstacles, then the box walls (the order of rx_sph_pbd.cpp:1380-1395) */
 __device__ inline float3 solid_project(float3 x, const DevParams &p) {
     if (p.nobs) x = obstacle_project(x, p);

@@ -669,6 +669,7 @@ __global__ void k_sph_integrate(DevParams p, const float4 *__restrict__ pos_b, c
     if (i >= p.n) return;
     float3 v = f3(vel_b[i]) + p.dt * f3(acc[i]);
     float3 x = f3(pos_b[i]) + p.dt * v;
+    if (p.ntri) polygon_collide(f3(pos_b[i]), x, v, p.dt, p); /* sphIntegrateWithPolygon, rx_sph_kernel.cu:852-895 */
     x = solid_project(x, p);
     pos_a[i] = make_float4(x.x, x.y, x.z, 0.0f);
     vel_a[i] = make_float4(v.x, v.y, v.z, 0.0f);
@@ -1116,6 +1117,21 @@ __global__ void __launch_bounds__(kBlock) k_reference_cells(int n, const float4 
         c[a] = k < 0 ? 0 : (k >= g[a] ? g[a] - 1 : k);
     }
     out[i] = ((unsigned int)c[2] * (unsigned int)gy + (unsigned int)c[1]) * (unsigned int)gx + (unsigned int)c[0];
+}
+
+/* The triangle-mesh collision alone, for parity: x1 and v updated in place
+ * from the segments x0 -> x1. */
+__global__ void __launch_bounds__(kBlock) k_polygon_collide(DevParams p, int n, const float4 *__restrict__ x0,
+                                                            float4 *__restrict__ x1, float4 *__restrict__ v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 x = f3(x1[i]), vv = f3(v[i]);
+    polygon_collide(f3(x0[i]), x, vv, p.dt, p);
+    x1[i] = make_float4(x.x, x.y, x.z, x1[i].w);
+    v[i] = make_float4(vv.x, vv.y, vv.z, v[i].w);
+}
+void launch_polygon_collide(const DevParams &p, int n, const float4 *x0, float4 *x1, float4 *v, cudaStream_t s) {
+    if (n > 0 && p.ntri) k_polygon_collide<<<blocks_for(n), kBlock, 0, s>>>(p, n, x0, x1, v);
 }
 
 void launch_reference_cells(int n, const float4 *pos, int rule, const double org[3], double cw, const int g[3],

@@ -153,6 +153,9 @@ int radix_passes(unsigned int ncells);
 void launch_radix_sort_cells(int n, const unsigned int *cell, unsigned int ncells, const RadixBufs &b,
                              unsigned int *perm, cudaStream_t s);
 
+/* ---- triangle-mesh collision of given segments (parity) ---- */
+void launch_polygon_collide(const DevParams &p, int n, const float4 *x0, float4 *x1, float4 *v, cudaStream_t s);
+
 /* ---- the reference's cell hash (rule 0: its CPU grid, 1: its GPU grid) ---- */
 void launch_reference_cells(int n, const float4 *pos, int rule, const double org[3], double cw, const int g[3],
                             unsigned int *out, cudaStream_t s);

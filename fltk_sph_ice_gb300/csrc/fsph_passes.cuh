@@ -208,8 +208,10 @@ __device__ __forceinline__ void predict_body(const DevParams &p, int i, const fl
     float3 x = f3(pos[i]);
     float3 v = f3(vel[i]);
     float3 a = acc ? f3(acc[i]) : p.gravity;
+    const float3 x_old = x;
     v = v + p.dt * a;
     x = x + p.dt * v;
+    if (p.ntri) polygon_collide(x_old, x, v, p.dt, p);
     x = solid_project(x, p);
     if (xpred_out) xpred_out[i] = make_float4(x.x, x.y, x.z, 0.0f);
     /* warm start: the iterations begin from walls(x* + predicted correction);

@@ -323,6 +323,29 @@ class rxParticleSystemBase:
         self._check(self.L.fsph_set_sphere_obstacle(self._ctx, _ptr(c), float(rad), _ptr(v), int(flg)),
                     "fsph_set_sphere_obstacle")
 
+    def SetPolygonObstacle(self, vrts, nrms, tris, vel=(0.0, 0.0, 0.0)):
+        """A triangle-mesh obstacle (rx_ps.h:268): vertices (nv, 3), normals
+        (unused, as in the reference's collision), triangles (nt, 3)."""
+        v = np.ascontiguousarray(vrts, np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+        w = np.ascontiguousarray(vel, np.float64)
+        self._check(self.L.fsph_set_polygon_obstacle(self._ctx, _ptr(v), v.shape[0], _ptr(t), t.shape[0], _ptr(w)),
+                    "fsph_set_polygon_obstacle")
+
+    def ClearPolygonObstacles(self):
+        self._check(self.L.fsph_clear_polygon_obstacles(self._ctx), "fsph_clear_polygon_obstacles")
+
+    def GetNumPolygonTriangles(self) -> int:
+        return int(self.L.fsph_num_polygon_triangles(self._ctx))
+
+    def PolygonCollide(self, x0, x1, v, dt: float):
+        """The triangle-mesh collision of the segments x0 -> x1 with velocities
+        v: returns the updated (x1, v), (n, 4) float32."""
+        a, b, c = _as4(x0), _as4(x1).copy(), _as4(v).copy()
+        self._check(self.L.fsph_polygon_collide(self._ctx, _ptr(a), _ptr(b), _ptr(c), a.shape[0], float(dt), abi.HOST),
+                    "fsph_polygon_collide")
+        return b, c
+
     def MoveSphereObstacle(self, b: int, disp):
         d = np.ascontiguousarray(disp, np.float64)
         self._check(self.L.fsph_move_sphere_obstacle(self._ctx, int(b), _ptr(d)), "fsph_move_sphere_obstacle")

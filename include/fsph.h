@@ -400,6 +400,38 @@ int fsph_get_sphere_obstacle_pos(const fsph_ctx *ctx, int b, double *pos);
 int fsph_clear_obstacles(fsph_ctx *ctx);
 int fsph_num_obstacles(const fsph_ctx *ctx);
 
+/* Triangle-mesh obstacle (SetPolygonObstacle, rx_ps.h:268;
+ * rxPBDSPH_GPU::SetPolygonObstacle, rx_sph_pbd_gpu.cpp:2367-2410): nv
+ * vertices (x, y, z doubles, stored as floats as the reference stores them)
+ * and nt triangles (three vertex indices into this mesh each), appended to
+ * the meshes already set; vel is unused, as in the reference.  The
+ * triangles are binned into the cells of the reference's GPU grid they
+ * intersect (setPolysToCell, rx_sph_pbd_gpu.cpp:2051-2200).  In the step's
+ * prediction (PBF; the WCSPH integration) each particle's segment from its
+ * position to its prediction is tested against the triangles of the cells
+ * of both ends, and a crossing from a triangle's front side puts the
+ * particle back on that side with the velocity component into the triangle
+ * removed (pbdsphIntegrateWithPolygon / calCollisionPolygonPB,
+ * rx_pbdsph_kernel.cu:916-1030; sphIntegrateWithPolygon,
+ * rx_sph_kernel.cu:852-895), before the box and sphere obstacles and the
+ * walls.  The reference re-runs that integration after every constraint
+ * iteration with zero velocity, where a zero-length segment never crosses,
+ * so only the prediction does it here.  Differences from the reference:
+ * the triangles of a later mesh index its own vertices (the reference
+ * appends them unshifted, so a second mesh points into the first);
+ * every non-empty cell of the table is closed (the reference leaves the
+ * last one open, dropping its triangles); a zero-area triangle is skipped
+ * (the reference reports a hit at a NaN point).  Synchronises. */
+int fsph_set_polygon_obstacle(fsph_ctx *ctx, const double *vrts, int nv, const int *tris, int nt,
+                              const double *vel);
+int fsph_clear_polygon_obstacles(fsph_ctx *ctx);
+int fsph_num_polygon_triangles(const fsph_ctx *ctx);
+/* The collision of the triangle meshes alone, for parity: for each of n
+ * segments x0[i] -> x1[i] (float4 stride) with velocity v[i], x1 and v are
+ * updated in place as the prediction does (host or device arrays per
+ * `where`).  Synchronises. */
+int fsph_polygon_collide(fsph_ctx *ctx, const float *x0_4, float *x1_4, float *v4, int n, float dt, int where);
+
 /* ---- learned warm start ---- */
 /* The network: FSPH_MLP_FEATURES -> 64 -> 64 -> 3, ReLU, BF16 tensor-core
  * arithmetic with FP32 accumulation.  Its parameters are one FP32 blob of

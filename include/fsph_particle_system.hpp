@@ -308,6 +308,19 @@ public:
         m_status = fsph_get_sphere_obstacle_pos(m_ctx, b, p.data);
         return p;
     }
+    /* SetPolygonObstacle(vrts, nrms, tris, vel) (rx_ps.h:268): a triangle
+     * mesh; the normals and the velocity are unused, as in the reference */
+    template <class VV, class VN, class VT, class V1>
+    void SetPolygonObstacle(const VV &vrts, const VN &nrms, const VT &tris, const V1 &vel) {
+        (void)nrms;
+        std::vector<double> v;
+        std::vector<int> t;
+        for (const auto &p : vrts) { const Vec3 q(p); v.insert(v.end(), q.data, q.data + 3); }
+        for (const auto &f : tris) for (int k = 0; k < 3; ++k) t.push_back((int)f[k]);
+        const Vec3 w(vel);
+        m_status = fsph_set_polygon_obstacle(m_ctx, v.data(), (int)(v.size() / 3), t.data(), (int)(t.size() / 3),
+                                             w.data);
+    }
 
     /* -- density on a lattice for meshing (rx_ps.h:280-285) ------------- */
     /* hF[k n0 n1 + j n0 + i] = density at minp + (i, j, k) d (host array) */

@@ -67,6 +67,8 @@ def orc_lib() -> ctypes.CDLL:
         L.fsph_orc_set_obstacles.argtypes = [vp, vp, ci]
         L.fsph_orc_project.argtypes = [vp, vp, ci, vp]
         L.fsph_orc_density_grid.argtypes = [vp, vp, vp, vp, vp]
+        L.fsph_orc_set_polygons.argtypes = [vp, vp, ci, vp, ci]
+        L.fsph_orc_polygon_collide.argtypes = [vp, vp, vp, vp, ci, cf]
         L.fsph_orc_neighbors.argtypes = [vp, vp, vp, vp, ctypes.c_longlong]
         L.fsph_orc_neighbors.restype = ctypes.c_longlong
         L.fsph_orc_pbf_lambda.argtypes = [vp, vp, vp, vp]
@@ -145,6 +147,19 @@ class Oracle:
         self.L.fsph_orc_density_grid(self.h, _vp(nn), _vp(np.ascontiguousarray(minp, np.float64)),
                                      _vp(np.ascontiguousarray(d, np.float64)), _vp(out))
         return out.reshape(nn[2], nn[1], nn[0])
+
+    def set_polygons(self, vrts, tris):
+        """Triangle-mesh obstacles (vertices stored as floats, as the product does)."""
+        v = np.ascontiguousarray(vrts, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+        self.L.fsph_orc_set_polygons(self.h, _vp(v), v.shape[0], _vp(t), t.shape[0])
+
+    def polygon_collide(self, x0, x1, v, dt):
+        a = np.ascontiguousarray(x0, np.float32)
+        b = np.array(x1, np.float32, copy=True)
+        c = np.array(v, np.float32, copy=True)
+        self.L.fsph_orc_polygon_collide(self.h, _vp(a), _vp(b), _vp(c), a.shape[0], dt)
+        return b, c
 
     def project(self, pos4):
         """The solid projection (obstacles, then the box walls) of the given points."""

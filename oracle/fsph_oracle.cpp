@@ -94,6 +94,197 @@ struct Kern {
 template <class T>
 inline void acc_add(T &a, double term) { a = (T)((double)a + term); }
 
+/* Triangle-mesh obstacles, the reference's GPU rule (rxPBDSPH_GPU::
+ * SetPolygonObstacle / setPolysToCell, rx_sph_pbd_gpu.cpp:2051-2200, 2367-2410;
+ * pbdsphIntegrateWithPolygon / calCollisionPolygonPB, rx_pbdsph_kernel.cu:
+ * 916-1030; intersectSegmentTriangle, rx_cu_common.cu:891-975), restated in
+ * T arithmetic, one rounding per operation: the triangles are binned into the
+ * cells of the reference's GPU grid that they intersect; a segment x0 -> x1
+ * is tested against the triangles of the cells of x0 and of x1, in that order
+ * (both, even when equal), each in ascending triangle index, and a crossing
+ * from a triangle's front side moves x1 back to that side with the velocity
+ * component into the triangle removed (restitution 0).  Zero-area triangles
+ * are skipped. */
+template <class T>
+struct PolyMesh {
+    struct P3 {
+        T x, y, z;
+    };
+    static P3 sub(P3 a, P3 b) { return P3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+    static P3 add(P3 a, P3 b) { return P3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+    static P3 scl(P3 a, T s) { return P3{a.x * s, a.y * s, a.z * s}; }
+    static T dot(P3 a, P3 b) {
+        T s = a.x * b.x;
+        s = s + a.y * b.y;
+        return s + a.z * b.z;
+    }
+    static P3 crs(P3 a, P3 b) { return P3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+    static T len(P3 a) { return std::sqrt(dot(a, a)); }
+    static P3 unit(P3 a) {
+        T l = len(a);
+        return P3{a.x / l, a.y / l, a.z / l};
+    }
+
+    int nt = 0;
+    std::vector<P3> V;                 /* vertices, rounded to float as stored */
+    std::vector<int> tri;              /* 3 per triangle */
+    std::vector<unsigned int> start, end, idx;
+    double org[3] = {0, 0, 0};
+    T orgT[3] = {0, 0, 0}, cw = 0;
+    int g[3] = {1, 1, 1};
+
+    /* separating axes of a triangle against the cube [-0.5, 0.5]^3 */
+    static bool overlap(const double v[3][3]) {
+        for (int a = 0; a < 3; ++a) {
+            double mn = std::min(v[0][a], std::min(v[1][a], v[2][a]));
+            double mx = std::max(v[0][a], std::max(v[1][a], v[2][a]));
+            if (mn > 0.5 || mx < -0.5) return false;
+        }
+        double e[3][3];
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) e[k][a] = v[(k + 1) % 3][a] - v[k][a];
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                double ax[3] = {0, 0, 0};
+                ax[(a + 1) % 3] = -e[k][(a + 2) % 3];
+                ax[(a + 2) % 3] = e[k][(a + 1) % 3];
+                double mn = 1e300, mx = -1e300;
+                for (int j = 0; j < 3; ++j) {
+                    double q = ax[0] * v[j][0] + ax[1] * v[j][1] + ax[2] * v[j][2];
+                    mn = std::min(mn, q);
+                    mx = std::max(mx, q);
+                }
+                double r = 0.5 * (std::fabs(ax[0]) + std::fabs(ax[1]) + std::fabs(ax[2]));
+                if (mn > r || mx < -r) return false;
+            }
+        double nr[3] = {e[0][1] * e[1][2] - e[0][2] * e[1][1], e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                        e[0][0] * e[1][1] - e[0][1] * e[1][0]};
+        double dp = nr[0] * v[0][0] + nr[1] * v[0][1] + nr[2] * v[0][2];
+        return std::fabs(dp) <= 0.5 * (std::fabs(nr[0]) + std::fabs(nr[1]) + std::fabs(nr[2]));
+    }
+
+    /* vertices as stored (floats), triangles, the grid over the box grown by
+     * 1 % (rx_sph_pbd_gpu.cpp:248-262, 1986-2011) */
+    void set(const float *v3f, int nv, const int *t, int ntri, const fsph_params &P) {
+        nt = ntri;
+        V.resize(nv);
+        for (int k = 0; k < nv; ++k) V[k] = P3{(T)v3f[3 * k], (T)v3f[3 * k + 1], (T)v3f[3 * k + 2]};
+        tri.assign(t, t + 3 * (size_t)ntri);
+        double lo[3], ws[3];
+        for (int a = 0; a < 3; ++a) {
+            double size = P.box_max[a] - P.box_min[a];
+            lo[a] = P.box_min[a] - 0.5 * 0.01 * size;
+            double hi = lo[a] + size * (1.0 + 0.01);
+            ws[a] = hi - lo[a];
+        }
+        double h = (double)P.h;
+        double max_axis = std::max(ws[0], std::max(ws[1], ws[2]));
+        int d = (int)(std::log(max_axis / h) / std::log(2.0) + 0.5);
+        int m = (int)(std::pow(2.0, (double)d) + 0.5);
+        double cwd = max_axis / m;
+        float cwf = (float)cwd;
+        cw = (T)cwf;
+        for (int a = 0; a < 3; ++a) {
+            org[a] = lo[a];
+            orgT[a] = (T)(float)lo[a];
+            g[a] = (int)(ws[a] / cwd) + 1;
+        }
+        double L = (double)cwf;
+        size_t ncell = (size_t)g[0] * g[1] * g[2];
+        start.assign(ncell, 0xffffffffu);
+        end.assign(ncell, 0u);
+        std::vector<std::vector<unsigned int>> per(ncell);
+        for (int i = 0; i < ntri; ++i) {
+            double P0[3][3];
+            for (int j = 0; j < 3; ++j) {
+                const float *q = v3f + 3 * (size_t)t[3 * i + j];
+                for (int a = 0; a < 3; ++a) P0[j][a] = (double)q[a];
+            }
+            int l0[3], h0[3];
+            for (int a = 0; a < 3; ++a) {
+                double b0 = std::min(P0[0][a], std::min(P0[1][a], P0[2][a])) - org[a];
+                double b1 = std::max(P0[0][a], std::max(P0[1][a], P0[2][a])) - org[a];
+                double f0 = std::max(std::min(b0 / L, (double)g[a]), -1.0), f1 = std::max(std::min(b1 / L, (double)g[a]), -1.0);
+                l0[a] = std::min(std::max((int)f0, 0), g[a] - 1);
+                h0[a] = std::min(std::max((int)f1, 0), g[a] - 1);
+            }
+            for (int x = l0[0]; x <= h0[0]; ++x)
+                for (int y = l0[1]; y <= h0[1]; ++y)
+                    for (int z = l0[2]; z <= h0[2]; ++z) {
+                        double cen[3] = {org[0] + (x + 0.5) * L, org[1] + (y + 0.5) * L, org[2] + (z + 0.5) * L};
+                        double vc[3][3];
+                        for (int j = 0; j < 3; ++j)
+                            for (int a = 0; a < 3; ++a) vc[j][a] = (P0[j][a] - cen[a]) / L;
+                        if (overlap(vc)) per[((size_t)z * g[1] + y) * g[0] + x].push_back((unsigned int)i);
+                    }
+        }
+        idx.clear();
+        for (size_t c = 0; c < ncell; ++c) {
+            if (per[c].empty()) continue;
+            start[c] = (unsigned int)idx.size();
+            idx.insert(idx.end(), per[c].begin(), per[c].end());
+            end[c] = (unsigned int)idx.size();
+        }
+    }
+
+    size_t cell(P3 x) const {
+        T xs[3] = {x.x, x.y, x.z};
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+            T f = std::floor((xs[a] - orgT[a]) / cw);
+            f = std::max(std::min(f, (T)g[a]), (T)-1);
+            int k = (int)f;
+            c[a] = k < 0 ? 0 : (k >= g[a] ? g[a] - 1 : k);
+        }
+        return ((size_t)c[2] * g[1] + c[1]) * g[0] + c[0];
+    }
+
+    static int seg_tri(P3 P0, P3 P1, P3 V0, P3 V1, P3 V2, P3 &I, P3 &n) {
+        P3 u = sub(V1, V0), v = sub(V2, V0);
+        P3 c = crs(u, v);
+        if (dot(c, c) == (T)0) return -1;
+        n = unit(c);
+        P3 dir = sub(P1, P0);
+        T a = dot(n, sub(P0, V0));
+        T b = dot(n, dir);
+        if ((double)std::fabs(b) < 1e-10) return a == (T)0 ? 2 : 0;
+        T r = -a / b;
+        if (r < (T)0 || std::fabs(a) > std::fabs(b) || b > (T)0) return 0;
+        I = add(P0, scl(dir, r));
+        T uu = dot(u, u), uv = dot(u, v), vv = dot(v, v);
+        P3 w = sub(I, V0);
+        T wu = dot(w, u), wv = dot(w, v);
+        T D = uv * uv - uu * vv;
+        T s = (uv * wv - vv * wu) / D;
+        if (s < (T)0 || s > (T)1) return 0;
+        T t = (uv * wu - uu * wv) / D;
+        if (t < (T)0 || s + t > (T)1) return 0;
+        return 1;
+    }
+
+    /* x0, x1, v in double from the caller; rounded to T first */
+    void collide(V3 x0d, V3 &x1d, V3 &vd, T dt) const {
+        P3 x0{(T)x0d.x, (T)x0d.y, (T)x0d.z}, x1{(T)x1d.x, (T)x1d.y, (T)x1d.z}, v{(T)vd.x, (T)vd.y, (T)vd.z};
+        const size_t cells[2] = {cell(x0), cell(x1)};
+        for (int k = 0; k < 2; ++k) {
+            if (start[cells[k]] == 0xffffffffu) continue;
+            for (unsigned int j = start[cells[k]]; j < end[cells[k]]; ++j) {
+                const int t = (int)idx[j];
+                P3 cp, n;
+                if (seg_tri(x0, x1, V[tri[3 * t]], V[tri[3 * t + 1]], V[tri[3 * t + 2]], cp, n) != 1) continue;
+                T d = len(sub(x1, cp));
+                n = unit(n);
+                P3 vr = scl(scl(n, (T)-1), dot(n, v));
+                T l = len(sub(x1, x0));
+                x1 = add(cp, scl(vr, (dt * d) / l));
+                v = add(v, vr);
+            }
+        }
+        x1d = v3((double)x1.x, (double)x1.y, (double)x1.z);
+        vd = v3((double)v.x, (double)v.y, (double)v.z);
+    }
+};
+
 template <class T>
 struct Solver {
     fsph_params P;
@@ -113,6 +304,8 @@ struct Solver {
         double cen[3], ext[3], R[3][3], rad;
     };
     std::vector<Obs> obs;
+    /* triangle-mesh obstacles (see PolyMesh) */
+    PolyMesh<T> mesh;
     int last_iters = 0;
     double last_err1 = 0, last_err2 = 0, last_errmax = 0;
 
@@ -369,8 +562,10 @@ struct Solver {
                    std::vector<T> &x1, std::vector<T> &v1, T dt) {
         for (int i = 0; i < n; ++i) {
             V3 x = at(x0, i), v = at(v0, i), a = at(a0, i);
+            const V3 xo = x;
             v = v + (double)dt * a;
             x = x + (double)dt * v;
+            if (mesh.nt) mesh.collide(xo, x, v, dt); /* in T arithmetic from the rounded end points */
             x = wall(x);
             size_t b = 4 * (size_t)i;
             x1[b] = (T)x.x; x1[b + 1] = (T)x.y; x1[b + 2] = (T)x.z;
@@ -897,6 +1092,30 @@ void fsph_orc_sph_step(fsph_orc *o, float dt) { ORC_DISPATCH(o, S->sph_step(dt))
 void fsph_orc_set_obstacles(fsph_orc *o, const double *rec, int n) {
     if (o->prec) set_obstacles((Solver<double> *)o->s, rec, n);
     else set_obstacles((Solver<float> *)o->s, rec, n);
+}
+
+/* Triangle-mesh obstacles: nv float vertices (xyz), nt triangles (3 ints);
+ * replaces any mesh set before. */
+void fsph_orc_set_polygons(fsph_orc *o, const float *vrts, int nv, const int *tris, int nt) {
+    ORC_DISPATCH(o, S->mesh.set(vrts, nv, tris, nt, S->P));
+}
+
+/* The mesh collision alone: x1 and v (float4 stride) updated from x0 -> x1. */
+extern "C++" template <class T>
+void polygon_collide(Solver<T> *S, const float *x0, float *x1, float *v, int n, float dt) {
+    for (int i = 0; i < n; ++i) {
+        const size_t b = 4 * (size_t)i;
+        V3 a = v3(x0[b], x0[b + 1], x0[b + 2]);
+        V3 c = v3(x1[b], x1[b + 1], x1[b + 2]);
+        V3 w = v3(v[b], v[b + 1], v[b + 2]);
+        if (S->mesh.nt) S->mesh.collide(a, c, w, (T)dt);
+        x1[b] = (float)c.x; x1[b + 1] = (float)c.y; x1[b + 2] = (float)c.z;
+        v[b] = (float)w.x; v[b + 1] = (float)w.y; v[b + 2] = (float)w.z;
+    }
+}
+void fsph_orc_polygon_collide(fsph_orc *o, const float *x0, float *x1, float *v, int n, float dt) {
+    if (o->prec) polygon_collide((Solver<double> *)o->s, x0, x1, v, n, dt);
+    else polygon_collide((Solver<float> *)o->s, x0, x1, v, n, dt);
 }
 
 /* rxPBDSPH::CalImplicitField of the current positions (see Solver::density_grid). */

@@ -61,6 +61,15 @@ int main(int argc, char **argv) {
     m_pPS->AddBox(-1, cen, Vec3(0.08, 0.08, 0.08), Vec3(0.0), pr * 2.0f);
     const int n0 = m_pPS->GetNumParticles();
     if (n0 <= 0) { std::fprintf(stderr, "AddBox placed no particles\n"); return 1; }
+    // a polygon obstacle as the scene loader hands one over (vertices, normals, index triples)
+    {
+        std::vector<Vec3> vrts = {m_pPS->GetMax() - Vec3(0.1, 0.1, 0.1), m_pPS->GetMax() - Vec3(0.02, 0.1, 0.1),
+                                  m_pPS->GetMax() - Vec3(0.1, 0.02, 0.1)};
+        std::vector<Vec3> nrms(3, Vec3(0.0, 0.0, 1.0));
+        std::vector<std::vector<int> > tris = {{0, 1, 2}};
+        m_pPS->SetPolygonObstacle(vrts, nrms, tris, Vec3(0.0));
+        if (m_pPS->LastStatus() != FSPH_OK) { std::fprintf(stderr, "SetPolygonObstacle failed\n"); return 1; }
+    }
     lap("scene placed");
 
     // StepPS

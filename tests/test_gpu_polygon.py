@@ -1,0 +1,129 @@
+"""Triangle-mesh obstacles on the GPU (fsph_set_polygon_obstacle;
+SetPolygonObstacle, rx_ps.h:268): the collision alone bit for bit against
+the numpy restatement of the reference's GPU rule (which pins the oracle,
+tests/test_polygon_oracle.py), and PBF / WCSPH steps onto a ramp against
+the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import assert_rel
+from fltk_sph_ice_gb300 import FsphError, abi, rxPBDSPH, rxSPH, scenes
+from test_polygon_oracle import collide_numpy, ramp_mesh, segments
+
+pytestmark = pytest.mark.gpu
+
+
+def test_collision_bit_exact(gpu):
+    sc = scenes.pbf_double_dam_break(block=(8, 8, 16))
+    p = sc.params
+    V, T = ramp_mesh(p)
+    x0, x1, v = segments(p, V, T)
+    ps = rxPBDSPH(p)
+    ps.SetPolygonObstacle(V, None, T)
+    assert ps.GetNumPolygonTriangles() == len(T)
+    gx, gv = ps.PolygonCollide(x0, x1, v, 0.0016)
+    wx, wv, hits = collide_numpy(p, V, T, x0, x1, v, 0.0016)
+    assert hits > 500
+    assert np.array_equal(gx[:, :3], wx[:, :3]) and np.array_equal(gv[:, :3], wv[:, :3])
+    ps.ClearPolygonObstacles()
+    gx2, _ = ps.PolygonCollide(x0, x1, v, 0.0016)
+    assert np.array_equal(gx2, x1)
+
+
+def test_second_mesh_indexes_its_own_vertices(gpu):
+    """Two meshes set one after the other act as their union (the reference
+    appends the second mesh's indices unshifted)."""
+    sc = scenes.pbf_double_dam_break(block=(8, 8, 16))
+    p = sc.params
+    V, T = ramp_mesh(p)
+    x0, x1, v = segments(p, V, T)
+    a = rxPBDSPH(p)
+    a.SetPolygonObstacle(V, None, T)
+    b = rxPBDSPH(p)
+    b.SetPolygonObstacle(V[:4], None, T[:2])
+    b.SetPolygonObstacle(V[4:], None, T[2:] - 4)
+    ga, _ = a.PolygonCollide(x0, x1, v, 0.0016)
+    gb, _ = b.PolygonCollide(x0, x1, v, 0.0016)
+    assert np.array_equal(ga, gb)
+    with pytest.raises(FsphError):
+        b.SetPolygonObstacle(V[:3], None, [[0, 1, 3]])  # index outside the mesh
+    assert b.GetNumPolygonTriangles() == len(T)
+
+
+def _ramp_scene(solver):
+    h = scenes.H_DEFAULT
+    s = 0.5 * h
+    box_max = [0.8, 0.8, 0.5]
+    pos = scenes.lattice_block([0.2, 0.5, 0.12], (14, 10, 12), s, 0.01 * h, 4, 0)
+    p = scenes.pbf_params(h, [0, 0, 0], box_max, pos.shape[0])
+    p.eta, p.min_iter, p.max_iter = 0.0, 4, 4
+    p.xsph_c, p.vort_eps = 0.0, 0.0
+    if solver == "sph":
+        p.solver = abi.SOLVER_WCSPH
+        p.mass, p.gas_k, p.viscosity = 0.02, 3.0, 3.5 / scenes.REST_DENS
+    vel = np.zeros_like(pos)
+    vel[:, 1] = -1.0
+    V, T = ramp_mesh(p)
+    return p, pos, vel, V[:4], T[:2]  # the ramp alone: no edge of it within reach of the block
+
+
+@pytest.mark.parametrize("solver", ["pbf", "sph"])
+def test_ramp_steps_match_oracle(gpu, solver):
+    p, pos, vel, V, T = _ramp_scene(solver)
+    cls = rxPBDSPH if solver == "pbf" else rxSPH
+    ps = cls(p)
+    ps.Set(pos, vel)
+    ps.SetPolygonObstacle(V, None, T)
+    o = oracle.Oracle(p, pos.shape[0], threads=4)
+    o.set(pos, vel)
+    o.set_polygons(V, T)
+    dt = 0.0016 if solver == "pbf" else 0.001
+    up = np.cross(V[3] - V[0], V[1] - V[0])
+    up /= np.linalg.norm(up)
+    for k in range(30):
+        ps.Update(dt)
+        if solver == "pbf":
+            o.pbf_step(dt, fixed_iters=4)
+        else:
+            o.sph_step(dt)
+    xg, xo = ps.GetArrayVBO(abi.RX_POSITION)[:, :3], o.get("pos")[:, :3]
+    near = np.abs((xo - V[0]) @ up) < 0.02
+    assert near.sum() > 50  # the block reached the ramp
+    assert_rel(xg, xo, 2e-4, f"{solver}: positions after 30 steps onto the ramp")
+
+
+def test_wcsph_does_not_cross_the_ramp(gpu):
+    p, pos, vel, V, T = _ramp_scene("sph")
+    ps = rxSPH(p)
+    ps.Set(pos, vel)
+    ps.SetPolygonObstacle(V, None, T)
+    up = np.cross(V[3] - V[0], V[1] - V[0])
+    up /= np.linalg.norm(up)
+    inside = lambda x: ((x[:, 0] > V[0, 0]) & (x[:, 0] < V[1, 0]) & (x[:, 2] > V[0, 2]) & (x[:, 2] < V[3, 2]))  # noqa: E731
+    for _ in range(150):
+        ps.Update(0.001)
+        x = ps.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64)
+        side = (x - V[0]) @ up
+        assert (side[inside(x)] > -1e-5).all(), "a particle crossed the ramp"
+
+
+def test_polygons_follow_params_and_state(gpu, tmp_path):
+    p, pos, vel, V, T = _ramp_scene("pbf")
+    ps = rxPBDSPH(p)
+    ps.Set(pos, vel)
+    ps.SetPolygonObstacle(V, None, T)
+    q = abi.FsphParams.from_buffer_copy(p)
+    q.h = p.h * 1.2  # another grid: the table is rebuilt on it
+    ps.SetParams(q)
+    x0, x1, v = segments(q, V, T)
+    gx, _ = ps.PolygonCollide(x0, x1, v, 0.0016)
+    wx, _, _ = collide_numpy(q, V, T, x0, x1, v, 0.0016)
+    assert np.array_equal(gx[:, :3], wx[:, :3])
+    path = str(tmp_path / "poly.state")
+    ps.SaveState(path)
+    fresh = rxPBDSPH(p)
+    fresh.LoadState(path)
+    assert fresh.GetNumPolygonTriangles() == len(T)
+    fx, _ = fresh.PolygonCollide(x0, x1, v, 0.0016)
+    assert np.array_equal(fx, gx)

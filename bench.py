@@ -286,7 +286,7 @@ def run_leg(ctx, warm: bool, blob):
         step()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    iters, errs, kernels, builds = [], [], [], []
+    iters, errs, kernels, builds, unconv = [], [], [], [], 0
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -302,6 +302,7 @@ def run_leg(ctx, warm: bool, blob):
         errs.append(stats.density_error_one_sided)
         kernels.append(stats.kernels)
         builds.append(stats.grid_builds)
+        unconv += int(stats.status == abi.NOT_CONVERGED)
     torch.cuda.synchronize()
     tot_ms = sum(a.elapsed_time(b) for a, b in ev)
     n = sc.n
@@ -309,7 +310,8 @@ def run_leg(ctx, warm: bool, blob):
     tot_ms = secs * 1000.0
     return ps, sc, {"value": value, "ms_per_step": tot_ms / args.steps,
                     "mean_iterations": float(np.mean(iters)), "max_error": float(np.max(errs)),
-                    "iterations": iters, "kernels": int(sum(kernels)), "grid_builds": float(np.mean(builds))}
+                    "iterations": iters, "kernels": int(sum(kernels)), "grid_builds": float(np.mean(builds)),
+                    "not_converged_steps": unconv, "status": "FSPH_NOT_CONVERGED" if unconv else "FSPH_OK"}
 
 
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "k_lambda_k_correction_pbf_double_dam_break_1M.md")

@@ -153,7 +153,7 @@ EXPORTS = [
     "fsph_clear_obstacles", "fsph_num_obstacles", "fsph_density_grid", "fsph_num_active", "fsph_add_delete_region",
     "fsph_clear_delete_regions", "fsph_add_inlet_line", "fsph_clear_inlets", "fsph_emit_inlets",
     "fsph_set_step_log", "fsph_set_alloc_fault", "fsph_reference_cell_hash", "fsph_save_state", "fsph_load_state",
-    "fsph_set_polygon_obstacle", "fsph_clear_polygon_obstacles", "fsph_num_polygon_triangles", "fsph_polygon_collide",
+    "fsph_set_polygon_obstacle", "fsph_clear_polygon_obstacles", "fsph_num_polygon_triangles", "fsph_polygon_collide", "fsph_num_inlets",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
     "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
     "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
@@ -219,6 +219,7 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_save_state.argtypes = [c_void_p, ctypes.c_char_p]
     L.fsph_set_polygon_obstacle.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]
     L.fsph_clear_polygon_obstacles.argtypes = [c_void_p]
+    L.fsph_num_inlets.argtypes = [c_void_p]
     L.fsph_num_polygon_triangles.argtypes = [c_void_p]
     L.fsph_polygon_collide.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_int]
     L.fsph_load_state.argtypes = [c_void_p, ctypes.c_char_p]
@@ -270,7 +271,7 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
                  "fsph_clear_delete_regions", "fsph_add_inlet_line", "fsph_clear_inlets", "fsph_emit_inlets",
                  "fsph_set_step_log", "fsph_set_alloc_fault", "fsph_reference_cell_hash", "fsph_save_state",
                  "fsph_load_state", "fsph_set_polygon_obstacle", "fsph_clear_polygon_obstacles",
-                 "fsph_num_polygon_triangles", "fsph_polygon_collide"]:
+                 "fsph_num_polygon_triangles", "fsph_polygon_collide", "fsph_num_inlets"]:
         getattr(L, name).restype = c_int
     return L
 

@@ -2117,13 +2117,14 @@ int fsph_clear_delete_regions(fsph_ctx *c) {
 
 int fsph_add_inlet_line(fsph_ctx *c, const double *pos1, const double *pos2, const double *vel, const double *up,
                         int accum, int span, double spacing) {
-    if (!c || !pos1 || !pos2 || !vel || !up) return FSPH_INVALID_ARG;
-    if (accum < 1 || span < 0 || !(spacing >= 0.0)) return fail(c, FSPH_INVALID_ARG, "inlet: accum >= 1, span >= 0");
+    /* the count of lines is returned, so a failure is the negated status */
+    if (!c || !pos1 || !pos2 || !vel || !up) return -FSPH_INVALID_ARG;
+    if (accum < 1 || span < 0 || !(spacing >= 0.0)) return -fail(c, FSPH_INVALID_ARG, "inlet: accum >= 1, span >= 0");
     fsph_ctx::Inlet q;
     for (int a = 0; a < 3; ++a) {
         q.pos1[a] = pos1[a]; q.pos2[a] = pos2[a]; q.vel[a] = vel[a]; q.up[a] = up[a];
         if (!std::isfinite(pos1[a]) || !std::isfinite(pos2[a]) || !std::isfinite(vel[a]) || !std::isfinite(up[a]))
-            return fail(c, FSPH_INVALID_ARG, "inlet: finite vectors");
+            return -fail(c, FSPH_INVALID_ARG, "inlet: finite vectors");
     }
     q.accum = accum; q.span = span; q.spacing = spacing;
     c->inlets.push_back(q);
@@ -2136,6 +2137,8 @@ int fsph_clear_inlets(fsph_ctx *c) {
     c->inlet_start = -1;
     return FSPH_OK;
 }
+
+int fsph_num_inlets(const fsph_ctx *c) { return c ? (int)c->inlets.size() : -1; }
 
 namespace {
 /* U[0, 1) from (seed, index): the SplitMix64 finaliser */

@@ -46,13 +46,16 @@ constexpr int kBatch = FSPH_KBATCH;
 #endif
 /* FSPH_PERSIST_LAMBDA / FSPH_PERSIST_CORRECTION 1: that single-scene
  * constraint pass runs as many blocks as are resident on the GPU, each warp
- * taking 32-slot chunks round-robin (FSPH_PERSIST sets both) */
+ * taking 32-slot chunks round-robin (FSPH_PERSIST sets both).  Measured on
+ * the 1M double dam break: lambda 92 -> 82 us with identical results, so on
+ * by default; the correction pass gains nothing (89 us either way) and its
+ * persistent form was 7 % slower in an earlier form, so off. */
 #ifdef FSPH_PERSIST
 #define FSPH_PERSIST_LAMBDA FSPH_PERSIST
 #define FSPH_PERSIST_CORRECTION FSPH_PERSIST
 #endif
 #ifndef FSPH_PERSIST_LAMBDA
-#define FSPH_PERSIST_LAMBDA 0
+#define FSPH_PERSIST_LAMBDA 1
 #endif
 #ifndef FSPH_PERSIST_CORRECTION
 #define FSPH_PERSIST_CORRECTION 0

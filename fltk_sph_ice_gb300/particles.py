@@ -166,8 +166,8 @@ class rxParticleSystemBase:
         a, b, v, u = d(pos1), d(pos2), d(vel), d(up)
         k = self.L.fsph_add_inlet_line(self._ctx, _ptr(a), _ptr(b), _ptr(v), _ptr(u), int(accum), int(span),
                                        float(spacing))
-        if k <= 0:
-            self._check(k if k else abi.INVALID_ARG, "fsph_add_inlet_line")
+        if k <= 0:  # a negated status
+            self._check(-k if k else abi.INVALID_ARG, "fsph_add_inlet_line")
         self._inlets = k
         return k
 
@@ -193,6 +193,7 @@ class rxParticleSystemBase:
 
     def LoadState(self, path: str):
         self._check(self.L.fsph_load_state(self._ctx, os.fsencode(path)), "fsph_load_state")
+        self._inlets = int(self.L.fsph_num_inlets(self._ctx))  # the state's inlet lines emit from here on
 
     def OutputParticles(self, path: str):
         """The reference's particle file (rx_ps.cpp:581-612): uint32 N, N x 3

@@ -274,7 +274,7 @@ public:
         const int k = fsph_add_inlet_line(m_ctx, line.pos1.data, line.pos2.data, line.vel.data, line.up.data,
                                           line.accum, line.span, line.spacing);
         if (k > 0) m_inlets = k;
-        else m_status = k;
+        else m_status = -k; /* a negated status */
         return k;
     }
     /* the particles that take part in the steps (deleted ones excluded) */
@@ -472,6 +472,7 @@ public:
         }
         m_status = fsph_load_state(m_ctx, (fn + ".state").c_str());
         if (m_status == FSPH_OK) {
+            m_inlets = fsph_num_inlets(m_ctx);
             const fsph_params p = params();
             m_use_vorticity = p.vort_eps != 0.0f;
             m_artificial_pressure = p.use_ap != 0;

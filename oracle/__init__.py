@@ -47,6 +47,14 @@ def _vp(a):
     return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _f4(a, n: int) -> np.ndarray:
+    """a contiguous float32 (n, 4) array (the C side reads 4 n floats)"""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.shape != (n, 4):
+        raise ValueError(f"expected a float4 array of shape ({n}, 4), got {a.shape}")
+    return a
+
+
 def orc_lib() -> ctypes.CDLL:
     global _orc
     if _orc is None:
@@ -102,7 +110,7 @@ class Oracle:
             self.h = None
 
     def set(self, pos4, vel4=None):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         vel4 = None if vel4 is None else np.ascontiguousarray(vel4, dtype=np.float32)
         self.L.fsph_orc_set(self.h, _vp(pos4), _vp(vel4))
 
@@ -163,14 +171,14 @@ class Oracle:
 
     def project(self, pos4):
         """The solid projection (obstacles, then the box walls) of the given points."""
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, len(pos4))
         out = np.zeros_like(pos4)
         self.L.fsph_orc_project(self.h, _vp(pos4), pos4.shape[0], _vp(out))
         return out
 
     def finalize_ext(self, pos4, vel4, dens, dt: float):
         """XSPH + vorticity confinement alone on the given state: (velocity after both, omega)."""
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
         dens = np.ascontiguousarray(dens, dtype=np.float32)
         vo = np.zeros((self.n, 4), np.float32)
@@ -179,7 +187,7 @@ class Oracle:
         return vo, om
 
     def neighbors(self, pos4):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         off = np.zeros(self.n + 1, dtype=np.int32)
         cap = self.n * 80
         idx = np.zeros(cap, dtype=np.int32)
@@ -190,21 +198,21 @@ class Oracle:
         return off, idx[:t]
 
     def lambda_pass(self, pos4):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         d = np.zeros(self.n, np.float32)
         l = np.zeros(self.n, np.float32)
         self.L.fsph_orc_pbf_lambda(self.h, _vp(pos4), _vp(d), _vp(l))
         return d, l
 
     def correction_pass(self, pos4, lam, dt):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         lam = np.ascontiguousarray(lam, dtype=np.float32)
         dp = np.zeros((self.n, 4), np.float32)
         self.L.fsph_orc_pbf_correction(self.h, _vp(pos4), _vp(lam), dt, _vp(dp))
         return dp
 
     def sph_forces(self, pos4, vel4):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
         d = np.zeros(self.n, np.float32)
         p = np.zeros(self.n, np.float32)
@@ -310,7 +318,7 @@ class RefSolver:
             self.h = None
 
     def set(self, pos4, vel4=None):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         vel4 = np.zeros_like(pos4) if vel4 is None else np.ascontiguousarray(vel4, dtype=np.float32)
         getattr(self.L, f"fsph_ref_{self.kind}_set")(self.h, self.n, _vp(pos4), _vp(vel4))
 
@@ -341,13 +349,13 @@ class RefSolver:
     def cell_hash(self, pos4):
         """rxNNGrid::CalGridHash(Vec3) of each position on the reference's CPU
         grid, and that grid's cell count."""
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, len(pos4))
         out = np.zeros(pos4.shape[0], np.uint32)
         cells = self.L.fsph_ref_cell_hash(self.h, _vp(pos4), pos4.shape[0], _vp(out))
         return out, int(cells)
 
     def neighbors(self, pos4):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         off = np.zeros(self.n + 1, dtype=np.int32)
         cap = self.n * 80
         idx = np.zeros(cap, dtype=np.int32)
@@ -357,14 +365,14 @@ class RefSolver:
         return off, idx[:t], d2[:t]
 
     def lambda_pass(self, pos4, dt):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         d = np.zeros(self.n, np.float32)
         l = np.zeros(self.n, np.float32)
         self.L.fsph_ref_pbf_lambda(self.h, _vp(pos4), self.n, dt, _vp(d), _vp(l))
         return d, l
 
     def correction_pass(self, pos4, lam, dt):
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, self.n)
         lam = np.ascontiguousarray(lam, dtype=np.float32)
         dp = np.zeros((self.n, 4), np.float32)
         self.L.fsph_ref_pbf_dp(self.h, _vp(pos4), _vp(lam), self.n, dt, _vp(dp))
@@ -373,7 +381,7 @@ class RefSolver:
     def density_grid(self, pos4, n, minp, d):
         """rxPBDSPH::CalImplicitField of the given particles on an n[0] x n[1] x n[2]
         lattice from minp with spacing d; returns (n[2], n[1], n[0])."""
-        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        pos4 = _f4(pos4, len(pos4))
         nn = np.ascontiguousarray(n, dtype=np.int32)
         out = np.zeros(int(np.prod(nn)), np.float32)
         self.L.fsph_ref_pbf_density_grid(self.h, _vp(pos4), pos4.shape[0], _vp(nn),

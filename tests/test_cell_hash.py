@@ -103,11 +103,14 @@ def test_gpu_cell_hash_bit_exact(gpu, ref_lib, rule):
     ps = rxPBDSPH(p)
     got, g, cw = ps.CalGridHash(x, rule)
     want, gw, cww = cell_hash_numpy(p, x, rule)
-    assert np.array_equal(g, gw) and cw == cww
-    assert np.array_equal(got, want)
+    assert np.array_equal(g, gw), (g, gw)
+    assert cw == cww, (cw, cww)
+    bad = np.nonzero(got != want)[0]
+    assert bad.size == 0, (bad.size, bad[:5], got[bad[:5]], want[bad[:5]], x[bad[:5]])
     if rule == 0:
         ref, _ = oracle.RefSolver(p, x.shape[0], "pbf").cell_hash(x)
-        assert np.array_equal(got, ref)
+        bad = np.nonzero(got != ref)[0]
+        assert bad.size == 0, (bad.size, bad[:5], got[bad[:5]], ref[bad[:5]], x[bad[:5]])
 
 
 @pytest.mark.gpu

@@ -83,7 +83,9 @@ def density_sensitivity(x, dx, p):
     carries into its densities."""
     n = x.shape[0]
     o = oracle.Oracle(p, n, threads=4)
-    off, idx = o.neighbors(np.ascontiguousarray(x, np.float32))
+    x4 = np.zeros((n, 4), np.float32)
+    x4[:, :3] = x[:, :3]
+    off, idx = o.neighbors(x4)
     rows = np.repeat(np.arange(n), np.diff(off))
     h = float(np.float32(p.h))
     aw = 315.0 / (64.0 * np.pi * h ** 9)

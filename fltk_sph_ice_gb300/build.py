@@ -19,7 +19,10 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no contraction of a * b + c into fused multiply-adds (gcc does it by default where the ISA has
+# them, as on Arm), so host arithmetic -- parameter derivation, grid geometry -- rounds the same on every host
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", INCLUDE, "-I", CSRC]
 
 

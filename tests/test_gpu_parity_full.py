@@ -302,8 +302,29 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
         if rebuilds:
             assert g.last_stats.grid_builds > 1, g.last_stats.grid_builds
         assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-5 * eta
-        assert_step_equal(g, r, x, x, f"1M, skin {skin}")
+        try:
+            assert_step_equal(g, r, x, x, f"1M, skin {skin}")
+        except AssertionError:
+            describe_worst(g, r, x, base)
+            raise
         g.close()
+
+
+def describe_worst(g, r, x, p):
+    """print the particles whose position change differs most (shown with a failure)"""
+    xg, xr = g.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64), r.get("pos")[:, :3].astype(np.float64)
+    x0 = np.asarray(x, np.float64)[:, :3]
+    err = np.abs((xg - x0) - (xr - x0)).max(1)
+    worst = np.argsort(err)[-5:][::-1]
+    off, idx, _ = r.neighbors(np.ascontiguousarray(x, np.float32))
+    lo = np.array(p.box_min) + float(np.float32(p.particle_radius))
+    hi = np.array(p.box_max) - float(np.float32(p.particle_radius))
+    dg, dr = g.GetArrayVBO(abi.RX_DENSITY), r.get("dens")
+    lg, lr = g.GetArrayVBO(abi.RX_SCALING_FACTOR), r.get("lambda")
+    for i in worst:
+        print(f"particle {i}: err {err[i]:.3e} dx_gpu {xg[i] - x0[i]} dx_ref {xr[i] - x0[i]} x0 {x0[i]} "
+              f"neighbours {off[i + 1] - off[i]} wall gap {min((x0[i] - lo).min(), (hi - x0[i]).min()):.3e} "
+              f"dens {dg[i]:.6g}/{dr[i]:.6g} lambda {lg[i]:.6g}/{lr[i]:.6g}")
 
 
 def test_c1_wcsph_steps_match_reference(gpu, ref_available):

@@ -36,9 +36,10 @@ int main(int argc, char **argv) {
     rxSPHEnviroment sph_env;
     sph_env.max_particles = 20000;
     sph_env.boundary_cen = Vec3(0.0, 0.0, 0.0);
-    sph_env.boundary_ext = Vec3(0.4, 0.2, 0.2);
+    sph_env.boundary_ext = Vec3(0.8, 0.4, 0.4);
     sph_env.dens = (RXREAL)998.29;
-    sph_env.mass = (RXREAL)0.0002;
+    sph_env.mass = (RXREAL)0.02;  // h = 0.0457 (kernel_particles 20); at h = 0.01 the reference's dt^2-scaled
+                                  // tensile correction outweighs lambda and the block explodes
     sph_env.kernel_particles = (RXREAL)20.0;
     sph_env.dt = (RXREAL)0.002;
     sph_env.epsilon = (RXREAL)100.0;
@@ -57,8 +58,8 @@ int main(int argc, char **argv) {
 
     // SetLiquidBox: a block of fluid in the lower corner of the box
     RXREAL pr = m_pPS->GetParticleRadius();
-    Vec3 cen = m_pPS->GetMin() + Vec3(0.1, 0.1, 0.1);
-    m_pPS->AddBox(-1, cen, Vec3(0.08, 0.08, 0.08), Vec3(0.0), pr * 2.0f);
+    Vec3 cen = m_pPS->GetMin() + Vec3(0.25, 0.25, 0.25);
+    m_pPS->AddBox(-1, cen, Vec3(0.2, 0.2, 0.2), Vec3(0.0), pr * 2.0f);
     const int n0 = m_pPS->GetNumParticles();
     if (n0 <= 0) { std::fprintf(stderr, "AddBox placed no particles\n"); return 1; }
     // a polygon obstacle as the scene loader hands one over (vertices, normals, index triples)

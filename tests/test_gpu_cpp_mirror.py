@@ -80,9 +80,9 @@ def test_reference_style_caller_runs(gpu, tmp_path):
     f = r.stdout.split()
     vals = {f[k]: f[k + 1] for k in range(0, 12, 2)}
     n = int(vals["particles"])
-    assert n == 25 ** 3                      # AddBox: (2 sx + 1)^3 with sx = (int)(0.08 / 2r) - 1 = 12
+    assert n == 13 ** 3                      # AddBox: (2 sx + 1)^3 with sx = (int)(0.2 / 2r) - 1 = 6
     assert int(vals["max"]) == 20000
-    assert int(vals["neighbours"]) > 20 * n  # ~33 per particle at the lattice spacing 2r
+    assert int(vals["neighbours"]) > 10 * n  # ~20 per interior particle at the lattice spacing 2r, fewer at the surface
     assert float(vals["dist_check"]) < 2.5e-7  # Dist = fl32(sqrt(Dist2)): Dist^2 within ~1 ulp of Dist2
     assert int(vals["unmoved"]) == 1          # UpdateWithoutPosAndVel leaves the particles
     assert f[10] == "density" and f[13] == "dim"

@@ -95,7 +95,7 @@ def density_sensitivity(x, dx, p):
     return np.bincount(rows, weights=float(np.float32(p.mass)) * wp * (dx[rows] + dx[idx]), minlength=n)
 
 
-def assert_step_equal(gpu, ref, x0g, x0r, what, p=None):
+def assert_step_equal(gpu, ref, x0g, x0r, what, p=None, extra_atol=None):
     """One step's results from the two sides' start positions x0g / x0r
     (equal for a first step, else apart by what earlier steps left): the
     position change (element-wise, with one storage ulp of each position and
@@ -106,12 +106,14 @@ def assert_step_equal(gpu, ref, x0g, x0r, what, p=None):
     x0g = np.asarray(x0g, np.float64)[:, :3]
     x0r = np.asarray(x0r, np.float64)[:, :3]
     carried = ulp32(xr) + ulp32(x0r) + np.abs(x0g - x0r)
+    if extra_atol is not None:
+        carried = carried + extra_atol
     assert_close(xg - x0g, xr.astype(np.float64) - x0r, f"{what}: position change", atol=carried)
     vg, vr = gpu.GetArrayVBO(abi.RX_VELOCITY)[:, :3], ref.get("vel")[:, :3]
     assert_close(vg, vr, f"{what}: velocity", atol=carried / PBF_DT)
     dg, dr = gpu.GetArrayVBO(abi.RX_DENSITY), ref.get("dens")
     atol = None
-    if p is not None and not np.array_equal(x0g, x0r):
+    if p is not None and (extra_atol is not None or not np.array_equal(x0g, x0r)):
         dx = np.maximum(np.linalg.norm(xg - xr.astype(np.float64), axis=1), np.linalg.norm(x0g - x0r, axis=1))
         atol = 2.0 * density_sensitivity(xr, dx, p)
     assert_close(dg, dr, f"{what}: density", etol=1e-5, floor=0.0, atol=atol)
@@ -292,6 +294,14 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
     it, _ = r.update(PBF_DT)
     eta = ref_mean_error(r, base)
     assert it == 4
+    # the same step in FP64: how far the reference's own FP32 result lies from exact
+    o = oracle.Oracle(base, sc.n, precision="double", threads=16)
+    o.set(x, v)
+    o.pbf_step(PBF_DT, fixed_iters=4)
+    x0 = np.asarray(x, np.float64)[:, :3]
+    dx64 = o.get("pos")[:, :3].astype(np.float64) - x0
+    dxr = r.get("pos")[:, :3].astype(np.float64) - x0
+    err_ref = np.abs(dxr - dx64).max(1)
     for skin, rebuilds in ((0.1, False), (0.005, True)):
         p = abi.FsphParams.from_buffer_copy(base)
         p.cell_skin = skin
@@ -302,8 +312,18 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
         if rebuilds:
             assert g.last_stats.grid_builds > 1, g.last_stats.grid_builds
         assert abs(g.last_stats.density_error_two_sided - eta) <= 1e-5 * eta
+        dxg = g.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64) - x0
+        err_gpu = np.abs(dxg - dx64).max(1)
+        print(f"skin {skin}: max |dx - dx_fp64| GPU {err_gpu.max():.3e}, reference {err_ref.max():.3e}; "
+              f"mean GPU {err_gpu.mean():.3e}, reference {err_ref.mean():.3e}")
+        # as close to the FP64 step as the reference's own FP32 step is
+        assert err_gpu.max() <= 2.0 * err_ref.max() and err_gpu.mean() <= 2.0 * err_ref.mean()
         try:
-            assert_step_equal(g, r, x, x, f"1M, skin {skin}")
+            # element-wise against the reference: 1e-5 of the largest change, the storage rounding of the
+            # positions, and the reference's own FP32 error of that particle (splash particles with two
+            # or three neighbours near h, where FP32 r^2 against the reference's double loses digits)
+            atol = 3.0 * err_ref[:, None]
+            assert_step_equal(g, r, x, x, f"1M, skin {skin}", p=base, extra_atol=atol)
         except AssertionError:
             describe_worst(g, r, x, base)
             raise

@@ -84,7 +84,8 @@ class FsphParams(ctypes.Structure):
         ("collect_features", ctypes.c_int),
         ("compensated_density", ctypes.c_int),
         ("grid_sort", ctypes.c_int),
-        ("reserved", ctypes.c_int * 2),
+        ("mlp_tcgen05", ctypes.c_int),
+        ("reserved", ctypes.c_int * 1),
     ]
 
     def to_dict(self) -> dict:
@@ -155,7 +156,7 @@ EXPORTS = [
     "fsph_set_step_log", "fsph_set_alloc_fault", "fsph_reference_cell_hash", "fsph_save_state", "fsph_load_state",
     "fsph_set_polygon_obstacle", "fsph_clear_polygon_obstacles", "fsph_num_polygon_triangles", "fsph_polygon_collide", "fsph_num_inlets",
     "fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob", "fsph_mlp_last_error",
-    "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
+    "fsph_mlp_forward", "fsph_mlp_forward_tcgen05", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
     "fsph_set_boundary", "fsph_num_boundary", "fsph_get_boundary",
     "fsph_batch_create", "fsph_batch_destroy", "fsph_batch_last_error", "fsph_batch_num_particles",
     "fsph_batch_offsets", "fsph_batch_set_particles", "fsph_batch_step", "fsph_batch_get_array",
@@ -233,6 +234,7 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
     L.fsph_mlp_last_error.argtypes = [c_void_p]
     L.fsph_mlp_last_error.restype = c_char_p
     L.fsph_mlp_forward.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_void_p]
+    L.fsph_mlp_forward_tcgen05.argtypes = [c_void_p, c_void_p, c_int, c_void_p]
     L.fsph_mlp_gradient.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, P(c_float)]
     L.fsph_mlp_train.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_float, c_void_p]
     L.fsph_set_warm_start_model.argtypes = [c_void_p, c_void_p]
@@ -260,7 +262,8 @@ def _declare(L: ctypes.CDLL) -> ctypes.CDLL:
                  "fsph_batch_set_config", "fsph_batch_get_config", "fsph_batch_autotune"]:
         getattr(L, name).restype = c_int
     for name in ["fsph_mlp_create", "fsph_mlp_destroy", "fsph_mlp_set_blob", "fsph_mlp_get_blob",
-                 "fsph_mlp_forward", "fsph_mlp_gradient", "fsph_mlp_train", "fsph_set_warm_start_model",
+                 "fsph_mlp_forward", "fsph_mlp_forward_tcgen05", "fsph_mlp_gradient", "fsph_mlp_train",
+                 "fsph_set_warm_start_model",
                  "fsph_time_pass", "fsph_create", "fsph_destroy", "fsph_set_params", "fsph_get_params", "fsph_num_particles",
                  "fsph_set_particles", "fsph_set_array", "fsph_step", "fsph_last_stats", "fsph_get_array",
                  "fsph_sync", "fsph_neighbors", "fsph_pbf_eval_lambda", "fsph_pbf_eval_correction",

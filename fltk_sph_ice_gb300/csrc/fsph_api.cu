@@ -210,6 +210,7 @@ int validate(const fsph_params &p, std::string &why) {
     if (p.cell_skin < 0.0f || p.cell_skin > 1.0f) { why = "cell_skin must lie in [0, 1]"; return FSPH_INVALID_ARG; }
     if (p.warm_start < 0 || p.warm_start > 1) { why = "warm_start must be 0 or 1"; return FSPH_INVALID_ARG; }
     if (p.grid_sort < 0 || p.grid_sort > 1) { why = "grid_sort must be 0 or 1"; return FSPH_INVALID_ARG; }
+    if (p.mlp_tcgen05 < 0 || p.mlp_tcgen05 > 1) { why = "mlp_tcgen05 must be 0 or 1"; return FSPH_INVALID_ARG; }
     return FSPH_OK;
 }
 
@@ -705,7 +706,11 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     /* warm-start correction of every particle, home order */
     const float4 *dw = nullptr;
     if (c->P.warm_start == 1) {
-        launch_mlp_infer(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, s, !c->model_nbr);
+        if (c->P.mlp_tcgen05)
+            launch_mlp_infer_tc(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, &c->ctl->mlp_err, s,
+                                !c->model_nbr);
+        else
+            launch_mlp_infer(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, s, !c->model_nbr);
         dw = c->dwarm;
     }
     int src = 0, it = 1;
@@ -939,6 +944,7 @@ void fill_stats(fsph_ctx *c, fsph_step_stats *st) {
         st->kernels = c->k_top + (int)h.iter * c->k_iter + ((int)h.builds - 1) * c->k_rebuild;
     if (c->P.solver == FSPH_SOLVER_PBF) {
         if (h.nan_flag) st->status = FSPH_NAN_DETECTED;
+        else if (h.mlp_err) st->status = FSPH_TIMEOUT; /* the tcgen05 inference gave up on an MMA */
         else if (st->density_error > c->P.eta) st->status = FSPH_NOT_CONVERGED;
     }
 }
@@ -1404,6 +1410,7 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
             std::fflush(c->log);
         }
         if (stats->status == FSPH_NAN_DETECTED) return fail(c, FSPH_NAN_DETECTED, "NaN in density or position");
+        if (stats->status == FSPH_TIMEOUT) return fail(c, FSPH_TIMEOUT, "warm-start inference: an MMA wait ran out");
     }
     return FSPH_OK;
 }

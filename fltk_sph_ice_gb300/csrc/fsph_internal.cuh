@@ -155,7 +155,7 @@ struct DevCtl {
     unsigned int parity;        /* which ppos buffer holds the current x* */
     unsigned int nan_flag;
     unsigned int disp2_bits;    /* max |x* - xb|^2 of the last correction pass (float bits) */
-    unsigned int pad;
+    unsigned int mlp_err;       /* 1 when a tcgen05 inference gave up waiting on an MMA */
     float err1, err2, errmax;   /* errors of the last lambda pass */
     float pad2;
 };

@@ -483,6 +483,7 @@ struct fsph_mlp {
     float *part = nullptr, *loss_part = nullptr, *loss = nullptr;
     int part_blocks = 0;
     int step = 0;
+    unsigned int *tc_err = nullptr; /* set by the tcgen05 forward when a wait ran out */
     cudaStream_t stream = nullptr;
     std::string err;
 };
@@ -530,6 +531,8 @@ int fsph_mlp_create(fsph_mlp **out) {
     for (float **p : {&m->blob, &m->m1, &m->m2, &m->grad})
         if (cudaMalloc((void **)p, kBlob * sizeof(float)) != cudaSuccess) return bail(FSPH_OOM);
     if (cudaMalloc((void **)&m->loss, sizeof(float)) != cudaSuccess) return bail(FSPH_OOM);
+    if (cudaMalloc((void **)&m->tc_err, sizeof(unsigned int)) != cudaSuccess) return bail(FSPH_OOM);
+    cudaMemsetAsync(m->tc_err, 0, sizeof(unsigned int), m->stream);
     cudaMemsetAsync(m->blob, 0, kBlob * sizeof(float), m->stream);
     cudaMemsetAsync(m->m1, 0, kBlob * sizeof(float), m->stream);
     cudaMemsetAsync(m->m2, 0, kBlob * sizeof(float), m->stream);
@@ -544,7 +547,7 @@ int fsph_mlp_destroy(fsph_mlp *m) {
     if (m->stream) cudaStreamSynchronize(m->stream);
     cudaFree(m->dev);
     cudaFree(m->blob); cudaFree(m->m1); cudaFree(m->m2); cudaFree(m->grad);
-    cudaFree(m->part); cudaFree(m->loss_part); cudaFree(m->loss);
+    cudaFree(m->part); cudaFree(m->loss_part); cudaFree(m->loss); cudaFree(m->tc_err);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
     return FSPH_OK;
@@ -575,6 +578,23 @@ int fsph_mlp_forward(fsph_mlp *m, const float *x, int n, float *y, void *stream)
     launch_mlp_forward3(m->dev, x, n, y, s);
     MLP_CUDA(m, cudaGetLastError());
     if (!stream) MLP_CUDA(m, cudaStreamSynchronize(s));
+    return FSPH_OK;
+}
+
+int fsph_mlp_forward_tcgen05(fsph_mlp *m, const float *x, int n, float *y) {
+    if (!m || n < 0 || (n > 0 && (!x || !y))) return FSPH_INVALID_ARG;
+    if (n == 0) return FSPH_OK;
+    cudaStream_t s = m->stream;
+    MLP_CUDA(m, cudaMemsetAsync(m->tc_err, 0, sizeof(unsigned int), s));
+    launch_mlp_forward3_tc(m->dev, x, n, y, m->tc_err, s);
+    MLP_CUDA(m, cudaGetLastError());
+    unsigned int e = 0;
+    MLP_CUDA(m, cudaMemcpyAsync(&e, m->tc_err, sizeof(e), cudaMemcpyDeviceToHost, s));
+    MLP_CUDA(m, cudaStreamSynchronize(s));
+    if (e) {
+        m->err = "tcgen05 forward: a wait on an MMA ran out";
+        return FSPH_TIMEOUT;
+    }
     return FSPH_OK;
 }
 

@@ -59,6 +59,11 @@ void launch_mlp_infer(const MlpDev *m, const float *x, int n, float4 *y, float s
                       cudaStream_t s, bool local_only = false);
 /* same network, plain n x 3 output (for training checks) */
 void launch_mlp_forward3(const MlpDev *m, const float *x, int n, float *y, cudaStream_t s);
+/* the same two on the tcgen05 tensor cores with TMEM accumulators
+ * (fsph_mlp_tc.cu); *err |= 1 when a wait on an MMA ran out */
+void launch_mlp_infer_tc(const MlpDev *m, const float *x, int n, float4 *y, float scale, const unsigned int *valid,
+                         unsigned int *err, cudaStream_t s, bool local_only = false);
+void launch_mlp_forward3_tc(const MlpDev *m, const float *x, int n, float *y, unsigned int *err, cudaStream_t s);
 /* per-block partial gradients of L = mean_i sum_k (y_ik - t_ik / out_scale)^2
  * (blob layout, nblocks rows) and per-block loss sums */
 int mlp_grad_blocks(int n);

@@ -94,12 +94,17 @@ class WarmStartNet:
         self._check(self.L.fsph_mlp_get_blob(self.h, b.ctypes.data_as(ctypes.c_void_p)), "get_blob")
         return b
 
-    def forward(self, x: np.ndarray) -> np.ndarray:
+    def forward(self, x: np.ndarray, tcgen05: bool = False) -> np.ndarray:
+        """network(x) for rows of x; tcgen05: on the tcgen05 tensor cores
+        (fsph_mlp_forward_tcgen05) instead of the mma.sync kernel"""
         import torch
         xd = torch.from_numpy(np.ascontiguousarray(x, np.float32)).cuda()
         yd = torch.empty((x.shape[0], NO), dtype=torch.float32, device="cuda")
-        self._check(self.L.fsph_mlp_forward(self.h, ctypes.c_void_p(xd.data_ptr()), x.shape[0],
-                                            ctypes.c_void_p(yd.data_ptr()), None), "forward")
+        xp, yp = ctypes.c_void_p(xd.data_ptr()), ctypes.c_void_p(yd.data_ptr())
+        if tcgen05:
+            self._check(self.L.fsph_mlp_forward_tcgen05(self.h, xp, x.shape[0], yp), "forward (tcgen05)")
+        else:
+            self._check(self.L.fsph_mlp_forward(self.h, xp, x.shape[0], yp, None), "forward")
         return yd.cpu().numpy()
 
     def gradient(self, x: np.ndarray, t: np.ndarray):

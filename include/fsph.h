@@ -130,7 +130,9 @@ typedef struct fsph_params {
                                 order of the 64-bit key (cell << 32 | previous slot):
                                 0: counting sort (atomic ranks, then each cell's slots sorted);
                                 1: LSD radix sort of the 64-bit keys, 8 cell bits per pass */
-    int reserved[2];
+    int mlp_tcgen05;         /* warm-start inference: 0 mma.sync fragments (m16n8k16);
+                                1 tcgen05.mma with TMEM accumulators (fsph_mlp_forward_tcgen05) */
+    int reserved[1];
 } fsph_params;
 
 /* Scene description in the reference's own terms (rxSPHEnviroment). */
@@ -459,6 +461,13 @@ const char *fsph_mlp_last_error(const fsph_mlp *m);
  * gradient / train, which take no stream, synchronise the producing stream).
  * y[n][3] = network(x[n][16]); device pointers; stream NULL = synchronous */
 int fsph_mlp_forward(fsph_mlp *m, const float *x, int n, float *y, void *stream);
+/* The same forward pass on the tcgen05 tensor cores (operands in shared
+ * memory, FP32 accumulators in tensor memory), 128 rows per MMA; the
+ * accumulation order inside an MMA differs from fsph_mlp_forward's, so the
+ * two agree to FP32 rounding of the sums (and the BF16 rounding of a hidden
+ * unit that lands between them).  Synchronous; FSPH_TIMEOUT if a bounded wait
+ * on an MMA ran out. */
+int fsph_mlp_forward_tcgen05(fsph_mlp *m, const float *x, int n, float *y);
 /* gradient of the mean squared error mean_i sum_k (y_ik - t_ik)^2 w.r.t. the
  * blob (host, FSPH_MLP_BLOB_SIZE floats; zero for mu, sigma, out_scale);
  * x, t device pointers; *loss receives the loss. Synchronous. */

@@ -1,0 +1,55 @@
+"""The warm-start network's inference on the tcgen05 tensor cores
+(fsph_mlp_forward_tcgen05; operands in shared memory, FP32 accumulators in
+tensor memory) against the numpy oracle and the mma.sync kernel, and a
+warm-started step with it (params.mlp_tcgen05 = 1).
+
+Bars as for the mma.sync kernel (tests/test_gpu_mlp.py): 5e-3 in
+max|a-b| / max|b| against the BF16-emulating oracle; the two GPU kernels
+round at the same points and differ only in FP32 summation order, 1e-3."""
+import numpy as np
+import pytest
+
+from oracle import mlp as omlp
+from test_gpu_mlp import random_problem, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [37, 128, 1000 + 37, 65536 + 5])
+def test_tcgen05_forward_matches_oracle_and_mma_sync(gpu, n):
+    from fltk_sph_ice_gb300.warmstart import WarmStartNet
+    x, _, blob = random_problem(n, seed=n)
+    net = WarmStartNet(blob)
+    y_tc = net.forward(x, tcgen05=True)
+    y_mma = net.forward(x)
+    y_bf, _ = omlp.forward(blob, x, bf16_emul=True)
+    print(f"n {n}: tcgen05 vs bf16 oracle {rel(y_tc, y_bf):.2e}, vs mma.sync {rel(y_tc, y_mma):.2e}")
+    assert np.isfinite(y_tc).all()
+    assert rel(y_tc, y_bf) < 5e-3
+    assert rel(y_tc, y_mma) < 1e-3
+    # a second call gives the same values (no state carried between calls)
+    assert np.array_equal(net.forward(x, tcgen05=True), y_tc)
+
+
+def test_tcgen05_warm_start_step(gpu):
+    """20 warm-started steps of a double dam break with each inference kernel:
+    the same iteration counts within one, positions to the step tolerance."""
+    from fltk_sph_ice_gb300 import abi, rxPBDSPH, scenes, warmstart
+    blob, _ = warmstart.load_model()
+    sc = scenes.pbf_double_dam_break(block=(24, 24, 48))
+    out = {}
+    for tc in (0, 1):
+        p = abi.FsphParams.from_buffer_copy(sc.params)
+        p.warm_start, p.mlp_tcgen05 = 1, tc
+        p.eta, p.error_mode, p.clamp_constraint, p.max_iter = 1e-3, abi.ERR_ONE_SIDED, 1, 100
+        ps = rxPBDSPH(p)
+        ps.SetWarmStartModel(blob)
+        ps.Set(sc.pos, sc.vel)
+        its = []
+        for _ in range(20):
+            ps.Update(sc.dt)
+            its.append(ps.LastStats().iterations)
+            assert ps.LastStats().status in (abi.OK, abi.NOT_CONVERGED)
+        out[tc] = (np.array(its), ps.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64))
+    assert np.abs(out[0][0] - out[1][0]).max() <= 1, (out[0][0], out[1][0])
+    assert np.abs(out[0][1] - out[1][1]).max() < 1e-3 * sc.params.h

@@ -33,7 +33,10 @@ def test_tcgen05_forward_matches_oracle_and_mma_sync(gpu, n):
 
 def test_tcgen05_warm_start_step(gpu):
     """20 warm-started steps of a double dam break with each inference kernel:
-    the same iteration counts within one, positions to the step tolerance."""
+    the same iteration counts within one per step.  Positions are compared
+    after 3 steps: later, a step that stops one iteration earlier or later
+    (both within the tolerance) sends the two runs apart the way any two
+    converged solves of this flow part."""
     from fltk_sph_ice_gb300 import abi, rxPBDSPH, scenes, warmstart
     blob, _ = warmstart.load_model()
     sc = scenes.pbf_double_dam_break(block=(24, 24, 48))
@@ -46,10 +49,13 @@ def test_tcgen05_warm_start_step(gpu):
         ps.SetWarmStartModel(blob)
         ps.Set(sc.pos, sc.vel)
         its = []
-        for _ in range(20):
+        for k in range(20):
             ps.Update(sc.dt)
             its.append(ps.LastStats().iterations)
-            assert ps.LastStats().status in (abi.OK, abi.NOT_CONVERGED)
-        out[tc] = (np.array(its), ps.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64))
+            assert ps.LastStats().status == abi.OK
+            if k == 2:
+                x3 = ps.GetArrayVBO(abi.RX_POSITION)[:, :3].astype(np.float64)
+        out[tc] = (np.array(its), x3)
     assert np.abs(out[0][0] - out[1][0]).max() <= 1, (out[0][0], out[1][0])
+    assert abs(out[0][0].mean() - out[1][0].mean()) <= 0.5
     assert np.abs(out[0][1] - out[1][1]).max() < 1e-3 * sc.params.h

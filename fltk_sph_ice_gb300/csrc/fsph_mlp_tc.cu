@@ -220,6 +220,17 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const MlpDev *__res
     const uint32_t b1 = smem_u32(S.b1), b2 = smem_u32(S.b2), b3 = smem_u32(S.b3);
     uint32_t phase = 0;
     bool failed = false;
+    /* this row's raw inputs of the coming tile: loaded while the previous
+     * tile's MMAs run */
+    float4 in[4 * KT];
+    auto fetch = [&](int tile) {
+        const int r = tile * kTcRows + t;
+#pragma unroll
+        for (int q = 0; q < 4 * KT; ++q)
+            in[q] = (tile < ntiles && r < n) ? __ldg(reinterpret_cast<const float4 *>(x + (size_t)r * kIn) + q)
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    fetch(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         const int row = tile * kTcRows + t;
         /* layer 1 operand: the normalised inputs of this row, BF16 */
@@ -227,8 +238,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const MlpDev *__res
         for (int kc = 0; kc < kIn / 8; ++kc) {
             float v[8];
             if (row < n && kc < 2 * KT) {
-                const float4 *src = reinterpret_cast<const float4 *>(x + (size_t)row * kIn + 8 * kc);
-                const float4 p0 = __ldg(src), p1 = __ldg(src + 1);
+                const float4 p0 = in[2 * kc], p1 = in[2 * kc + 1];
                 const float raw[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
 #pragma unroll
                 for (int e = 0; e < 8; ++e) v[e] = (raw[e] - S.mu[8 * kc + e]) * S.isig[8 * kc + e];
@@ -254,6 +264,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const MlpDev *__res
                          idesc_bf16(kTcRows, kHid), ks > 0);
             mma_commit(mbar);
         }
+        fetch(tile + gridDim.x);
         failed = __syncthreads_or(!mbar_wait(mbar, phase)) != 0;
         phase ^= 1u;
         if (failed) break;
@@ -317,7 +328,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const MlpDev *__res
 
 unsigned int tc_blocks(int n) {
     const unsigned int tiles = (unsigned int)((n + kTcRows - 1) / kTcRows);
-    return tiles < 2u * 152u ? (tiles > 0 ? tiles : 1u) : 2u * 152u; /* two CTAs (256 TMEM columns) per SM */
+    return tiles < 4u * 152u ? (tiles > 0 ? tiles : 1u) : 4u * 152u; /* four CTAs (512 TMEM columns) per SM */
 }
 
 }  // namespace

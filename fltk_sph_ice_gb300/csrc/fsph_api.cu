@@ -1123,6 +1123,7 @@ void fsph_params_default(fsph_params *o) {
     o->ap_q = 0.2f;
     o->cell_skin = 0.05f;
     o->use_graph = 1;
+    o->mlp_tcgen05 = 1; /* warm-start inference on tcgen05 (same step time as mma.sync, measured) */
 }
 
 int fsph_params_from_env(const fsph_env *e, fsph_params *o) {

@@ -134,6 +134,7 @@ def pbf_params(h: float, box_min, box_max, n: int, **kw) -> abi.FsphParams:
     p.cell_skin = 0.05
     p.use_graph = 1
     p.warm_start = 0
+    p.mlp_tcgen05 = 1
     for k, v in kw.items():
         setattr(p, k, v)
     return p

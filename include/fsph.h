@@ -131,7 +131,8 @@ typedef struct fsph_params {
                                 0: counting sort (atomic ranks, then each cell's slots sorted);
                                 1: LSD radix sort of the 64-bit keys, 8 cell bits per pass */
     int mlp_tcgen05;         /* warm-start inference: 0 mma.sync fragments (m16n8k16);
-                                1 tcgen05.mma with TMEM accumulators (fsph_mlp_forward_tcgen05) */
+                                1 tcgen05.mma with TMEM accumulators (fsph_mlp_forward_tcgen05),
+                                the default of fsph_params_default */
     int reserved[1];
 } fsph_params;
 

@@ -152,10 +152,13 @@ def load_model(path: str = DEFAULT_MODEL):
     return d["blob"].astype(np.float32), json.loads(str(d["meta"]))
 
 
-def collect_rollout(block, seed: int, steps: int, per_step: int, skip: int = 5, rng=None):
-    """Plain-solver rollout of a double dam break with feature collection:
-    (features before a step, correction / h that step needed) for a random
-    subset of particles of every step after the first `skip`."""
+def collect_rollout(block, seed: int, steps: int, per_step: int, skip: int = 5, rng=None, warm_blob=None):
+    """Rollout of a double dam break with feature collection: (features
+    before a step, correction / h that step needed) for a random subset of
+    particles of every step after the first `skip`.  With warm_blob the
+    rollout runs warm-started by that network, so the samples come from the
+    states the warm-started solver visits (the correction target is the full
+    correction from the prediction either way)."""
     from .particles import rxPBDSPH
     sc = scenes.pbf_double_dam_break(block=block, seed=seed)
     p = sc.params
@@ -163,7 +166,10 @@ def collect_rollout(block, seed: int, steps: int, per_step: int, skip: int = 5, 
     p.eta = 1e-3
     p.max_iter = 400
     p.collect_features = 1
+    p.warm_start = 1 if warm_blob is not None else 0
     ps = rxPBDSPH(p)
+    if warm_blob is not None:
+        ps.SetWarmStartModel(warm_blob)
     ps.Set(sc.pos, sc.vel)
     rng = rng or np.random.default_rng(seed)
     X, T, iters = [], [], []
@@ -292,6 +298,10 @@ def main():
     ap.add_argument("--seeds", default=None, metavar="LIST",
                     help="train one network per seed (e.g. 0,1,2,3,4,5) on the same samples and keep the one "
                          "with the fewest iterations on the validation scenes")
+    ap.add_argument("--warm-from", default=None, metavar="MODEL",
+                    help="also collect --warm-rollouts rollouts warm-started by MODEL and train on both sets "
+                         "(samples of the states the warm-started solver visits)")
+    ap.add_argument("--warm-rollouts", type=int, default=128)
     ap.add_argument("--data", default=None, metavar="NPZ",
                     help="reuse the rollout samples stored in NPZ (written there when it does not exist)")
     args = ap.parse_args()
@@ -320,6 +330,16 @@ def main():
         x, t, _ = collect_rollout(blk, seed=1000 + r, steps=args.steps, per_step=args.per_step, rng=rng)
         X.append(x)
         T.append(t)
+    if args.warm_from:
+        wblob, _ = load_model(args.warm_from)
+        wrng = np.random.default_rng(54321)
+        for r in range(args.warm_rollouts):
+            blk = next_block(args.sizes, wrng)
+            blocks.append(blk)
+            x, t, _ = collect_rollout(blk, seed=2000 + r, steps=args.steps, per_step=args.per_step, rng=wrng,
+                                      warm_blob=wblob)
+            X.append(x)
+            T.append(t)
     X = np.concatenate(X).astype(np.float32)
     T = np.concatenate(T).astype(np.float32)
     if args.data is not None and not loaded:
@@ -333,7 +353,8 @@ def main():
         meta = dict(samples=int(X.shape[0]), rollouts=len(blocks), steps=args.steps, per_step=args.per_step,
                     epochs=args.epochs, batch=args.batch, lr=args.lr, loss=hist, collect_s=t_collect,
                     train_s=time.time() - t1, target_var=float((T / blob[O_SCALE]).var() * 3),
-                    sizes=args.sizes, features=args.features, seed=sd, blocks=blocks[:8])
+                    sizes=args.sizes, features=args.features, seed=sd, blocks=blocks[:8],
+                    warm_rollouts=args.warm_rollouts if args.warm_from else 0)
         alpha, table = calibrate_damping(blob)
         blob[O_SCALE] *= alpha
         meta["output_damping"] = alpha

@@ -40,16 +40,18 @@ namespace fsph {
 constexpr int kBatch = FSPH_KBATCH;
 
 /* FSPH_FOLD 1: the constraint passes keep constant factors out of the pair
- * loop (fewer instructions per candidate; same results to rounding) */
+ * loop (fewer instructions per candidate; same results to rounding).
+ * Measured on the 1M double dam break: lambda 82 -> 80 us, warm step
+ * 2.855 -> 2.817 ms, plain step 10.25 -> 10.06 ms; on by default. */
 #ifndef FSPH_FOLD
-#define FSPH_FOLD 0
+#define FSPH_FOLD 1
 #endif
 /* FSPH_PERSIST_LAMBDA / FSPH_PERSIST_CORRECTION 1: that single-scene
  * constraint pass runs as many blocks as are resident on the GPU, each warp
  * taking 32-slot chunks round-robin (FSPH_PERSIST sets both).  Measured on
  * the 1M double dam break: lambda 92 -> 82 us with identical results, so on
- * by default; the correction pass gains nothing (89 us either way) and its
- * persistent form was 7 % slower in an earlier form, so off. */
+ * by default; the correction pass gets slower (90 -> 95 us, warm step 2.855
+ * -> 2.917 ms), so off. */
 #ifdef FSPH_PERSIST
 #define FSPH_PERSIST_LAMBDA FSPH_PERSIST
 #define FSPH_PERSIST_CORRECTION FSPH_PERSIST

@@ -259,7 +259,8 @@ int fsph_clear_delete_regions(fsph_ctx *ctx);
 int fsph_add_inlet_line(fsph_ctx *ctx, const double *pos1, const double *pos2, const double *vel,
                         const double *up, int accum, int span, double spacing);
 int fsph_clear_inlets(fsph_ctx *ctx);
-/* The number of inlet lines (-1 for a NULL context). */
+/* The number of inlet lines (the size of the reference's m_vInletLines,
+ * rx_ps.h:171; -1 for a NULL context). */
 int fsph_num_inlets(const fsph_ctx *ctx);
 /* Emit the particles of the lines due at `step` (rxPBDSPH_GPU::Update,
  * rx_sph_pbd_gpu.cpp:795-815, before the step): after the existing

@@ -1242,6 +1242,12 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
     if (!rebuild && p->max_particles != c->P.max_particles && c->n > p->max_particles)
         return fail(c, FSPH_INVALID_ARG, "max_particles below the current particle count");
     const int old_cap = c->P.max_particles;
+    const fsph_params old = c->P;
+    bool same_box = old.h == p->h;
+    for (int a = 0; a < 3; ++a) same_box = same_box && old.box_min[a] == p->box_min[a] && old.box_max[a] == p->box_max[a];
+    /* what the boundary's cell table and volumes, and the triangles' table, depend on */
+    const bool same_grid = same_box && old.cell_skin == p->cell_skin;
+    const bool same_boundary = same_grid && old.mass == p->mass && old.rest_dens == p->rest_dens;
     c->P = *p;
     drop_graph(c);
     if (rebuild || p->max_particles != old_cap) {
@@ -1265,8 +1271,11 @@ int fsph_set_params(fsph_ctx *c, const fsph_params *p) {
     }
     c->broken = true;
     FSPH_TRY(alloc_grid(c));
-    FSPH_TRY(boundary_build(c)); /* the boundary's cell table follows the grid */
-    if (!c->poly_t.empty()) FSPH_TRY(polygons_upload(c)); /* so does the triangles' */
+    /* the boundary's cell table and volumes follow the grid and the kernel; the
+     * triangles' table the reference grid (box and h).  A call that changes
+     * neither (gravity, iterations, flags) leaves them */
+    if (rebuild || !same_boundary) FSPH_TRY(boundary_build(c));
+    if (!c->poly_t.empty() && (rebuild || !same_box)) FSPH_TRY(polygons_upload(c));
     FSPH_CUDA(c, cudaStreamSynchronize(c->stream));
     c->broken = false;
     return FSPH_OK;
@@ -1742,7 +1751,7 @@ int fsph_step_fields(fsph_ctx *c, float dt, void *stream) {
 extern "C++" {
 namespace {
 const char kStateMagic[8] = {'F', 'S', 'P', 'H', 'S', 'T', 'A', 'T'};
-const int kStateVersion = 2;
+const int kStateVersion = 3;
 
 struct StateHeader {
     char magic[8];
@@ -1753,6 +1762,7 @@ struct StateHeader {
     int mlp_bytes, features;
     long long steps_done;
     int poly_nv, poly_nt;
+    int obstacle_bytes, inlet_bytes; /* layouts of the raw records that follow */
 };
 
 template <class T>
@@ -1803,6 +1813,8 @@ int fsph_save_state(fsph_ctx *c, const char *path) {
     h.steps_done = c->steps_done;
     h.poly_nv = (int)(c->poly_v.size() / 3);
     h.poly_nt = (int)(c->poly_t.size() / 3);
+    h.obstacle_bytes = (int)sizeof(Obstacle);
+    h.inlet_bytes = (int)sizeof(fsph_ctx::Inlet);
     bool ok = put(fc.f, &h, 1) && put(fc.f, &c->P, 1) && put(fc.f, c->inlets.data(), c->inlets.size()) &&
               put(fc.f, c->del_regions.data(), c->del_regions.size()) && put(fc.f, c->boxes.data(), c->boxes.size()) &&
               put(fc.f, c->spheres.data(), c->spheres.size()) && put(fc.f, c->poly_v.data(), c->poly_v.size()) &&
@@ -1830,7 +1842,8 @@ int fsph_load_state(fsph_ctx *c, const char *path) {
     if (!get(fc.f, &h, 1) || std::memcmp(h.magic, kStateMagic, 8) != 0)
         return fail(c, FSPH_INVALID_ARG, "not a state file");
     if (h.version != kStateVersion || h.params_size != (int)sizeof(fsph_params) || h.mlp_bytes != (int)sizeof(MlpDev) ||
-        h.features != kFeatures)
+        h.features != kFeatures || h.obstacle_bytes != (int)sizeof(Obstacle) ||
+        h.inlet_bytes != (int)sizeof(fsph_ctx::Inlet))
         return fail(c, FSPH_INVALID_ARG, "state file of another version or build");
     fsph_params P{};
     if (!get(fc.f, &P, 1)) return fail(c, FSPH_INVALID_ARG, "state file: truncated");

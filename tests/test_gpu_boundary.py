@@ -141,3 +141,37 @@ def test_boundary_removed_and_rejected_for_wcsph(gpu):
     b4 = np.ascontiguousarray(bnd, dtype=np.float32)
     st = sph.L.fsph_set_boundary(sph.handle, b4.ctypes.data_as(ctypes.c_void_p), b4.shape[0], abi.HOST)
     assert st == abi.UNSUPPORTED
+
+
+def test_params_change_keeps_or_rebuilds_the_boundary(gpu):
+    """fsph_set_params with only gravity changed keeps the boundary's table
+    and volumes (callers set gravity and iterations every step); a new h
+    recomputes the volumes, as the oracle does for that h."""
+    pos, bnd, p = resting_scene()
+    ps = rxPBDSPH(p)
+    ps.Set(pos)
+    ps.SetBoundary(bnd)
+    vol0 = ps.GetBoundary(abi.BOUNDARY_VOLUME)
+    ps.Update(0.0016)
+    q = abi.FsphParams.from_buffer_copy(p)
+    q.gravity[1] = -5.0
+    ps.SetParams(q)
+    assert np.array_equal(ps.GetBoundary(abi.BOUNDARY_VOLUME), vol0)
+    ps.Update(0.0016)
+    # the same step with the boundary set afresh under the new gravity
+    ref = rxPBDSPH(q)
+    ref.Set(ps.GetArrayVBO(abi.RX_POSITION), ps.GetArrayVBO(abi.RX_VELOCITY))
+    ref.SetBoundary(bnd)
+    x0 = ps.GetArrayVBO(abi.RX_POSITION)
+    ps.Update(0.0016)
+    ref.Update(0.0016)
+    assert_rel(ps.GetArrayVBO(abi.RX_POSITION)[:, :3] - x0[:, :3],
+               ref.GetArrayVBO(abi.RX_POSITION)[:, :3] - x0[:, :3], 1e-5, "step after a gravity change")
+    r = abi.FsphParams.from_buffer_copy(q)
+    r.h = p.h * 1.1
+    ps.SetParams(r)
+    o = oracle.Oracle(r, pos.shape[0], threads=4)
+    o.set(pos)
+    o.set_boundary(bnd)
+    assert not np.array_equal(ps.GetBoundary(abi.BOUNDARY_VOLUME), vol0)
+    assert_rel(ps.GetBoundary(abi.BOUNDARY_VOLUME), o.get_boundary("vol"), 1e-5, "psi_b after a new h")

@@ -330,7 +330,8 @@ def test_bench_state_step_matches_reference(gpu, ref_available, bench_rolled):
             out = np.abs(dxg - dxr).max(1) > bar
             print(f"skin {skin}: {out.sum()} particles past the reference's own error bar")
             assert out.sum() <= 10 and (err_gpu[out] <= err_ref.max()).all()
-            atol = 3.0 * (err_ref + np.where(out, err_gpu, 0.0))[:, None]
+            # per entry: never stricter than the field's 1e-5 bar
+            atol = 3.0 * (err_ref + np.where(out, err_gpu, 0.0))[:, None] + 1e-5 * scale
             assert_step_equal(g, r, x, x, f"1M, skin {skin}", p=base, extra_atol=atol)
         except AssertionError:
             describe_worst(g, r, x, base)

@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const MlpDev *__res
     if (failed) {
         if (t == 0) {
             atomicOr(err, 1u);
-            mbar_wait(mbar, phase); /* the MMA that did not complete in time, once more */
+            mbar_wait(mbar, phase ^ 1u); /* the phase that did not complete in time, once more */
         }
         __syncthreads();
     }

@@ -251,69 +251,6 @@ __global__ void k_build_list(DevParams p, const unsigned int *__restrict__ cell_
     build_list_body(p, i, cell_start, xb, cellb, list, cnt);
 }
 
-/* The same lists, built by the warp together: per (dz, dy) row the warp
- * walks the union of its lanes' slot ranges once, each lane loading one
- * candidate of every 32 and the warp broadcasting them; a lane keeps the
- * candidates of its own range that pass its test, in the same ascending
- * order, so every list is identical to build_list_body's. */
-__global__ void __launch_bounds__(kBlock) k_build_list_warp(DevParams p, const unsigned int *__restrict__ cell_start,
-                                                            const float4 *__restrict__ xb,
-                                                            const unsigned int *__restrict__ cellb,
-                                                            ListEntry *__restrict__ list,
-                                                            unsigned char *__restrict__ cnt) {
-    const int lane = threadIdx.x & 31;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i - lane >= p.n) return; /* whole warps past n leave together */
-    const bool valid = i < p.n;
-    const float3 xi = valid ? f3(xb[i]) : make_float3(0.0f, 0.0f, 0.0f);
-    const int cb = valid ? (int)cellb[i] : 0;
-    int k = 0;
-    bool ovf = false;
-    ListEntry last = 0;
-#pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-        unsigned int s = 0xffffffffu, e = 0u;
-        if (valid) {
-            const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
-            s = __ldg(cell_start + base - 1);
-            e = __ldg(cell_start + base + 2);
-            if (e - s > 4095u) ovf = true;
-        }
-        const unsigned int S = __reduce_min_sync(0xffffffffu, s), E = __reduce_max_sync(0xffffffffu, e);
-#pragma unroll 1
-        for (unsigned int c0 = S; c0 < E; c0 += 32) {
-            const unsigned int jl = c0 + (unsigned int)lane;
-            const float4 xc = jl < E ? __ldg(xb + jl) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            const int m = (int)min(32u, E - c0);
-#pragma unroll 4
-            for (int t = 0; t < m; ++t) {
-                const float3 xj = make_float3(__shfl_sync(0xffffffffu, xc.x, t), __shfl_sync(0xffffffffu, xc.y, t),
-                                              __shfl_sync(0xffffffffu, xc.z, t));
-                const unsigned int j = c0 + (unsigned int)t;
-                if (j >= s && j < e) {
-                    const float3 d = xi - xj;
-                    if (dot3(d, d) < p.rl2) {
-#ifdef FSPH_LIST32
-                        last = j;
-#else
-                        last = (ListEntry)((r << 12) | (j - s));
-#endif
-                        if (k < kListMax) list[list_at(k, i, p.n)] = last;
-                        ++k;
-                    }
-                }
-            }
-        }
-    }
-    if (!valid) return;
-    const bool overflow = ovf || k > kListMax;
-#ifdef FSPH_LIST_GROUPED
-    if (!overflow)
-        for (int t = k; (t & 3) != 0; ++t) list[list_at(t, i, p.n)] = last;
-#endif
-    cnt[i] = overflow ? kListOverflow : (unsigned char)k;
-}
-
 /* ======================================================================== */
 /* PBF                                                                      */
 /* ======================================================================== */
@@ -1051,11 +988,7 @@ void launch_lambda(const DevParams &p, const unsigned int *cell_start, float4 *p
 void launch_build_list(const DevParams &p, const unsigned int *cell_start, const float4 *xb, const NbrLists &nl,
                        cudaStream_t s) {
     if (!p.use_lists) return;
-#if FSPH_LIST_WARP
-    k_build_list_warp<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, xb, nl.cellb, nl.list, nl.cnt);
-#else
     k_build_list<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, xb, nl.cellb, nl.list, nl.cnt);
-#endif
 }
 void launch_correction(const DevParams &p, const unsigned int *cell_start, float4 *ppos0, float4 *ppos1,
                        const float4 *xb, DevCtl *ctl, float *part, unsigned long long if_handle,

@@ -46,11 +46,6 @@ constexpr int kBatch = FSPH_KBATCH;
 #ifndef FSPH_FOLD
 #define FSPH_FOLD 1
 #endif
-/* FSPH_LIST_WARP 1: the single-scene list build walks each row's candidates
- * once per warp (k_build_list_warp; the same lists) */
-#ifndef FSPH_LIST_WARP
-#define FSPH_LIST_WARP 0
-#endif
 /* FSPH_PERSIST_LAMBDA / FSPH_PERSIST_CORRECTION 1: that single-scene
  * constraint pass runs as many blocks as are resident on the GPU, each warp
  * taking 32-slot chunks round-robin (FSPH_PERSIST sets both).  Measured on

@@ -443,6 +443,11 @@ public:
         m_status = fsph_save_state(m_ctx, (fn + ".state").c_str());
         if (m_status != FSPH_OK) return 0;
         const fsph_params p = params();
+        std::string state; /* the state file's name as a JSON string body */
+        for (char ch : fn + ".state") {
+            if (ch == '"' || ch == '\\') state.push_back('\\');
+            state.push_back(ch);
+        }
         FILE *f = std::fopen((fn + ".json").c_str(), "w");
         if (!f) return 0;
         std::fprintf(f,
@@ -450,10 +455,10 @@ public:
                      "\"active\": %d, \"max_particles\": %d, \"seed\": %llu, \"inlets\": %d, "
                      "\"h\": %.9g, \"mass\": %.9g, \"rest_dens\": %.9g, \"dt_note\": \"dt is an Update argument\", "
                      "\"box_min\": [%.17g, %.17g, %.17g], \"box_max\": [%.17g, %.17g, %.17g], "
-                     "\"state\": \"%s.state\"}\n",
+                     "\"state\": \"%s\"}\n",
                      p.solver, GetNumParticles(), GetNumActiveParticles(), p.max_particles,
                      (unsigned long long)m_seed, m_inlets, (double)p.h, (double)p.mass, (double)p.rest_dens,
-                     p.box_min[0], p.box_min[1], p.box_min[2], p.box_max[0], p.box_max[1], p.box_max[2], fn.c_str());
+                     p.box_min[0], p.box_min[1], p.box_min[2], p.box_max[0], p.box_max[1], p.box_max[2], state.c_str());
         const bool ok = std::fclose(f) == 0;
         return ok ? 1 : 0;
     }

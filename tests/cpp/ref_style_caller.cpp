@@ -14,6 +14,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
+#include <vector>
 
 #include "fsph_particle_system.hpp"
 
@@ -114,9 +116,27 @@ int main(int argc, char **argv) {
     lap("neighbours and fields");
     // the particle file
     if (!m_pPS->OutputParticles(argv[1])) { std::fprintf(stderr, "OutputParticles failed\n"); return 1; }
-    std::printf("particles %d max %d neighbours %zu dist_check %.3e unmoved %d density %.3f %.3f dim %.3f %.3f %.3f\n",
+    // a checkpoint: a second system resumed from it steps as this one does
+    const std::string ckpt = std::string(argv[1]) + ".ckpt";
+    if (!m_pPS->SaveCheckpoint(ckpt)) { std::fprintf(stderr, "SaveCheckpoint failed\n"); return 1; }
+    rxParticleSystemBase *resumed = new RXSPH(true);
+    ((RXSPH *)resumed)->Initialize(sph_env);
+    if (!resumed->LoadCheckpoint(ckpt)) { std::fprintf(stderr, "LoadCheckpoint failed\n"); return 1; }
+    for (int k = 0; k < 5; ++k) {
+        m_pPS->Update((RXREAL)m_fDt, steps + 1 + k);
+        resumed->Update((RXREAL)m_fDt, steps + 1 + k);
+    }
+    const int n = m_pPS->GetNumParticles();
+    std::vector<RXREAL> xa(m_pPS->GetArrayVBO(rxParticleSystemBase::RX_POSITION),
+                           m_pPS->GetArrayVBO(rxParticleSystemBase::RX_POSITION, false) + 4 * (size_t)n);
+    const RXREAL *xr = resumed->GetArrayVBO(rxParticleSystemBase::RX_POSITION);
+    int same = resumed->GetNumParticles() == n ? 1 : 0;
+    for (size_t k = 0; same && k < xa.size(); ++k) same = xa[k] == xr[k] ? 1 : 0;
+    delete resumed;
+    std::printf("particles %d max %d neighbours %zu dist_check %.3e unmoved %d density %.3f %.3f dim %.3f %.3f %.3f"
+                " resume %d\n",
                 m_pPS->GetNumParticles(), m_pPS->GetMaxParticles(), total, worst, x[0] == x0 ? 1 : 0, rmin, rmax,
-                m_pPS->GetDim()[0], m_pPS->GetDim()[1], m_pPS->GetDim()[2]);
+                m_pPS->GetDim()[0], m_pPS->GetDim()[1], m_pPS->GetDim()[2], same);
     delete m_pPS;
     return 0;
 }

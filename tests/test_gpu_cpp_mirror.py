@@ -85,8 +85,9 @@ def test_reference_style_caller_runs(gpu, tmp_path):
     assert int(vals["neighbours"]) > 10 * n  # ~20 per interior particle at the lattice spacing 2r, fewer at the surface
     assert float(vals["dist_check"]) < 2.5e-7  # Dist = fl32(sqrt(Dist2)): Dist^2 within ~1 ulp of Dist2
     assert int(vals["unmoved"]) == 1          # UpdateWithoutPosAndVel leaves the particles
-    assert f[10] == "density" and f[13] == "dim"
+    assert f[10] == "density" and f[13] == "dim" and f[17] == "resume"
     rho_min, rho_max = float(f[11]), float(f[12])
+    assert int(f[18]) == 1  # SaveCheckpoint / LoadCheckpoint: five more steps bit-identical
     assert 0 < rho_min < rho_max < 2000.0
     pos, vel = read_particles(tmp_path / "out.dat")
     assert pos.shape == (n, 3) and np.isfinite(pos).all() and np.isfinite(vel).all()

@@ -11,7 +11,9 @@ import ctypes
 import os
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG_DIR, "_build", "libfsph.so")
+# FSPH_LIBRARY names another build of the same library to load instead (the
+# bounds-checking debug build, fltk_sph_ice_gb300.build --debug-bounds)
+LIB_PATH = os.environ.get("FSPH_LIBRARY") or os.path.join(PKG_DIR, "_build", "libfsph.so")
 
 # fsph_status
 OK, INVALID_ARG, OOM, CUDA_ERROR, NAN_DETECTED, TIMEOUT, NOT_CONVERGED, NOT_INITIALIZED, UNSUPPORTED, NO_DEVICE = range(10)
@@ -129,7 +131,8 @@ class FsphStepStats(ctypes.Structure):
         ("density_error_max", ctypes.c_float),
         ("status", ctypes.c_int),
         ("kernels", ctypes.c_int),
-        ("reserved", ctypes.c_int * 2),
+        ("bounds_bits", ctypes.c_int),
+        ("reserved", ctypes.c_int * 1),
     ]
 
 

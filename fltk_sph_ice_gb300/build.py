@@ -1,9 +1,14 @@
 """In-tree build of libfsph.so for sm_103a (nvcc directly, no cmake).
 
-    python -m fltk_sph_ice_gb300.build        # or __graft_entry__.build()
+    python -m fltk_sph_ice_gb300.build                  # or __graft_entry__.build()
+    python -m fltk_sph_ice_gb300.build --debug-bounds   # the bounds-checking debug library
 
 Translation units compile in parallel into ``_build/*.o`` and link into
 ``_build/libfsph.so``; a unit is recompiled only when it or a header changed.
+``--debug-bounds`` builds ``_build/debug_bounds/libfsph.so`` with
+FSPH_DEBUG_BOUNDS=1: every neighbour slot, cell row and list count the passes
+read is checked before use and a failed check is reported in
+``fsph_step_stats.bounds_bits`` (load it with FSPH_LIBRARY=<path>).
 """
 from __future__ import annotations
 
@@ -17,6 +22,7 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
+OUT_DEBUG_BOUNDS = os.path.join(OUT, "debug_bounds")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no contraction of a * b + c into fused multiply-adds (gcc does it by default where the ISA has
@@ -50,22 +56,24 @@ def _compile(src: str, obj: str, extra: list[str], verbose: bool) -> None:
         print(r.stderr, file=sys.stderr)
 
 
-def build(verbose: bool = False, force: bool = False, extra: list[str] | None = None) -> str:
-    os.makedirs(OUT, exist_ok=True)
-    extra = list(extra or [])
+def build(verbose: bool = False, force: bool = False, extra: list[str] | None = None,
+          debug_bounds: bool = False) -> str:
+    out = OUT_DEBUG_BOUNDS if debug_bounds else OUT
+    os.makedirs(out, exist_ok=True)
+    extra = list(extra or []) + (["-DFSPH_DEBUG_BOUNDS=1"] if debug_bounds else [])
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr = _headers_mtime()
     jobs = []
     objs = []
     for s in srcs:
-        o = os.path.join(OUT, os.path.basename(s)[:-3] + ".o")
+        o = os.path.join(out, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
         if force or not os.path.exists(o) or os.path.getmtime(o) < max(os.path.getmtime(s), hdr):
             jobs.append((s, o))
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for f in [ex.submit(_compile, s, o, extra, verbose) for s, o in jobs]:
             f.result()
-    lib = os.path.join(OUT, "libfsph.so")
+    lib = os.path.join(out, "libfsph.so")
     if jobs or not os.path.exists(lib):
         cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-lcudart"]
         if verbose:
@@ -77,4 +85,4 @@ def build(verbose: bool = False, force: bool = False, extra: list[str] | None = 
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, debug_bounds="--debug-bounds" in sys.argv))

@@ -349,6 +349,7 @@ DevParams dev_for(const fsph_ctx *c, int n, float dt) {
     p.obs = c->obs_dev;
     p.ntri = c->ntri_dev;
     p.poly = c->poly;
+    p.dbg = &c->ctl->bounds_bits;
     return p;
 }
 
@@ -940,6 +941,7 @@ void fill_stats(fsph_ctx *c, fsph_step_stats *st) {
     st->density_error_max = h.errmax;
     st->density_error = c->P.error_mode ? h.err2 : h.err1;
     st->status = FSPH_OK;
+    st->bounds_bits = (int)h.bounds_bits;
     if (c->last_step_graph) /* every grid build after the first is one run of the rebuild body */
         st->kernels = c->k_top + (int)h.iter * c->k_iter + ((int)h.builds - 1) * c->k_rebuild;
     if (c->P.solver == FSPH_SOLVER_PBF) {
@@ -947,6 +949,8 @@ void fill_stats(fsph_ctx *c, fsph_step_stats *st) {
         else if (h.mlp_err) st->status = FSPH_TIMEOUT; /* the tcgen05 inference gave up on an MMA */
         else if (st->density_error > c->P.eta) st->status = FSPH_NOT_CONVERGED;
     }
+    if (h.bounds_bits && st->status != FSPH_NAN_DETECTED)
+        st->status = FSPH_CUDA_ERROR; /* a debug build's index check failed */
 }
 
 /* Load n host/device float4 positions (and optional velocities) in particle order. */
@@ -1421,6 +1425,9 @@ int fsph_step(fsph_ctx *c, float dt, void *stream, fsph_step_stats *stats) {
         }
         if (stats->status == FSPH_NAN_DETECTED) return fail(c, FSPH_NAN_DETECTED, "NaN in density or position");
         if (stats->status == FSPH_TIMEOUT) return fail(c, FSPH_TIMEOUT, "warm-start inference: an MMA wait ran out");
+        if (stats->bounds_bits)
+            return fail(c, FSPH_CUDA_ERROR, "debug bounds check: an index out of range (bits " +
+                                                std::to_string(stats->bounds_bits) + ")");
     }
     return FSPH_OK;
 }

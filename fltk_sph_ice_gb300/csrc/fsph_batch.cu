@@ -450,6 +450,7 @@ int apply_config(fsph_batch *b, const fsph_batch_config &cfg, float dt) {
         q.walk_cells = 0;
         h[s] = dev_params_for(q, b->n, dt);
         h[s].cell_off = (unsigned int)cells;
+        h[s].dbg = &b->ctl->bounds_bits;
         cells += (unsigned long long)h[s].gx * h[s].gy * h[s].gz;
     }
     if (cells > (1ull << 30)) return bfail(b, FSPH_INVALID_ARG, "the scenes' grids exceed 2^30 cells");
@@ -509,6 +510,7 @@ BLaunch launch_of(const fsph_batch *b) {
 DevParams loop_params(const fsph_batch *b, float dt) {
     DevParams lp{};
     lp.n = b->n;
+    lp.dbg = &b->ctl->bounds_bits;
     lp.min_iter = b->iters;
     lp.max_iter = b->iters;
     lp.eta = -1.0f;
@@ -876,7 +878,8 @@ int fsph_batch_scene_stats(fsph_batch *b, int scene, fsph_step_stats *st) {
     st->density_error_two_sided = b->h_err[3 * scene + 1];
     st->density_error_max = b->h_err[3 * scene + 2];
     st->density_error = b->P[scene].error_mode ? st->density_error_two_sided : st->density_error_one_sided;
-    st->status = b->ctl_host->nan_flag ? FSPH_NAN_DETECTED : FSPH_OK;
+    st->bounds_bits = (int)b->ctl_host->bounds_bits;
+    st->status = b->ctl_host->nan_flag ? FSPH_NAN_DETECTED : st->bounds_bits ? FSPH_CUDA_ERROR : FSPH_OK;
     return FSPH_OK;
 }
 

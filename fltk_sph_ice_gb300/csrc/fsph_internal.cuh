@@ -84,7 +84,52 @@ struct DevParams {
     /* triangle-mesh obstacles (ntri = 0: none) */
     int ntri;
     PolyTable poly;
+    /* FSPH_DEBUG_BOUNDS builds: where failed index checks are recorded (may be null) */
+    unsigned int *dbg;
 };
+
+/* FSPH_DEBUG_BOUNDS 1 (a debug build, fltk_sph_ice_gb300.build --debug-bounds):
+ * every slot, cell and list index the passes read is checked against its
+ * table before it is used; an index out of range is replaced by a valid one
+ * (the step's numbers are then wrong, never its memory accesses) and sets a
+ * bit of DevParams::dbg, which the step reports in fsph_step_stats.
+ * bounds_bits.  Off (0) in the product build: the checks compile away. */
+#ifndef FSPH_DEBUG_BOUNDS
+#define FSPH_DEBUG_BOUNDS 0
+#endif
+enum : unsigned int {
+    kBoundSlot = 1u,      /* a neighbour slot (list entry or cell walk) >= n */
+    kBoundCell = 2u,      /* a cell-table row outside the scene's cells */
+    kBoundCount = 8u,     /* a list count above kListMax that is not the overflow mark */
+    kBoundBoundary = 16u  /* a boundary slot >= nb */
+};
+/* v if v < limit, else record `bit` and give 0 */
+__device__ __forceinline__ unsigned int bounded(const DevParams &p, unsigned int v, unsigned int limit,
+                                                unsigned int bit) {
+#if FSPH_DEBUG_BOUNDS
+    if (v >= limit) {
+        if (p.dbg) atomicOr(p.dbg, bit);
+        return 0u;
+    }
+#else
+    (void)p; (void)limit; (void)bit;
+#endif
+    return v;
+}
+/* a cell-table row [base - 1, base + 2] inside the scene's cells (the table
+ * has one more entry than cells): false (recorded) when not */
+__device__ __forceinline__ bool cell_row_ok(const DevParams &p, unsigned int base) {
+#if FSPH_DEBUG_BOUNDS
+    const unsigned int end = p.cell_off + (unsigned int)p.gx * (unsigned int)p.gy * (unsigned int)p.gz;
+    if (base < p.cell_off + 1u || base + 2u > end) {
+        if (p.dbg) atomicOr(p.dbg, kBoundCell);
+        return false;
+    }
+#else
+    (void)p; (void)base;
+#endif
+    return true;
+}
 
 /* Neighbour lists: up to kListMax entries per particle, transposed (entry
  * k of slot i at list_at(k, i, n)) so a warp's lanes read consecutive
@@ -157,7 +202,7 @@ struct DevCtl {
     unsigned int disp2_bits;    /* max |x* - xb|^2 of the last correction pass (float bits) */
     unsigned int mlp_err;       /* 1 when a tcgen05 inference gave up waiting on an MMA */
     float err1, err2, errmax;   /* errors of the last lambda pass */
-    float pad2;
+    unsigned int bounds_bits;   /* FSPH_DEBUG_BOUNDS builds: the index checks that failed (kBound*) */
 };
 
 /* Per-block partial sums of the lambda pass (one-sided, two-sided, max). */
@@ -357,8 +402,9 @@ __device__ inline void row_range(const unsigned int *__restrict__ cell_start, in
     unsigned int base = p.cell_off +
                         ((unsigned int)(c.z + dz) * (unsigned int)p.gy + (unsigned int)(c.y + dy)) * (unsigned int)p.gx +
                         (unsigned int)c.x;
+    if (!cell_row_ok(p, base)) { s = e = 0u; return; }
     s = __ldg(cell_start + base - 1);
-    e = __ldg(cell_start + base + 2);
+    e = bounded(p, __ldg(cell_start + base + 2), (unsigned int)p.n + 1u, kBoundSlot);
 }
 
 /* Warp/block reductions. */

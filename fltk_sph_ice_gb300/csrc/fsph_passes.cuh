@@ -115,7 +115,13 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
                                                    const unsigned char *__restrict__ cnt,
                                                    const unsigned int *__restrict__ cellb, int i, float3 xi,
                                                    unsigned int *rs, int sub, Load &&load, F &&f) {
-    const int k = list ? (int)cnt[i] : (int)kListOverflow;
+    int k = list ? (int)cnt[i] : (int)kListOverflow;
+#if FSPH_DEBUG_BOUNDS
+    if (k > kListMax && k != (int)kListOverflow) { /* a count the build never writes: walk the cells */
+        if (p.dbg) atomicOr(p.dbg, kBoundCount);
+        k = (int)kListOverflow;
+    }
+#endif
 #ifdef FSPH_LIST_GROUPED
     if (LPP == 1 && kBatch == 4 && k != (int)kListOverflow) {
         /* one 16-byte load brings the next four entries (the tail group is
@@ -127,7 +133,10 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
         for (int t0 = 0; t0 < k; t0 += 4) {
             if (t0 + 4 * kListAhead < k) prefetch_list_group(lg + (size_t)((t0 >> 2) + kListAhead) * (size_t)p.n);
             const uint4 e = load_list_group(lg + (size_t)(t0 >> 2) * (size_t)p.n);
-            const unsigned int j[4] = {e.x, e.y, e.z, e.w};
+            const unsigned int j[4] = {bounded(p, e.x, (unsigned int)p.n, kBoundSlot),
+                                       bounded(p, e.y, (unsigned int)p.n, kBoundSlot),
+                                       bounded(p, e.z, (unsigned int)p.n, kBoundSlot),
+                                       bounded(p, e.w, (unsigned int)p.n, kBoundSlot)};
             decltype(load(0u)) xj[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) xj[u] = load(j[u]);
@@ -143,7 +152,7 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
             const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
-            rs[r * blockDim.x] = __ldg(cell_start + base - 1);
+            rs[r * blockDim.x] = cell_row_ok(p, (unsigned int)base) ? __ldg(cell_start + base - 1) : 0u;
         }
 #endif
         for (int t0 = sub; t0 < k; t0 += kBatch * LPP) {
@@ -153,10 +162,10 @@ __device__ __forceinline__ void for_each_candidate(const DevParams &p, const uns
             for (int u = 0; u < kBatch; ++u) {
                 const int t = t0 + u * LPP < k ? t0 + u * LPP : k - 1;
 #ifdef FSPH_LIST32
-                j[u] = __ldg(list + list_at(t, i, p.n));
+                j[u] = bounded(p, __ldg(list + list_at(t, i, p.n)), (unsigned int)p.n, kBoundSlot);
 #else
                 const unsigned int e = __ldg(list + list_at(t, i, p.n));
-                j[u] = rs[(e >> 12) * blockDim.x] + (e & 0xfffu);
+                j[u] = bounded(p, rs[((e >> 12) % 9u) * blockDim.x] + (e & 0xfffu), (unsigned int)p.n, kBoundSlot);
 #endif
             }
 #pragma unroll
@@ -188,7 +197,9 @@ __device__ __forceinline__ void for_each_boundary(const DevParams &p, float3 x, 
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy) {
             const unsigned int base = ci + (unsigned int)((dz * p.gy + dy) * p.gx);
-            const unsigned int s = __ldg(p.bcell + base - 1), e = __ldg(p.bcell + base + 2);
+            if (!cell_row_ok(p, base)) continue;
+            const unsigned int s = __ldg(p.bcell + base - 1);
+            const unsigned int e = bounded(p, __ldg(p.bcell + base + 2), (unsigned int)p.nb + 1u, kBoundBoundary);
             for (unsigned int j = s; j < e; ++j) f(j, __ldg(p.bpos + j));
         }
 }
@@ -248,7 +259,9 @@ __device__ __forceinline__ void build_list_body(const DevParams &p, int i, const
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
         const int base = cb + ((r / 3 - 1) * p.gy + (r % 3 - 1)) * p.gx;
-        const unsigned int s = __ldg(cell_start + base - 1), e = __ldg(cell_start + base + 2);
+        if (!cell_row_ok(p, (unsigned int)base)) continue;
+        const unsigned int s = __ldg(cell_start + base - 1);
+        const unsigned int e = bounded(p, __ldg(cell_start + base + 2), (unsigned int)p.n + 1u, kBoundSlot);
         if (e - s > 4095u) ovf = true;
         /* four candidates' loads in flight before their tests */
         for (unsigned int j0 = s; j0 < e; j0 += 4) {

@@ -161,7 +161,10 @@ typedef struct fsph_step_stats {
     float density_error_max;      /* max_i |rho_i - rho0| / rho0 */
     int status;                   /* FSPH_OK, FSPH_NOT_CONVERGED, FSPH_NAN_DETECTED */
     int kernels;                  /* kernel launches the step executed (PBF graph mode; 0 = not counted) */
-    int reserved[2];
+    int bounds_bits;              /* a library built with FSPH_DEBUG_BOUNDS (fltk_sph_ice_gb300.build
+                                     --debug-bounds): the index checks that failed this step, 1 neighbour
+                                     slot, 2 cell row, 8 list count, 16 boundary slot; always 0 otherwise */
+    int reserved[1];
 } fsph_step_stats;
 
 typedef struct fsph_ctx fsph_ctx;

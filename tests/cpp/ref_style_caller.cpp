@@ -106,6 +106,7 @@ int main(int argc, char **argv) {
     const double x0 = x[0];
     if (!m_pPS->UpdateWithoutPosAndVel((RXREAL)m_fDt, steps)) { std::fprintf(stderr, "fields failed\n"); return 1; }
     x = m_pPS->GetArrayVBO(rxParticleSystemBase::RX_POSITION);
+    const int unmoved = x[0] == x0 ? 1 : 0; /* read now: the resume check below steps the system on */
     RXREAL *rho = m_pPS->GetArrayVBO(rxParticleSystemBase::RX_DENSITY);
     double rmin = 1e30, rmax = 0.0;
     for (int i = 0; i < m_pPS->GetNumParticles(); ++i) {
@@ -135,7 +136,7 @@ int main(int argc, char **argv) {
     delete resumed;
     std::printf("particles %d max %d neighbours %zu dist_check %.3e unmoved %d density %.3f %.3f dim %.3f %.3f %.3f"
                 " resume %d\n",
-                m_pPS->GetNumParticles(), m_pPS->GetMaxParticles(), total, worst, x[0] == x0 ? 1 : 0, rmin, rmax,
+                m_pPS->GetNumParticles(), m_pPS->GetMaxParticles(), total, worst, unmoved, rmin, rmax,
                 m_pPS->GetDim()[0], m_pPS->GetDim()[1], m_pPS->GetDim()[2], same);
     delete m_pPS;
     return 0;

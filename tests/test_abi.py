@@ -33,6 +33,16 @@ def test_exports_every_declared_symbol(fsph):
     assert set(names) == set(abi.EXPORTS)
 
 
+def test_debug_bounds_library_exports_the_same_symbols(fsph):
+    """the FSPH_DEBUG_BOUNDS build is the same library with checks added"""
+    from fltk_sph_ice_gb300 import build
+    path = build.build(debug_bounds=True)
+    assert path != abi.LIB_PATH and os.path.isfile(path)
+    syms = [set(re.findall(r" T (fsph_\w+)", subprocess.run(["nm", "-D", "--defined-only", p], capture_output=True,
+                                                           text=True).stdout)) for p in (abi.LIB_PATH, path)]
+    assert syms[0] == syms[1] and set(declared_functions()) <= syms[1]
+
+
 def test_struct_layout_matches_header(tmp_path):
     c = tmp_path / "sz.c"
     c.write_text(

@@ -215,6 +215,27 @@ __device__ inline float3 operator-(float3 a, float3 b) { return make_float3(a.x 
 __device__ inline float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
 __device__ inline float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
 __device__ inline float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+/* 1 / sqrt(max(r2, 1e-20)) for the pair loops.  FSPH_RSQRT_FTZ 1 (default)
+ * issues rsqrt.approx.ftz.f32: the argument is clamped to a normal number
+ * and the result is normal, so the flush-to-zero form, which skips the
+ * handling of subnormal inputs, gives the same approximation as rsqrtf.
+ * Measured on the 1 M double dam break: the same positions bit for bit,
+ * lambda 80.1 -> 79.2 us, correction 88.7 -> 86.6 us, warm step 2.820 ->
+ * 2.769 ms, plain step 10.08 -> 9.85 ms (0, rsqrtf, is the other form). */
+#ifndef FSPH_RSQRT_FTZ
+#define FSPH_RSQRT_FTZ 1
+#endif
+__device__ __forceinline__ float pair_rsqrt(float r2) {
+    const float x = fmaxf(r2, 1e-20f);
+#if FSPH_RSQRT_FTZ
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+#else
+    return rsqrtf(x);
+#endif
+}
 __device__ inline float3 cross3(float3 a, float3 b) {
     return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }

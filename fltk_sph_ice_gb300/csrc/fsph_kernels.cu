@@ -479,7 +479,7 @@ __global__ void k_boundary_static(DevParams p, float2 *__restrict__ bstat) {
         const float3 d = xb - f3(c4);
         const float r2 = dot3(d, d);
         const float q = fmaxf(p.h2 - r2, 0.0f);
-        const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+        const float inv_r = pair_rsqrt(r2);
         const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
         const float gb = c4.w * agr * t * t * inv_r;
         bw += c4.w * q * q * q;
@@ -523,7 +523,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_lambda(DevParams p, const u
             const float3 d = xb - f3(xj4);
             const float r2 = dot3(d, d);
             const float q = fmaxf(p.h2 - r2, 0.0f);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float inv_r = pair_rsqrt(r2);
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = agr * t * t * inv_r;
             wsum += q * q * q;

@@ -324,7 +324,7 @@ __device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned 
             const float3 d = xi - f3(xj4);
             const float r2 = dot3(d, d);
             const float q = fmaxf(p.h2 - r2, 0.0f);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float inv_r = pair_rsqrt(r2);
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = agl * t * t * inv_r; /* grad W / rho0 = (agr / agl) g d */
             if (KAHAN) { /* compensated sum of the density terms */
@@ -360,7 +360,7 @@ __device__ __forceinline__ float lambda_body(const DevParams &p, const unsigned 
             const float3 d = xi - f3(b4);
             const float r2 = dot3(d, d);
             const float q = fmaxf(p.h2 - r2, 0.0f);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float inv_r = pair_rsqrt(r2);
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float gb = b4.w * agr * t * t * inv_r;
             bw += b4.w * q * q * q;
@@ -474,7 +474,7 @@ __device__ __forceinline__ float correction_body(const DevParams &p, const unsig
             /* branch-free: t = 0 outside h and d = 0 for the self pair */
             const float3 d = xi - f3(xj4);
             const float r2 = dot3(d, d);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float inv_r = pair_rsqrt(r2);
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = agl * t * t * inv_r;
             float coef = li + xj4.w;
@@ -510,7 +510,7 @@ __device__ __forceinline__ float correction_body(const DevParams &p, const unsig
         for_each_boundary(p, xi, [&](unsigned int b, const float4 &b4) {
             const float3 d = xi - f3(b4);
             const float r2 = dot3(d, d);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float inv_r = pair_rsqrt(r2);
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = agr * t * t * inv_r;
             float sc = 0.0f;
@@ -615,7 +615,7 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
             const float r2 = dot3(d, d);
             const float inside = r2 < p.h2 ? 1.0f : 0.0f;
             const float q = fmaxf(p.h2 - r2, 0.0f);
-            const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+            const float inv_r = pair_rsqrt(r2);
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = p.ag * t * t * inv_r;
             const float3 vij = f3(__ldg(vel + j)) - vi;
@@ -631,7 +631,7 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
                 const float3 ds = d - p.dt * vij;
                 const float r2s = dot3(ds, ds);
                 const float qs = fmaxf(p.h2 - r2s, 0.0f);
-                const float inv_rs = rsqrtf(fmaxf(r2s, 1e-20f));
+                const float inv_rs = pair_rsqrt(r2s);
                 const float ts = fmaxf(p.h - r2s * inv_rs, 0.0f);
                 wpred += qs * qs * qs;
                 cg = cg + (p.ag * ts * ts * inv_rs) * ds;
@@ -700,7 +700,7 @@ __device__ __forceinline__ void vort_apply_body(const DevParams &p, int i, const
             [&](unsigned int j, const float4 &xj4) {
                 const float3 d = xi - f3(xj4);
                 const float r2 = dot3(d, d);
-                const float inv_r = rsqrtf(fmaxf(r2, 1e-20f));
+                const float inv_r = pair_rsqrt(r2);
                 const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
                 const float g = p.ag * t * t * inv_r;
                 const float3 wj = f3(__ldg(vort + j));

@@ -590,7 +590,7 @@ int alloc_particles(fsph_ctx *c, int cap) {
         FSPH_TRY(dalloc(c, &c->radix.hist, nh)); FSPH_TRY(dalloc(c, &c->radix.offs, nh + 1)); /* + the total */
         FSPH_TRY(dalloc(c, &c->radix.bsum, scan_blocks((unsigned int)nh)));
     }
-    FSPH_TRY(dalloc(c, &c->epart, blocks_for((long long)n, kPassBlock)));
+    FSPH_TRY(dalloc(c, &c->epart, 2 * blocks_for((long long)n, kPassBlock))); /* room for ErrPartialFix */
     FSPH_TRY(dalloc(c, &c->dpart, blocks_for((long long)n, kPassBlock)));
     for (int k = 0; k < 2; ++k) {
         FSPH_CUDA(c, cudaMemsetAsync(c->set[k].pos, 0, n * sizeof(float4), c->stream));

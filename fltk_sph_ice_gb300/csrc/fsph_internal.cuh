@@ -203,11 +203,19 @@ struct DevCtl {
     unsigned int mlp_err;       /* 1 when a tcgen05 inference gave up waiting on an MMA */
     float err1, err2, errmax;   /* errors of the last lambda pass */
     unsigned int bounds_bits;   /* FSPH_DEBUG_BOUNDS builds: the index checks that failed (kBound*) */
+    unsigned int grab, grab2;   /* FSPH_DYN_CHUNKS: chunks handed out on demand (lambda, correction pass) */
 };
 
 /* Per-block partial sums of the lambda pass (one-sided, two-sided, max). */
 struct ErrPartial {
     float s1, s2, mx, pad;
+};
+/* The same in fixed point (units of 2^-32, exact and order-free sums) for
+ * the lambda pass with chunks handed out on demand; occupies two ErrPartial
+ * slots per block. */
+struct ErrPartialFix {
+    unsigned long long s1, s2;
+    float mx, pad[3];
 };
 
 __host__ __device__ inline float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }

@@ -334,6 +334,28 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_lambda(DevParams
     const unsigned int par = *((volatile unsigned int *)&ctl->parity);
     float4 *pp = par ? ppos1 : ppos0;
     float e1 = 0.f, e2 = 0.f, em = 0.f;
+#if FSPH_PERSIST_LAMBDA && FSPH_DYN_CHUNKS
+    /* persistent warps: whole round-robin rounds, then the leftover chunks
+     * on demand; the error sums are fixed point, exact in any order */
+    unsigned long long q1 = 0ull, q2 = 0ull;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5, nchunks = (p.n + 31) >> 5;
+    const int stat = max(nchunks / nw - FSPH_DYN_EXTRA, 0) * nw;
+    for (int c = first_chunk((blockIdx.x * blockDim.x + threadIdx.x) >> 5, stat, &ctl->grab, lane); c < nchunks;
+         c = next_chunk(c, nw, stat, &ctl->grab, lane)) {
+        const int i = c * 32 + lane;
+        if (i < p.n) {
+            const float C = lambda_body<1, KAHAN>(p, cell_start, pp, dens, ctl, list, cnt, cellb, s_rs + threadIdx.x,
+                                                  i, 0, true);
+            q1 += err_fix(C > 0.0f ? C : 0.0f);
+            q2 += err_fix(fabsf(C));
+            em = fmaxf(em, fabsf(C));
+        }
+    }
+    (void)e1; (void)e2;
+    lambda_tail_fix(p, ctl, part, q1, q2, em, hwhile, use_graph);
+}
+#else
 #if FSPH_PERSIST_LAMBDA
     /* persistent warps: warp w takes the 32-slot chunks w, w + W, ... in a
      * fixed order (the error sums stay deterministic) */
@@ -355,6 +377,7 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_lambda(DevParams
     }
     lambda_tail(p, ctl, part, e1, e2, em, hwhile, use_graph);
 }
+#endif
 
 /* correction pass: dp_i = sum_j (lambda_i + lambda_j + s_corr) grad W_ij / rho0,
  * x*_i <- walls(x*_i + dp_i) into the other ping-pong buffer; the largest
@@ -374,7 +397,13 @@ __global__ void __launch_bounds__(kPassBlock, FSPH_PASS_MINB) k_correction(DevPa
     const float4 *__restrict__ src = par ? ppos1 : ppos0;
     float4 *__restrict__ dst = par ? ppos0 : ppos1;
     float disp2 = 0.f;
-#if FSPH_PERSIST_CORRECTION
+#if FSPH_PERSIST_CORRECTION && FSPH_DYN_CHUNKS
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5, nchunks = (p.n + 31) >> 5, stat = (nchunks / nw) * nw;
+    for (int c = first_chunk((blockIdx.x * blockDim.x + threadIdx.x) >> 5, stat, &ctl->grab2, lane); c < nchunks;
+         c = next_chunk(c, nw, stat, &ctl->grab2, lane)) {
+        const int i = c * 32 + lane;
+#elif FSPH_PERSIST_CORRECTION
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c * 32 < p.n; c += nw) {

@@ -41,7 +41,8 @@ constexpr size_t kOffX = align256(kOffPerm + kMaxP * 4);                    /* f
 constexpr size_t kOffDens = align256(kOffX + kMaxP * 16);
 constexpr size_t kOffCtl = align256(kOffDens + kMaxP * 4);
 constexpr size_t kOffPart = align256(kOffCtl + sizeof(DevCtl));
-constexpr size_t kScratchBytes = align256(kOffPart + ((kMaxP + kPassBlock - 1) / kPassBlock) * sizeof(ErrPartial));
+/* two ErrPartial slots per block: room for the fixed-point partials (ErrPartialFix) */
+constexpr size_t kScratchBytes = align256(kOffPart + 2 * ((kMaxP + kPassBlock - 1) / kPassBlock) * sizeof(ErrPartial));
 
 constexpr int kMaxDevices = 64;
 

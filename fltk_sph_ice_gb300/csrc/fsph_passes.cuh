@@ -56,6 +56,23 @@ constexpr int kBatch = FSPH_KBATCH;
 #define FSPH_PERSIST_LAMBDA FSPH_PERSIST
 #define FSPH_PERSIST_CORRECTION FSPH_PERSIST
 #endif
+/* FSPH_DYN_CHUNKS 1 (default): the persistent passes take their last
+ * chunks on demand (an atomic counter per pass) instead of round-robin, so
+ * warps that finish early take the leftovers; the lambda pass then sums its
+ * errors in 64-bit fixed point (units of 2^-32), which is exact and so
+ * independent of which warp ran which chunk.  FSPH_DYN_EXTRA whole rounds
+ * join the leftovers in the on-demand pool.  Measured on the 1M double dam
+ * break (same positions bit for bit): lambda 78.1 -> 75.6 us with the
+ * leftovers alone, 73.7 us with one more round (default), 75 / 76 us with
+ * two / three, 81 us with every chunk on demand (the counter contends);
+ * the correction pass made persistent this way got slower (86 -> 92 us) and
+ * stays a plain grid. */
+#ifndef FSPH_DYN_CHUNKS
+#define FSPH_DYN_CHUNKS 1
+#endif
+#ifndef FSPH_DYN_EXTRA
+#define FSPH_DYN_EXTRA 1
+#endif
 #ifndef FSPH_PERSIST_LAMBDA
 #define FSPH_PERSIST_LAMBDA 1
 #endif
@@ -440,6 +457,94 @@ __device__ __forceinline__ void lambda_tail(const DevParams &lp, DevCtl *ctl, Er
     }
 }
 
+/* |C| in units of 2^-32, saturating (a diverged step is caught by the NaN
+ * flag and the error itself) */
+__device__ __forceinline__ unsigned long long err_fix(float x) {
+    return (unsigned long long)__float2ll_rn(fminf(x, 1024.0f) * 4294967296.0f);
+}
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+/* the next chunk of a persistent pass: round-robin while whole rounds last,
+ * then on demand from the pass's counter (warp-uniform) */
+__device__ __forceinline__ int next_chunk(int c, int nw, int stat, unsigned int *ctr, int lane) {
+    c += nw;
+    if (c < stat) return c;
+    unsigned int v = 0u;
+    if (lane == 0) v = atomicAdd(ctr, 1u);
+    return stat + (int)__shfl_sync(0xffffffffu, v, 0);
+}
+__device__ __forceinline__ int first_chunk(int w, int stat, unsigned int *ctr, int lane) {
+    if (w < stat) return w;
+    unsigned int v = 0u;
+    if (lane == 0) v = atomicAdd(ctr, 1u);
+    return stat + (int)__shfl_sync(0xffffffffu, v, 0);
+}
+
+/* lambda_tail for fixed-point error sums: integer sums are exact, so the
+ * block partials may combine in any order */
+__device__ __forceinline__ void lambda_tail_fix(const DevParams &lp, DevCtl *ctl, ErrPartial *part,
+                                                unsigned long long q1, unsigned long long q2, float em,
+                                                cudaGraphConditionalHandle hwhile, int use_graph) {
+    __shared__ unsigned long long sq1[32], sq2[32];
+    __shared__ float shm[32];
+    __shared__ int s_last;
+    ErrPartialFix *pf = reinterpret_cast<ErrPartialFix *>(part);
+    q1 = warp_sum_u64(q1);
+    q2 = warp_sum_u64(q2);
+    em = warp_max(em);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) { sq1[warp] = q1; sq2[warp] = q2; shm[warp] = em; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = 0ull, b = 0ull;
+        float m = 0.f;
+        for (int w = 0; w < nw; ++w) { a += sq1[w]; b += sq2[w]; m = fmaxf(m, shm[w]); }
+        pf[blockIdx.x].s1 = a;
+        pf[blockIdx.x].s2 = b;
+        pf[blockIdx.x].mx = m;
+        __threadfence();
+        unsigned int t = atomicAdd(&ctl->ticket, 1u);
+        s_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    unsigned long long a = 0ull, b = 0ull;
+    float m = 0.f;
+    for (unsigned int k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+        a += __ldcg(&pf[k].s1);
+        b += __ldcg(&pf[k].s2);
+        m = fmaxf(m, __ldcg(&pf[k].mx));
+    }
+    a = warp_sum_u64(a);
+    b = warp_sum_u64(b);
+    m = warp_max(m);
+    __syncthreads(); /* every warp has read its shared entries above */
+    if (lane == 0) { sq1[warp] = a; sq2[warp] = b; shm[warp] = m; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = 0ull; b = 0ull; m = 0.f;
+        for (int w = 0; w < nw; ++w) { a += sq1[w]; b += sq2[w]; m = fmaxf(m, shm[w]); }
+        float err1 = (float)((double)a * 0x1p-32 / (double)lp.n);
+        float err2 = (float)((double)b * 0x1p-32 / (double)lp.n);
+        ctl->err1 = err1;
+        ctl->err2 = err2;
+        ctl->errmax = m;
+        unsigned int it = ctl->iter + 1u;
+        ctl->iter = it;
+        float err = lp.error_mode ? err2 : err1;
+        int minit = lp.min_iter > 1 ? lp.min_iter : 1;
+        int cont = ((int)it < lp.max_iter) && !(err <= lp.eta && (int)it >= minit);
+        if (ctl->nan_flag) cont = 0;
+        ctl->done = cont ? 0u : 1u;
+        ctl->ticket = 0u;
+        ctl->grab = 0u; /* every block has passed its loop: the counter is free for the next pass */
+        if (use_graph & 1) cudaGraphSetConditional(hwhile, cont ? 1u : 0u);
+    }
+}
+
 /* correction pass of one particle: dp_i = sum_j (lambda_i + lambda_j + s_corr)
  * grad W_ij / rho0, x*_i <- walls(x*_i + dp_i) into dst (lane 0 of a valid
  * group).  Returns |x*_i - xb_i|^2 (0 for the other lanes). */
@@ -571,6 +676,7 @@ __device__ __forceinline__ void correction_tail(const DevParams &lp, DevCtl *ctl
         ctl->rebuild = rb;
         ctl->parity = 1u - par;
         ctl->ticket2 = 0u;
+        ctl->grab2 = 0u;
         if (use_graph & 1) {
             unsigned int more = ctl->done ? 0u : 1u;
             cudaGraphSetConditional(hif, rb & more);

@@ -383,6 +383,24 @@ def ncu_warp_instructions(kname: str):
     return None
 
 
+def ncu_l1tex(kname: str):
+    """L1TEX throughput of one launch of kname at 1M particles, % of its peak
+    while the SMs are active, from the committed ncu summary (the pass's
+    binding unit: the gathered positions and streamed list groups); None if
+    absent or captured from other kernel sources than these."""
+    import re
+    if not profile_current():
+        return None
+    with open(TRAFFIC_PROFILE) as f:
+        for line in f:
+            if line.startswith("| **L1TEX throughput"):
+                m = [float(x) for x in re.findall(r"([0-9.]+) %", line)]
+                col = {"k_lambda": 0, "k_correction": 1}.get(kname)
+                if col is not None and len(m) >= 2:
+                    return {"pct_of_peak_active": m[col], "source": "ncu l1tex__throughput"}
+    return None
+
+
 def issue_bound(kname: str, launch_ms: float):
     """The pass against the instruction-issue bound: the profiled warp
     instructions of one launch over its live launch time, against one warp
@@ -424,7 +442,7 @@ def roofline_of(L, abi, ps, n, mean_iters):
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": traffic, "traffic_source": src, "kernel": kname, "launch_ms": kms, "peak_kind": peak_kind,
             "lambda_ms": t_lam.value, "correction_ms": t_cor.value, "grid_build_ms": t_grid.value,
-            "list_build_ms": t_list.value, "issue": issue_bound(kname, kms),
+            "list_build_ms": t_list.value, "issue": issue_bound(kname, kms), "l1tex": ncu_l1tex(kname),
             "passes_ms_per_step": mean_iters * (t_lam.value + t_cor.value)}
 
 

@@ -12,6 +12,9 @@ def test_profile_figures_are_read(monkeypatch):
         i = bench.ncu_warp_instructions(k)
         assert t is not None and 1e7 < t < 1e10
         assert i is not None and 1e6 < i < 1e10
+        l1 = bench.ncu_l1tex(k)
+        assert l1 is not None and 0.0 < l1["pct_of_peak_active"] <= 100.0
+    assert bench.ncu_l1tex("k_other") is None
     assert bench.ncu_traffic("k_other") is None
     assert bench.ncu_warp_instructions("k_other") is None
 
@@ -21,6 +24,7 @@ def test_stale_profile_figures_are_dropped(monkeypatch):
     assert not bench.profile_current()
     assert bench.ncu_traffic("k_lambda") is None
     assert bench.ncu_warp_instructions("k_lambda") is None
+    assert bench.ncu_l1tex("k_lambda") is None
     d = bench.kernel_sources_digest()
     assert len(d) == 12 and int(d, 16) >= 0
     monkeypatch.setattr(bench, "profile_digest", lambda: d)

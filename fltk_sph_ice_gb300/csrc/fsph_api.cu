@@ -76,6 +76,8 @@ struct fsph_ctx {
     BufSet set[2];
     float4 *ppos[2] = {nullptr, nullptr};
     float4 *xb = nullptr, *acc = nullptr, *vort = nullptr;
+    float *mrho = nullptr;  /* m / rho per particle, for the XSPH and vorticity passes */
+    float2 *wm = nullptr;   /* (|omega|, m / rho) per particle, from the XSPH pass to the vorticity pass */
     float *dens = nullptr, *pres = nullptr;
     unsigned int *key = nullptr, *rank = nullptr, *perm = nullptr;
     NbrLists nl;
@@ -305,6 +307,9 @@ void free_particles(fsph_ctx *c) {
     c->xpred = c->dstep = c->dwarm = c->tmp4 = nullptr;
     c->feat = nullptr;
     c->xb = c->acc = c->vort = nullptr;
+    cudaFree(c->mrho); cudaFree(c->wm);
+    c->mrho = nullptr;
+    c->wm = nullptr;
     c->dens = c->pres = nullptr;
     c->key = c->rank = c->perm = nullptr;
     c->epart = nullptr;
@@ -573,6 +578,7 @@ int alloc_particles(fsph_ctx *c, int cap) {
         FSPH_TRY(dalloc(c, &c->ppos[k], n));
     }
     FSPH_TRY(dalloc(c, &c->xb, n)); FSPH_TRY(dalloc(c, &c->acc, n)); FSPH_TRY(dalloc(c, &c->vort, n));
+    FSPH_TRY(dalloc(c, &c->mrho, n)); FSPH_TRY(dalloc(c, &c->wm, n));
     FSPH_TRY(dalloc(c, &c->dens, n)); FSPH_TRY(dalloc(c, &c->pres, n));
     FSPH_TRY(dalloc(c, &c->key, n)); FSPH_TRY(dalloc(c, &c->rank, n)); FSPH_TRY(dalloc(c, &c->perm, n));
     FSPH_TRY(dalloc(c, &c->res_id, n));
@@ -750,12 +756,20 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     return it;
 }
 
+/* FSPH_POST_PRE 1 (default): k_finalize writes m / rho per particle and the
+ * XSPH pass hands (|omega|, m / rho) to the vorticity pass, so neither
+ * divides nor takes a square root per pair (0: per pair, as before; the
+ * results are the same bit for bit). */
+#ifndef FSPH_POST_PRE
+#define FSPH_POST_PRE 1
+#endif
 void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
     const bool ws = pbf_warm_active(c);
+    const bool ext = pbf_finalize_ext(c), pre = ext && FSPH_POST_PRE;
     launch_finalize(p, c->set[it].pos, c->ppos[0], c->ppos[1], c->ctl, c->set[it].id, c->set[it].attr,
                     c->set[0].pos, c->set[0].vel, c->set[0].id, c->set[0].attr, ws ? c->xpred : nullptr,
-                    ws ? c->dstep : nullptr, s);
-    if (pbf_finalize_ext(c)) {
+                    ws ? c->dstep : nullptr, s, c->dens, pre ? c->mrho : nullptr);
+    if (ext) {
         FeatureOut fo;
         if (ws) {
             fo.feat = c->feat;
@@ -767,8 +781,9 @@ void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
             fo.valid = c->warm_valid;
         }
         launch_xsph_vort(p, c->cell_start, c->set[0].pos, c->set[0].vel, c->dens, c->set[1].vel, c->vort, fo, c->nl,
-                         s);
-        launch_vort_apply(p, c->cell_start, c->set[0].pos, c->vort, c->dens, c->set[1].vel, c->set[0].vel, c->nl, s);
+                         s, pre ? c->mrho : nullptr, pre ? c->wm : nullptr);
+        launch_vort_apply(p, c->cell_start, c->set[0].pos, c->vort, c->dens, c->set[1].vel, c->set[0].vel, c->nl, s,
+                          pre ? c->wm : nullptr);
     }
 }
 

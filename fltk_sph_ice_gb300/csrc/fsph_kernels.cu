@@ -426,9 +426,10 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
                            const unsigned int *__restrict__ attr_b, float4 *__restrict__ pos_a,
                            float4 *__restrict__ vel_a, unsigned int *__restrict__ id_a,
                            unsigned int *__restrict__ attr_a, const float4 *__restrict__ xpred,
-                           float4 *__restrict__ dstep) {
+                           float4 *__restrict__ dstep, const float *__restrict__ dens, float *__restrict__ mrho) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    if (mrho) mrho[i] = p.mass / dens[i]; /* m / rho_i for the XSPH and vorticity passes */
     const float4 *pp = ctl->parity ? ppos1 : ppos0;
     float3 xs = f3(pp[i]);
     float3 x = f3(pos_b[i]);
@@ -446,22 +447,25 @@ __global__ void k_finalize(DevParams p, const float4 *__restrict__ pos_b, const 
 
 /* omega_i = sum_j (v_j - v_i) x grad_j W_ij (grad_j = -grad_i), and the
  * XSPH update v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij. */
-template <bool NBR>
+template <bool NBR, bool PRE>
 __global__ void __launch_bounds__(kBlock) k_xsph_vort(DevParams p, const unsigned int *__restrict__ cell_start,
                                                       const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                       const float *__restrict__ dens, float4 *__restrict__ vel_out,
                                                       float4 *__restrict__ vort, FeatureOut fo,
                                                       const ListEntry *__restrict__ list,
                                                       const unsigned char *__restrict__ cnt,
-                                                      const unsigned int *__restrict__ cellb) {
+                                                      const unsigned int *__restrict__ cellb,
+                                                      const float *__restrict__ mrho, float2 *__restrict__ wm) {
     __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    xsph_vort_body<NBR>(p, i, cell_start, pos, vel, dens, vel_out, vort, fo, list, cnt, cellb, s_rs + threadIdx.x);
+    xsph_vort_body<NBR, PRE>(p, i, cell_start, pos, vel, dens, vel_out, vort, fo, list, cnt, cellb,
+                             s_rs + threadIdx.x, mrho, wm);
 }
 
 /* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
  * v_i <- v_i + dt f. */
+template <bool PRE>
 __global__ void __launch_bounds__(kBlock) k_vort_apply(DevParams p, const unsigned int *__restrict__ cell_start,
                                                        const float4 *__restrict__ pos,
                                                        const float4 *__restrict__ vort,
@@ -470,11 +474,13 @@ __global__ void __launch_bounds__(kBlock) k_vort_apply(DevParams p, const unsign
                                                        float4 *__restrict__ vel_out,
                                                        const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
-                                                       const unsigned int *__restrict__ cellb) {
+                                                       const unsigned int *__restrict__ cellb,
+                                                       const float2 *__restrict__ wm) {
     __shared__ unsigned int s_rs[9 * kBlock];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    vort_apply_body(p, i, cell_start, pos, vort, dens, vel_in, vel_out, list, cnt, cellb, s_rs + threadIdx.x);
+    vort_apply_body<PRE>(p, i, cell_start, pos, vort, dens, vel_in, vel_out, list, cnt, cellb, s_rs + threadIdx.x,
+                         wm);
 }
 
 /* ======================================================================== */
@@ -1032,22 +1038,26 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
 void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
                      const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,
                      float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, const float4 *xpred, float4 *dstep,
-                     cudaStream_t s) {
+                     cudaStream_t s, const float *dens, float *mrho) {
     k_finalize<<<blocks_for(p.n), kBlock, 0, s>>>(p, pos_b, ppos0, ppos1, ctl, id_b, attr_b, pos_a, vel_a, id_a,
-                                                  attr_a, xpred, dstep);
+                                                  attr_a, xpred, dstep, dens, mrho);
 }
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
                       const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, const NbrLists &nl,
-                      cudaStream_t s) {
+                      cudaStream_t s, const float *mrho, float2 *wm) {
     /* the neighbour means cost a gather per pair: only when they are used */
-    auto k = (fo.feat && fo.nbr) ? k_xsph_vort<true> : k_xsph_vort<false>;
+    const bool nbr = fo.feat && fo.nbr, pre = mrho && wm;
+    auto k = nbr ? (pre ? k_xsph_vort<true, true> : k_xsph_vort<true, false>)
+                 : (pre ? k_xsph_vort<false, true> : k_xsph_vort<false, false>);
     k<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, vel_out, vort, fo,
-                                         p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
+                                         p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb, mrho, wm);
 }
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
-                       const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s) {
-    k_vort_apply<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vort, dens, vel_in, vel_out,
-                                                    p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb);
+                       const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s,
+                       const float2 *wm) {
+    auto k = wm ? k_vort_apply<true> : k_vort_apply<false>;
+    k<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vort, dens, vel_in, vel_out,
+                                         p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb, wm);
 }
 void launch_sph_density(const DevParams &p, const unsigned int *cell_start, float4 *pos, float4 *vel, float *dens,
                         float *pres, const NbrLists &nl, cudaStream_t s) {

@@ -86,13 +86,17 @@ void launch_correction(const DevParams &p, const unsigned int *cell_start, float
 void launch_finalize(const DevParams &p, const float4 *pos_b, const float4 *ppos0, const float4 *ppos1,
                      const DevCtl *ctl, const unsigned int *id_b, const unsigned int *attr_b, float4 *pos_a,
                      float4 *vel_a, unsigned int *id_a, unsigned int *attr_a, const float4 *xpred, float4 *dstep,
-                     cudaStream_t s);
-/* XSPH + vorticity (omega) pass; with fo.feat also the warm-start features */
+                     cudaStream_t s, const float *dens = nullptr, float *mrho = nullptr);
+/* XSPH + vorticity (omega) pass; with fo.feat also the warm-start features.
+ * With mrho (m / rho per particle, from launch_finalize) and wm the pass
+ * reads m / rho_j instead of dividing per pair and leaves (|omega|, m / rho)
+ * in wm, which launch_vort_apply then gathers in place of vort and dens. */
 void launch_xsph_vort(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
                       const float *dens, float4 *vel_out, float4 *vort, const FeatureOut &fo, const NbrLists &nl,
-                      cudaStream_t s);
+                      cudaStream_t s, const float *mrho = nullptr, float2 *wm = nullptr);
 void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
-                       const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s);
+                       const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s,
+                       const float2 *wm = nullptr);
 
 /* ---- static boundary particles (p.bpos / p.bcell / p.bnear of the sorted boundary) ---- */
 /* bscale[b] = rho0 psi_b / m with psi_b = m / sum_b' m W(r_bb') (rx_sph_pbd.cpp:1061-1090) */

@@ -695,14 +695,19 @@ __device__ __forceinline__ void correction_tail(const DevParams &lp, DevCtl *ctl
  * eps = 1e-4 then drives the flow unstable).  The XSPH update
  * v_i + c sum_j (m / rho_j)(v_j - v_i) W_ij, and (fo.feat) the warm-start
  * features of the particle. */
-template <bool NBR = true>
+/* PRE: m / rho_j comes from mrho (written once per particle by k_finalize,
+ * the same correctly rounded quotient) instead of a division per pair, and
+ * the pass leaves (|omega_i|, m / rho_i) in wm for vort_apply_body<true>. */
+template <bool NBR = true, bool PRE = false>
 __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
                                                const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                                                const float *__restrict__ dens, float4 *__restrict__ vel_out,
                                                float4 *__restrict__ vort, const FeatureOut &fo,
                                                const ListEntry *__restrict__ list,
                                                const unsigned char *__restrict__ cnt,
-                                               const unsigned int *__restrict__ cellb, unsigned int *rs) {
+                                               const unsigned int *__restrict__ cellb, unsigned int *rs,
+                                               const float *__restrict__ mrho_in = nullptr,
+                                               float2 *__restrict__ wm = nullptr) {
     const float3 xi = f3(pos[i]), vi = f3(vel[i]);
     float3 om = make_float3(0.f, 0.f, 0.f), xs = make_float3(0.f, 0.f, 0.f);
     float3 off = make_float3(0.f, 0.f, 0.f), cg = make_float3(0.f, 0.f, 0.f);
@@ -725,8 +730,8 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
             const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
             const float g = p.ag * t * t * inv_r;
             const float3 vij = f3(__ldg(vel + j)) - vi;
-            const float rhoj = __ldg(dens + j);
-            const float mrho = p.mass / rhoj;
+            const float rhoj = (NBR || !PRE) ? __ldg(dens + j) : 0.0f;
+            const float mrho = PRE ? __ldg(mrho_in + j) : p.mass / rhoj;
             om = om + cross3(vij, (-g * mrho) * d);
             xs = xs + (p.aw * q * q * q * mrho) * vij;
             cntf += inside;
@@ -754,6 +759,7 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
     float3 vn = vi + p.xsph_c * xs;
     vel_out[i] = make_float4(vn.x, vn.y, vn.z, 0.0f);
     vort[i] = make_float4(om.x, om.y, om.z, 0.0f);
+    if (PRE) wm[i] = make_float2(sqrtf(dot3(om, om)), mrho_in[i]);
     if (fo.feat) {
         /* warm-start features at the end of the step (dimensionless; see kFeatures) */
         const float inv_h = 1.0f / p.h;
@@ -789,12 +795,16 @@ __device__ __forceinline__ void xsph_vort_body(const DevParams &p, int i, const 
 
 /* eta_i = sum_j (m / rho_j)(|w_j| - |w_i|) grad_i W_ij; f = eps (eta/|eta|) x w_i;
  * v_i <- v_i + dt f. */
+/* PRE: (|omega_j|, m / rho_j) from wm (one 8-byte gather per pair, no
+ * division or square root; the same values xsph_vort_body<.., true> wrote). */
+template <bool PRE = false>
 __device__ __forceinline__ void vort_apply_body(const DevParams &p, int i, const unsigned int *__restrict__ cell_start,
                                                 const float4 *__restrict__ pos, const float4 *__restrict__ vort,
                                                 const float *__restrict__ dens, const float4 *__restrict__ vel_in,
                                                 float4 *__restrict__ vel_out, const ListEntry *__restrict__ list,
                                                 const unsigned char *__restrict__ cnt,
-                                                const unsigned int *__restrict__ cellb, unsigned int *rs) {
+                                                const unsigned int *__restrict__ cellb, unsigned int *rs,
+                                                const float2 *__restrict__ wm = nullptr) {
     float4 v4 = vel_in[i];
     if (p.vort_eps != 0.0f) {
         const float3 xi = f3(pos[i]);
@@ -809,8 +819,14 @@ __device__ __forceinline__ void vort_apply_body(const DevParams &p, int i, const
                 const float inv_r = pair_rsqrt(r2);
                 const float t = fmaxf(p.h - r2 * inv_r, 0.0f);
                 const float g = p.ag * t * t * inv_r;
-                const float3 wj = f3(__ldg(vort + j));
-                const float k = p.mass / __ldg(dens + j) * (sqrtf(dot3(wj, wj)) - wmi) * g;
+                float k;
+                if (PRE) {
+                    const float2 b = __ldg(wm + j); /* (|omega_j|, m / rho_j) */
+                    k = b.y * (b.x - wmi) * g;
+                } else {
+                    const float3 wj = f3(__ldg(vort + j));
+                    k = p.mass / __ldg(dens + j) * (sqrtf(dot3(wj, wj)) - wmi) * g;
+                }
                 eta = eta + k * d;
             });
         float en = sqrtf(dot3(eta, eta));

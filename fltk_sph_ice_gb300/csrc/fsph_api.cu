@@ -756,13 +756,6 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     return it;
 }
 
-/* FSPH_POST_PRE 1 (default): k_finalize writes m / rho per particle and the
- * XSPH pass hands (|omega|, m / rho) to the vorticity pass, so neither
- * divides nor takes a square root per pair (0: per pair, as before; the
- * results are the same bit for bit). */
-#ifndef FSPH_POST_PRE
-#define FSPH_POST_PRE 1
-#endif
 void enqueue_pbf_post(fsph_ctx *c, const DevParams &p, int it, cudaStream_t s) {
     const bool ws = pbf_warm_active(c);
     const bool ext = pbf_finalize_ext(c), pre = ext && FSPH_POST_PRE;

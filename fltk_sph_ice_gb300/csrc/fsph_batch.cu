@@ -166,6 +166,18 @@ __global__ void __launch_bounds__(BLOCK, FSPH_PASS_THREADS / BLOCK) kb_correctio
     correction_tail(lp, ctl, part, worst, par, hif, hif2, use_graph);
 }
 
+/* m / rho_i of every particle with its scene's mass, for the XSPH and
+ * vorticity passes (FSPH_POST_PRE) */
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) kb_mrho(BatchArgs b, const float *__restrict__ dens,
+                                                 float *__restrict__ mrho) {
+    __shared__ DevParams s_p;
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const BTile tl = tile_begin(b, t, s_p);
+        if ((int)threadIdx.x < tl.count) mrho[tl.start + threadIdx.x] = s_p.mass / dens[tl.start + threadIdx.x];
+    }
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) kb_xsph_vort(BatchArgs b, const unsigned int *__restrict__ cell_start,
                                                       const float4 *__restrict__ pos, const float4 *__restrict__ vel,
@@ -173,7 +185,8 @@ __global__ void __launch_bounds__(BLOCK) kb_xsph_vort(BatchArgs b, const unsigne
                                                       float4 *__restrict__ vort,
                                                       const ListEntry *__restrict__ list,
                                                       const unsigned char *__restrict__ cnt,
-                                                      const unsigned int *__restrict__ cellb) {
+                                                      const unsigned int *__restrict__ cellb,
+                                                      const float *__restrict__ mrho, float2 *__restrict__ wm) {
     __shared__ DevParams s_p;
     __shared__ unsigned int s_rs[9 * BLOCK];
     const FeatureOut fo{};
@@ -181,8 +194,8 @@ __global__ void __launch_bounds__(BLOCK) kb_xsph_vort(BatchArgs b, const unsigne
         const BTile tl = tile_begin(b, t, s_p);
         const DevParams p = s_p;
         if ((int)threadIdx.x < tl.count)
-            xsph_vort_body(p, tl.start + threadIdx.x, cell_start, pos, vel, dens, vel_out, vort, fo, list, cnt, cellb,
-                           s_rs + threadIdx.x);
+            xsph_vort_body<false, FSPH_POST_PRE != 0>(p, tl.start + threadIdx.x, cell_start, pos, vel, dens, vel_out,
+                                                      vort, fo, list, cnt, cellb, s_rs + threadIdx.x, mrho, wm);
     }
 }
 
@@ -193,15 +206,16 @@ __global__ void __launch_bounds__(BLOCK) kb_vort_apply(BatchArgs b, const unsign
                                                        const float4 *__restrict__ vel_in, float4 *__restrict__ vel_out,
                                                        const ListEntry *__restrict__ list,
                                                        const unsigned char *__restrict__ cnt,
-                                                       const unsigned int *__restrict__ cellb) {
+                                                       const unsigned int *__restrict__ cellb,
+                                                       const float2 *__restrict__ wm) {
     __shared__ DevParams s_p;
     __shared__ unsigned int s_rs[9 * BLOCK];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         const BTile tl = tile_begin(b, t, s_p);
         const DevParams p = s_p;
         if ((int)threadIdx.x < tl.count)
-            vort_apply_body(p, tl.start + threadIdx.x, cell_start, pos, vort, dens, vel_in, vel_out, list, cnt, cellb,
-                            s_rs + threadIdx.x);
+            vort_apply_body<FSPH_POST_PRE != 0>(p, tl.start + threadIdx.x, cell_start, pos, vort, dens, vel_in,
+                                                vel_out, list, cnt, cellb, s_rs + threadIdx.x, wm);
     }
 }
 
@@ -317,19 +331,25 @@ unsigned int blaunch_correction(const BLaunch &L, const DevParams &lp, const uns
     return g;
 }
 void blaunch_xsph_vort(const BLaunch &L, const unsigned int *cell_start, const float4 *pos, const float4 *vel,
-                       const float *dens, float4 *vel_out, float4 *vort, const NbrLists &nl, cudaStream_t s) {
+                       const float *dens, float4 *vel_out, float4 *vort, const NbrLists &nl, cudaStream_t s,
+                       float *mrho, float2 *wm) {
     FSPH_BLOCK_SWITCH(L.block, {
+        if (FSPH_POST_PRE) {
+            auto km = kb_mrho<B_>;
+            km<<<persistent_grid(km, B_, L.full.ntiles, L.sms), B_, 0, s>>>(L.full, dens, mrho);
+        }
         auto k = kb_xsph_vort<B_>;
         k<<<persistent_grid(k, B_, L.full.ntiles, L.sms), B_, 0, s>>>(L.full, cell_start, pos, vel, dens, vel_out, vort,
-                                                                       nl.list, nl.cnt, nl.cellb);
+                                                                       nl.list, nl.cnt, nl.cellb, mrho, wm);
     })
 }
 void blaunch_vort_apply(const BLaunch &L, const unsigned int *cell_start, const float4 *pos, const float4 *vort,
-                        const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s) {
+                        const float *dens, const float4 *vel_in, float4 *vel_out, const NbrLists &nl, cudaStream_t s,
+                        const float2 *wm) {
     FSPH_BLOCK_SWITCH(L.block, {
         auto k = kb_vort_apply<B_>;
         k<<<persistent_grid(k, B_, L.full.ntiles, L.sms), B_, 0, s>>>(L.full, cell_start, pos, vort, dens, vel_in,
-                                                                       vel_out, nl.list, nl.cnt, nl.cellb);
+                                                                       vel_out, nl.list, nl.cnt, nl.cellb, wm);
     })
 }
 
@@ -353,6 +373,8 @@ struct fsph_batch {
     float4 *ppos[2] = {nullptr, nullptr};
     float4 *xb = nullptr, *vort = nullptr, *tmp4 = nullptr;
     float *dens = nullptr, *tdens = nullptr;
+    float *mrho = nullptr;  /* m / rho per particle (XSPH and vorticity passes) */
+    float2 *wm = nullptr;   /* (|omega|, m / rho) per particle */
     unsigned int *key = nullptr, *rank = nullptr, *perm = nullptr;
     NbrLists nl;
     /* grid */
@@ -418,6 +440,7 @@ void bfree(fsph_batch *b) {
         cudaFree(b->pos[k]); cudaFree(b->vel[k]); cudaFree(b->id[k]); cudaFree(b->attr[k]); cudaFree(b->ppos[k]);
     }
     cudaFree(b->xb); cudaFree(b->vort); cudaFree(b->tmp4); cudaFree(b->dens); cudaFree(b->tdens);
+    cudaFree(b->mrho); cudaFree(b->wm);
     cudaFree(b->key); cudaFree(b->rank); cudaFree(b->perm);
     cudaFree(b->nl.list); cudaFree(b->nl.cnt); cudaFree(b->nl.cellb);
     cudaFree(b->count); cudaFree(b->cell_start); cudaFree(b->block_sums);
@@ -560,8 +583,8 @@ void benqueue_pre(fsph_batch *b, const BLaunch &L, cudaStream_t s) {
 void benqueue_post(fsph_batch *b, const BLaunch &L, const DevParams &lp, cudaStream_t s) {
     launch_finalize(lp, b->pos[1], b->ppos[0], b->ppos[1], b->ctl, b->id[1], b->attr[1], b->pos[0], b->vel[0],
                     b->id[0], b->attr[0], nullptr, nullptr, s);
-    blaunch_xsph_vort(L, b->cell_start, b->pos[0], b->vel[0], b->dens, b->vel[1], b->vort, b->nl, s);
-    blaunch_vort_apply(L, b->cell_start, b->pos[0], b->vort, b->dens, b->vel[1], b->vel[0], b->nl, s);
+    blaunch_xsph_vort(L, b->cell_start, b->pos[0], b->vel[0], b->dens, b->vel[1], b->vort, b->nl, s, b->mrho, b->wm);
+    blaunch_vort_apply(L, b->cell_start, b->pos[0], b->vort, b->dens, b->vel[1], b->vel[0], b->nl, s, b->wm);
     kb_scene_errors<<<b->nscenes, 256, 0, s>>>(b->d_offs, b->d_scenes, b->dens, b->d_err);
 }
 
@@ -760,6 +783,7 @@ int fsph_batch_create(const fsph_params *params, const int *counts, int nscenes,
         A(&b->pos[k], n); A(&b->vel[k], n); A(&b->id[k], n); A(&b->attr[k], n); A(&b->ppos[k], n);
     }
     A(&b->xb, n); A(&b->vort, n); A(&b->tmp4, n); A(&b->dens, n); A(&b->tdens, n);
+    A(&b->mrho, n); A(&b->wm, n);
     A(&b->key, n); A(&b->rank, n); A(&b->perm, n);
     A(&b->nl.list, n * kListMax); A(&b->nl.cnt, n); A(&b->nl.cellb, n);
     A(&b->d_scenes, (size_t)nscenes); A(&b->d_offs, (size_t)nscenes + 1); A(&b->d_err, 3 * (size_t)nscenes);

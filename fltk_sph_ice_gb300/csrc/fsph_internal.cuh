@@ -233,6 +233,12 @@ __device__ inline float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y 
 #ifndef FSPH_POST_PRE
 #define FSPH_POST_PRE 1
 #endif
+/* FSPH_SPH_DENSITY_LANES 1: the WCSPH density + list pass runs as many lanes
+ * per particle as the force pass (k_sph_density_lanes), so small scenes fill
+ * the GPU; 0: one thread per particle. */
+#ifndef FSPH_SPH_DENSITY_LANES
+#define FSPH_SPH_DENSITY_LANES 1
+#endif
 /* 1 / sqrt(max(r2, 1e-20)) for the pair loops.  FSPH_RSQRT_FTZ 1 (default)
  * issues rsqrt.approx.ftz.f32: the argument is clamped to a normal number
  * and the result is normal, so the flush-to-zero form, which skips the

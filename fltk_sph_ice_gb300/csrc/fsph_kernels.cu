@@ -652,6 +652,74 @@ __global__ void __launch_bounds__(kBlock) k_sph_density(DevParams p, const unsig
     reinterpret_cast<float *>(vel + i)[3] = 1.0f / rho;
 }
 
+/* k_sph_density with LPP lanes per particle, so that small scenes still
+ * fill the GPU: the lanes of a group take the candidates of each row in
+ * turn (lane s the s-th of every LPP consecutive ones), and each LPP-wide
+ * chunk's hits are ranked by a ballot inside the group, so the list holds
+ * the same slots in the same order as one thread's walk.  The density is
+ * the group's sum of the lanes' partial sums (same terms, other order). */
+template <int LPP>
+__global__ void __launch_bounds__(kBlock) k_sph_density_lanes(DevParams p, const unsigned int *__restrict__ cell_start,
+                                                              float4 *pos, float4 *vel, float *__restrict__ dens,
+                                                              float *__restrict__ pres, ListEntry *__restrict__ list,
+                                                              unsigned char *__restrict__ cnt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int sub = t % LPP, lane = threadIdx.x & 31;
+    const bool valid = t / LPP < p.n;
+    const int i = valid ? t / LPP : p.n - 1; /* padding groups walk a real slot and write nothing */
+    const unsigned int gmask = ((1u << LPP) - 1u) << (lane & ~(LPP - 1));
+    const float3 xi = f3(pos[i]);
+    const int3 c = cell_of(xi, p);
+    float acc = 0.0f;
+    int k = 0;
+    unsigned int last = (unsigned int)i;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy) {
+            unsigned int s, e;
+            row_range(cell_start, c, dy, dz, p, s, e);
+            for (unsigned int j0 = s; j0 < e; j0 += LPP) { /* the same trip count for the whole group */
+                const unsigned int j = j0 + (unsigned int)sub;
+                bool hit = false;
+                if (j < e) {
+                    const float3 d = xi - f3(__ldg(pos + j));
+                    const float r2 = dot3(d, d);
+                    if (r2 < p.h2) {
+                        const float q = p.h2 - r2;
+                        acc += q * q * q;
+                    }
+                    hit = r2 < p.rl2;
+                }
+                if (list) {
+                    const unsigned int m = __ballot_sync(gmask, hit) & gmask;
+                    if (m) {
+                        if (hit) {
+                            const int at = k + __popc(m & ((1u << lane) - 1u));
+                            if (at < kListMax) list[list_at(at, i, p.n)] = (ListEntry)j;
+                        }
+                        last = __shfl_sync(gmask, j, 31 - __clz(m));
+                        k += __popc(m);
+                    }
+                }
+            }
+        }
+    acc = group_sum<LPP>(acc);
+    if (!valid || sub != 0) return;
+    if (list) {
+        const bool ovf = k > kListMax;
+#ifdef FSPH_LIST_GROUPED
+        if (!ovf) /* pad the last group (k >= 1: the slot itself is always listed) */
+            for (int u = k; (u & 3) != 0; ++u) list[list_at(u, i, p.n)] = (ListEntry)last;
+#endif
+        cnt[i] = ovf ? kListOverflow : (unsigned char)k;
+    }
+    const float rho = p.mass * p.aw * acc;
+    const float prs = p.gas_k * (rho - p.rest_dens);
+    dens[i] = rho;
+    pres[i] = prs;
+    reinterpret_cast<float *>(pos + i)[3] = prs / (rho * rho);
+    reinterpret_cast<float *>(vel + i)[3] = 1.0f / rho;
+}
+
 /* a_i = -sum_j m (p_i/rho_i^2 + p_j/rho_j^2) grad W_ij + mu sum_j m (v_j - v_i)
  * lapW_ij / rho_j + g over 0 < r_ij < h (rxSPH::calForce, rx_sph_cpu.cpp:558-656),
  * from the list of the density pass (or the 27 cells when lists are off),
@@ -1059,10 +1127,18 @@ void launch_vort_apply(const DevParams &p, const unsigned int *cell_start, const
     k<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vort, dens, vel_in, vel_out,
                                          p.use_lists ? nl.list : nullptr, nl.cnt, nl.cellb, wm);
 }
+int sph_force_lanes(int n);
 void launch_sph_density(const DevParams &p, const unsigned int *cell_start, float4 *pos, float4 *vel, float *dens,
                         float *pres, const NbrLists &nl, cudaStream_t s) {
-    k_sph_density<<<blocks_for(p.n), kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres,
-                                                     p.use_lists ? nl.list : nullptr, nl.cnt);
+    ListEntry *l = p.use_lists ? nl.list : nullptr;
+    const int lanes = FSPH_SPH_DENSITY_LANES ? sph_force_lanes(p.n) : 1;
+    const unsigned int g = blocks_for((long long)p.n * lanes);
+    switch (lanes) {
+    case 1: k_sph_density<<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres, l, nl.cnt); break;
+    case 2: k_sph_density_lanes<2><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres, l, nl.cnt); break;
+    case 4: k_sph_density_lanes<4><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres, l, nl.cnt); break;
+    default: k_sph_density_lanes<8><<<g, kBlock, 0, s>>>(p, cell_start, pos, vel, dens, pres, l, nl.cnt); break;
+    }
 }
 /* lanes per particle of the WCSPH force pass: enough that the launch holds
  * about as many threads as the GPU keeps resident (1536 per SM), at most 8 */

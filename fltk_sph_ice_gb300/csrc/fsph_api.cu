@@ -1321,6 +1321,17 @@ int fsph_set_particles(fsph_ctx *c, const float *pos4, const float *vel4, int n,
     return FSPH_OK;
 }
 
+/* dst[slot] = src[p - start] for the slots whose particle p = id[slot] lies
+ * in [start, start + count): a range given in particle order lands in the
+ * slots of the last step's order, and no other array moves */
+__global__ void k_scatter_range4(int n, const unsigned int *__restrict__ id, int start, int count,
+                                 const float4 *__restrict__ src, float4 *__restrict__ dst) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    const unsigned int q = id[d] - (unsigned int)start;
+    if (q < (unsigned int)count) dst[d] = src[q];
+}
+
 int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count, int where) {
     if (!c || !data) return FSPH_INVALID_ARG;
     FSPH_USABLE(c);
@@ -1330,9 +1341,10 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
     if (count == 0) return FSPH_OK; /* nothing to overwrite (and no kernel for an empty range) */
     cudaStream_t s = c->stream;
     int n = c->n;
-    /* bring the home arrays to particle order (once after a step), then
-     * overwrite the range */
-    FSPH_TRY(home_to_particle_order(c));
+    /* attributes: bring the home arrays to particle order (once after a
+     * step), then overwrite the range; positions and velocities are
+     * scattered to their particles' slots without moving anything else */
+    if (type == FSPH_ATTRIBUTE) FSPH_TRY(home_to_particle_order(c));
     cudaMemcpyKind k = where == FSPH_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (type == FSPH_POSITION || type == FSPH_VELOCITY) {
         /* staged and checked before it replaces anything: a range with a
@@ -1345,11 +1357,16 @@ int fsph_set_array(fsph_ctx *c, int type, const void *data, int start, int count
         FSPH_TRY(check_launch(c));
         FSPH_CUDA(c, cudaStreamSynchronize(s));
         if (*c->flag_host) return fail(c, FSPH_NAN_DETECTED, "non-finite position or velocity");
-        float4 *dst = (type == FSPH_POSITION ? c->set[0].pos : c->set[0].vel) + start;
-        FSPH_CUDA(c, cudaMemcpyAsync(dst, c->tmp4, (size_t)count * 16, cudaMemcpyDeviceToDevice, s));
-    } else {
-        FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr + start, data, (size_t)count * 4, k, s));
+        float4 *dst = type == FSPH_POSITION ? c->set[0].pos : c->set[0].vel;
+        if (c->home_identity)
+            FSPH_CUDA(c, cudaMemcpyAsync(dst + start, c->tmp4, (size_t)count * 16, cudaMemcpyDeviceToDevice, s));
+        else
+            k_scatter_range4<<<(n + 255) / 256, 256, 0, s>>>(n, c->set[0].id, start, count, c->tmp4, dst);
+        /* the caller's buffer was read before the check above returned; the
+         * rest is ordered on the context's stream */
+        return check_launch(c);
     }
+    FSPH_CUDA(c, cudaMemcpyAsync(c->set[0].attr + start, data, (size_t)count * 4, k, s));
     FSPH_TRY(check_launch(c));
     FSPH_CUDA(c, cudaStreamSynchronize(s));
     /* an attribute of -1 deletes a particle, another value revives one */
@@ -1549,6 +1566,12 @@ int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
 
 const void *fsph_device_ptr(fsph_ctx *c, int type) {
     if (!c) return nullptr;
+    /* work the context queued without a caller stream (fsph_set_array's
+     * scatter) is complete before the caller reads through the pointer */
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        c->err = "stream synchronisation failed";
+        return nullptr;
+    }
     switch (type) {
     case FSPH_POSITION: return c->set[0].pos;
     case FSPH_VELOCITY: return c->set[0].vel;

@@ -197,7 +197,9 @@ int fsph_set_particles(fsph_ctx *ctx, const float *pos4, const float *vel4, int 
 /* Overwrite `count` particles from index `start` of one array
  * (SetArrayVBO, rx_ps.h:260-262).  FSPH_POSITION, FSPH_VELOCITY, FSPH_ATTRIBUTE.
  * Positions and velocities must be finite: a range holding a NaN or an
- * infinity returns FSPH_NAN_DETECTED and leaves the state unchanged. */
+ * infinity returns FSPH_NAN_DETECTED and leaves the state unchanged.  They
+ * land in their particles' device slots and nothing else moves, so writing
+ * back what fsph_get_array returned leaves the next steps bit-identical. */
 int fsph_set_array(fsph_ctx *ctx, int type, const void *data, int start, int count, int where);
 
 /* ---- step (Update) ---- */

@@ -218,7 +218,9 @@ int fsph_last_stats(fsph_ctx *ctx, fsph_step_stats *stats);
 int fsph_get_array(fsph_ctx *ctx, int type, void *dst, int where, void *stream);
 /* Borrowed device pointer to an internal array, in DEVICE order (see
  * FSPH_SORTED_ID for the device slot -> particle index map); valid until the
- * next fsph_step / fsph_set_particles.  NULL on error. */
+ * next fsph_step / fsph_set_particles.  Synchronises the context's own
+ * stream first, so work queued without a caller stream (fsph_set_array) is
+ * visible through it.  NULL on error. */
 const void *fsph_device_ptr(fsph_ctx *ctx, int type);
 /* Synchronise the context's stream. */
 int fsph_sync(fsph_ctx *ctx);

@@ -212,7 +212,7 @@ int validate(const fsph_params &p, std::string &why) {
     if (p.cell_skin < 0.0f || p.cell_skin > 1.0f) { why = "cell_skin must lie in [0, 1]"; return FSPH_INVALID_ARG; }
     if (p.warm_start < 0 || p.warm_start > 1) { why = "warm_start must be 0 or 1"; return FSPH_INVALID_ARG; }
     if (p.grid_sort < 0 || p.grid_sort > 1) { why = "grid_sort must be 0 or 1"; return FSPH_INVALID_ARG; }
-    if (p.mlp_tcgen05 < 0 || p.mlp_tcgen05 > 1) { why = "mlp_tcgen05 must be 0 or 1"; return FSPH_INVALID_ARG; }
+    if (p.mlp_tcgen05 < 0 || p.mlp_tcgen05 > 2) { why = "mlp_tcgen05 must be 0, 1 or 2"; return FSPH_INVALID_ARG; }
     return FSPH_OK;
 }
 
@@ -715,7 +715,7 @@ int enqueue_pbf_pre(fsph_ctx *c, const DevParams &p, cudaStream_t s) {
     if (c->P.warm_start == 1) {
         if (c->P.mlp_tcgen05)
             launch_mlp_infer_tc(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, &c->ctl->mlp_err, s,
-                                !c->model_nbr);
+                                !c->model_nbr, c->P.mlp_tcgen05 == 1);
         else
             launch_mlp_infer(c->mlp_dev, c->feat, p.n, c->dwarm, p.h, c->warm_valid, s, !c->model_nbr);
         dw = c->dwarm;
@@ -1958,6 +1958,7 @@ int fsph_set_warm_start_model(fsph_ctx *c, const float *blob) {
     if (!c || !blob) return FSPH_INVALID_ARG;
     for (int k = 0; k < FSPH_MLP_BLOB_SIZE; ++k)
         if (!std::isfinite(blob[k])) return fail(c, FSPH_INVALID_ARG, "non-finite network parameter");
+    mlp_tc_prepare(); /* before any step graph is captured */
     float *d = nullptr;
     FSPH_CUDA(c, cudaMalloc((void **)&d, FSPH_MLP_BLOB_SIZE * sizeof(float)));
     cudaError_t e = cudaMemcpyAsync(d, blob, FSPH_MLP_BLOB_SIZE * sizeof(float), cudaMemcpyHostToDevice, c->stream);

@@ -60,9 +60,14 @@ void launch_mlp_infer(const MlpDev *m, const float *x, int n, float4 *y, float s
 /* same network, plain n x 3 output (for training checks) */
 void launch_mlp_forward3(const MlpDev *m, const float *x, int n, float *y, cudaStream_t s);
 /* the same two on the tcgen05 tensor cores with TMEM accumulators
- * (fsph_mlp_tc.cu); *err |= 1 when a wait on an MMA ran out */
+ * (fsph_mlp_tc.cu); *err |= 1 when a wait on an MMA or a TMA load ran out.
+ * tma: a network of the 16 local inputs reads them by TMA boxes
+ * (k_mlp_infer_tma), else by per-thread loads (the same results) */
 void launch_mlp_infer_tc(const MlpDev *m, const float *x, int n, float4 *y, float scale, const unsigned int *valid,
-                         unsigned int *err, cudaStream_t s, bool local_only = false);
+                         unsigned int *err, cudaStream_t s, bool local_only = false, bool tma = true);
+/* looks up the driver entry point the TMA inference needs (outside any
+ * stream capture) */
+void mlp_tc_prepare();
 void launch_mlp_forward3_tc(const MlpDev *m, const float *x, int n, float *y, unsigned int *err, cudaStream_t s);
 /* per-block partial gradients of L = mean_i sum_k (y_ik - t_ik / out_scale)^2
  * (blob layout, nblocks rows) and per-block loss sums */

@@ -25,7 +25,10 @@
  * a wait that runs out sets *err, the CTA stops, waits (bounded) once more for
  * its MMAs and frees its TMEM.
  */
+#include <cuda.h>
+
 #include <cstdint>
+#include <cstring>
 
 #include "fsph_mlp.cuh"
 
@@ -326,6 +329,231 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tc(const MlpDev *__res
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+/* ---- the 16 local inputs of a tile by TMA (cp.async.bulk.tensor) ---- */
+
+constexpr int kTmaCols = 16;                                   /* features 0-15: one 64-byte row segment */
+constexpr uint32_t kTmaBytes = kTcRows * kTmaCols * 4;         /* one 128 x 16 FP32 box = 8 KB */
+
+__device__ __forceinline__ void mbar_init(uint32_t mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+}
+/* one thread: expect kTmaBytes on xbar and load the 128 x 16 box at rows
+ * [row0, row0 + 128), features [0, 16); rows past n read as zeros */
+__device__ __forceinline__ void tma_load_tile(const CUtensorMap *tmap, uint32_t dst, uint32_t xbar, int row0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(xbar), "r"(kTmaBytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(0), "r"(row0), "r"(xbar)
+        : "memory");
+}
+
+/* k_mlp_infer_tc<1> with the tile's inputs brought into shared memory by the
+ * tensor-memory accelerator: the next tile's box is requested as soon as the
+ * current one has been converted, and lands while this tile's three MMAs and
+ * epilogues run.  Each row reads exactly its 64 used bytes (the feature rows
+ * are 128 bytes apart).  Same arithmetic as k_mlp_infer_tc<1>, so the same
+ * results bit for bit. */
+__global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tma(const MlpDev *__restrict__ gm,
+                                                              const __grid_constant__ CUtensorMap tmap, int n,
+                                                              float4 *__restrict__ y, float scale,
+                                                              const unsigned int *__restrict__ valid,
+                                                              unsigned int *__restrict__ err) {
+    __shared__ TcSmem S;
+    __shared__ __align__(128) float xs[kTcRows * kTmaCols];
+    __shared__ __align__(8) unsigned long long xbar_word;
+    const int t = threadIdx.x, warp = t >> 5;
+    const int ntiles = (n + kTcRows - 1) / kTcRows;
+    const bool ok = valid == nullptr || *valid != 0u;
+    if (!ok) {
+        for (int r = blockIdx.x * kTcThreads + t; r < n; r += gridDim.x * kTcThreads)
+            y[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    for (int e = t; e < kHid * (kIn / 8); e += kTcThreads) {
+        const int nr = e / (kIn / 8), kc = e % (kIn / 8);
+        *reinterpret_cast<uint4 *>(S.b1 + kmaj(nr, kc, kIn)) =
+            *reinterpret_cast<const uint4 *>(gm->w1t + nr * kS1 + 8 * kc);
+    }
+    for (int e = t; e < kHid * (kHid / 8); e += kTcThreads) {
+        const int nr = e / (kHid / 8), kc = e % (kHid / 8);
+        *reinterpret_cast<uint4 *>(S.b2 + kmaj(nr, kc, kHid)) =
+            *reinterpret_cast<const uint4 *>(gm->w2t + nr * kS2 + 8 * kc);
+    }
+    for (int e = t; e < kN3 * (kHid / 8); e += kTcThreads) {
+        const int nr = e / (kHid / 8), kc = e % (kHid / 8);
+        *reinterpret_cast<uint4 *>(S.b3 + kmaj(nr, kc, kHid)) =
+            nr < 8 ? *reinterpret_cast<const uint4 *>(gm->w3t + nr * kS2 + 8 * kc) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    for (int e = t; e < kHid; e += kTcThreads) {
+        S.bias1[e] = gm->b1[e];
+        S.bias2[e] = gm->b2[e];
+    }
+    if (t < 8) S.bias3[t] = gm->b3[t];
+    if (t < kIn) {
+        S.mu[t] = gm->mu[t];
+        S.isig[t] = gm->isig[t];
+    }
+    const uint32_t mbar = smem_u32(&S.mbar), xbar = smem_u32(&xbar_word), xdst = smem_u32(xs);
+    if (t == 0) {
+        S.fail = 0u;
+        mbar_init(mbar);
+        mbar_init(xbar);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_proxy_async();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = S.tmem;
+    const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
+    const float k = gm->out_scale * scale;
+    const uint32_t a1 = smem_u32(S.a1), a2 = smem_u32(S.a2);
+    const uint32_t b1 = smem_u32(S.b1), b2 = smem_u32(S.b2), b3 = smem_u32(S.b3);
+    uint32_t phase = 0, xphase = 0;
+    bool failed = false, loading = false; /* loading: a box is in flight towards xs */
+    if ((int)blockIdx.x < ntiles) {
+        if (t == 0) tma_load_tile(&tmap, xdst, xbar, blockIdx.x * kTcRows);
+        loading = true;
+    }
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const int row = tile * kTcRows + t;
+        /* this tile's inputs have landed */
+        failed = __syncthreads_or(!mbar_wait(xbar, xphase)) != 0;
+        if (failed) break;
+        xphase ^= 1u;
+        loading = false;
+#pragma unroll
+        for (int kc = 0; kc < kIn / 8; ++kc) {
+            float v[8];
+            if (row < n && kc < kTmaCols / 8) {
+                const float4 p0 = *reinterpret_cast<const float4 *>(xs + t * kTmaCols + 8 * kc);
+                const float4 p1 = *reinterpret_cast<const float4 *>(xs + t * kTmaCols + 8 * kc + 4);
+                const float raw[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+#pragma unroll
+                for (int e = 0; e < 8; ++e) v[e] = (raw[e] - S.mu[8 * kc + e]) * S.isig[8 * kc + e];
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) v[e] = 0.0f;
+            }
+            uint4 w;
+            w.x = bf2(v[0], v[1]);
+            w.y = bf2(v[2], v[3]);
+            w.z = bf2(v[4], v[5]);
+            w.w = bf2(v[6], v[7]);
+            *reinterpret_cast<uint4 *>(S.a1 + kmaj(t, kc, kIn)) = w;
+        }
+        fence_proxy_async(); /* A1 for the MMA, and xs free for the next box */
+        fence_before();
+        __syncthreads();
+        fence_after();
+        const int next = tile + (int)gridDim.x;
+        if (t == 0) {
+            mma_bf16(tmem, sdesc(a1, 128, 128 * (kIn / 8)), sdesc(b1, 128, 128 * (kIn / 8)), idesc_bf16(kTcRows, kHid),
+                     0u);
+            mma_commit(mbar);
+            if (next < ntiles) tma_load_tile(&tmap, xdst, xbar, next * kTcRows);
+        }
+        loading = next < ntiles;
+        failed = __syncthreads_or(!mbar_wait(mbar, phase)) != 0;
+        phase ^= 1u;
+        if (failed) break;
+        fence_after();
+        hidden_epilogue(tlane, 0, S.bias1, S.a2, t);
+        fence_proxy_async();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (t == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kHid / 16; ++ks)
+                mma_bf16(tmem + 64, sdesc(a2 + 256 * ks, 128, 128 * (kHid / 8)),
+                         sdesc(b2 + 256 * ks, 128, 128 * (kHid / 8)), idesc_bf16(kTcRows, kHid), ks > 0);
+            mma_commit(mbar);
+        }
+        failed = __syncthreads_or(!mbar_wait(mbar, phase)) != 0;
+        phase ^= 1u;
+        if (failed) break;
+        fence_after();
+        hidden_epilogue(tlane, 64, S.bias2, S.a2, t);
+        fence_proxy_async();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (t == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kHid / 16; ++ks)
+                mma_bf16(tmem, sdesc(a2 + 256 * ks, 128, 128 * (kHid / 8)), sdesc(b3 + 256 * ks, 128, 128 * (kHid / 8)),
+                         idesc_bf16(kTcRows, kN3), ks > 0);
+            mma_commit(mbar);
+        }
+        failed = __syncthreads_or(!mbar_wait(mbar, phase)) != 0;
+        phase ^= 1u;
+        if (failed) break;
+        fence_after();
+        float o[16];
+        tmem_ld16(tlane, o);
+        if (row < n) {
+            const float r0 = (o[0] + S.bias3[0]) * k, r1 = (o[1] + S.bias3[1]) * k, r2 = (o[2] + S.bias3[2]) * k;
+            y[row] = make_float4(r0, r1, r2, 0.0f);
+        }
+        fence_before();
+        __syncthreads(); /* TMEM and A1 / A2 free for the next tile */
+        fence_after();
+    }
+    if (failed) {
+        if (t == 0) {
+            atomicOr(err, 1u);
+            mbar_wait(mbar, phase ^ 1u); /* an MMA phase that did not complete in time, once more */
+            if (loading) mbar_wait(xbar, xphase); /* a box still in flight towards xs, once more */
+        }
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+/* the 2-D map of the feature rows for k_mlp_infer_tma: n rows of kIn floats,
+ * 128 bytes apart, read as 128 x 16 boxes; false when the driver entry point
+ * is unavailable (the per-thread loads are used then) */
+typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encode_tiled() { /* the driver's cuTensorMapEncodeTiled, looked up once */
+    static EncodeTiled encode = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<EncodeTiled>(fn);
+    }
+    return encode;
+}
+bool feature_tensor_map(CUtensorMap *m, const float *x, int n) {
+    const EncodeTiled encode = encode_tiled();
+    if (!encode || n <= 0 || (reinterpret_cast<uintptr_t>(x) & 15u) != 0) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)kIn, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)kIn * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)kTmaCols, (cuuint32_t)kTcRows};
+    const cuuint32_t estr[2] = {1u, 1u};
+    std::memset(m, 0, sizeof(*m));
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(x), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 unsigned int tc_blocks(int n) {
     const unsigned int tiles = (unsigned int)((n + kTcRows - 1) / kTcRows);
     return tiles < 4u * 152u ? (tiles > 0 ? tiles : 1u) : 4u * 152u; /* four CTAs (512 TMEM columns) per SM */
@@ -333,9 +561,16 @@ unsigned int tc_blocks(int n) {
 
 }  // namespace
 
+void mlp_tc_prepare() { encode_tiled(); }
+
 void launch_mlp_infer_tc(const MlpDev *m, const float *x, int n, float4 *y, float scale, const unsigned int *valid,
-                         unsigned int *err, cudaStream_t s, bool local_only) {
+                         unsigned int *err, cudaStream_t s, bool local_only, bool tma) {
     if (n <= 0) return;
+    CUtensorMap map;
+    if (local_only && tma && feature_tensor_map(&map, x, n)) {
+        k_mlp_infer_tma<<<tc_blocks(n), kTcThreads, 0, s>>>(m, map, n, y, scale, valid, err);
+        return;
+    }
     auto k = local_only ? k_mlp_infer_tc<1> : k_mlp_infer_tc<kIn / 16>;
     k<<<tc_blocks(n), kTcThreads, 0, s>>>(m, x, n, y, nullptr, scale, valid, err);
 }

@@ -132,7 +132,9 @@ typedef struct fsph_params {
                                 1: LSD radix sort of the 64-bit keys, 8 cell bits per pass */
     int mlp_tcgen05;         /* warm-start inference: 0 mma.sync fragments (m16n8k16);
                                 1 tcgen05.mma with TMEM accumulators (fsph_mlp_forward_tcgen05),
-                                the default of fsph_params_default */
+                                a local-input network's rows brought in by TMA boxes, the default
+                                of fsph_params_default; 2 the same MMAs, inputs by per-thread
+                                loads (identical results) */
     int reserved[1];
 } fsph_params;
 

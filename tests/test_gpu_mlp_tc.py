@@ -59,3 +59,36 @@ def test_tcgen05_warm_start_step(gpu):
     assert np.abs(out[0][0] - out[1][0]).max() <= 1, (out[0][0], out[1][0])
     assert abs(out[0][0].mean() - out[1][0].mean()) <= 0.5
     assert np.abs(out[0][1] - out[1][1]).max() < 1e-3 * sc.params.h
+
+
+@pytest.mark.parametrize("n", [4096, 1 << 20])
+def test_tma_inputs_step_identically(gpu, n):
+    """The committed network weights only the 16 local inputs; with
+    mlp_tcgen05 = 1 their rows reach shared memory as TMA boxes
+    (cp.async.bulk.tensor, rows past n filled with zeros), with 2 by
+    per-thread loads.  Same arithmetic after that, so the warm-started
+    steps are bit-identical, including a last, partial 128-row tile."""
+    from fltk_sph_ice_gb300 import abi, rxPBDSPH, scenes, warmstart
+    blob, _ = warmstart.load_model()
+    side = 8 if n == 4096 else 64
+    sc = scenes.pbf_double_dam_break(block=(side, side, 2 * side))
+    keep = sc.n - 37  # a partial last tile
+    out = []
+    for mode in (1, 2):
+        p = abi.FsphParams.from_buffer_copy(sc.params)
+        p.warm_start, p.mlp_tcgen05 = 1, mode
+        p.max_iter = 60
+        ps = rxPBDSPH(p)
+        ps.SetWarmStartModel(blob)
+        ps.Set(sc.pos[:keep], sc.vel[:keep])
+        its = []
+        for _ in range(4):
+            ps.Update(sc.dt)
+            its.append(ps.LastStats().iterations)
+            assert ps.LastStats().status in (abi.OK, abi.NOT_CONVERGED)
+        out.append((its, ps.GetArrayVBO(abi.RX_POSITION), ps.GetArrayVBO(abi.RX_STEP_CORRECTION)))
+        ps.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
+    assert np.abs(out[0][2][:, :3]).max() > 0  # the network ran

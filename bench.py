@@ -929,7 +929,7 @@ def large_arm(args):
     def leg(warm: bool):
         p = abi.FsphParams.from_buffer_copy(sc.params)
         p.eta, p.error_mode, p.clamp_constraint = 1e-3, abi.ERR_ONE_SIDED, 1
-        p.min_iter, p.max_iter, p.use_graph = 2, 400, 1
+        p.min_iter, p.max_iter, p.use_graph = 2, args.max_iter, 1
         p.compensated_density = 1
         p.warm_start = 1 if warm else 0
         ps = rxPBDSPH(p)
@@ -973,7 +973,8 @@ def large_arm(args):
     bytes_ps = 396.0 + 60.0 * warm["mean_iterations"]
     if rank == 0:
         cfg = {"workload": "pbf_obstacle_drop_16M", "particles": sc.n, "boundary_particles": int(sc.boundary.shape[0]),
-               "block": [256, 256, 256], "dt": sc.dt, "eta_one_sided": 1e-3, "compensated_density": True,
+               "block": [256, 256, 256], "dt": sc.dt, "eta_one_sided": 1e-3, "max_iter": args.max_iter,
+               "compensated_density": True,
                "constraint": "unilateral (clamped C >= 0)", "method": method_of(meta),
                "mean_iterations": warm["mean_iterations"], "max_error": warm["max_error"],
                "not_converged_steps": warm["not_converged_steps"], "status": warm["status"],
@@ -1015,6 +1016,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="batched_256: skip the autotuner, default launch shape")
+    ap.add_argument("--max-iter", type=int, default=2000,
+                    help="pbf_obstacle_drop_16M: the constraint loop's iteration cap (a guard, default 2000: with "
+                         "400 the steps after the impact stop above the tolerance and every later step inherits "
+                         "their error)")
     ap.add_argument("--workload", default=WORKLOAD,
                     choices=[WORKLOAD, "batched_256", "pbf_obstacle_drop_16M", "pbf_dam_break_262k",
                              "wcsph_dam_break_32k"],

@@ -22,6 +22,7 @@
  *   k_sph_*            rxSPH::calDensity / calForce / integrate (rx_sph_cpu.cpp:495-1077)
  */
 #include <algorithm>
+#include <mutex>
 
 #include "fsph_kernels.cuh"
 #include "fsph_passes.cuh"
@@ -1061,9 +1062,12 @@ void launch_pbf_visc(const DevParams &p, const unsigned int *cell_start, const f
 static unsigned int pass_blocks(int n, const void *kernel, bool persistent) {
     unsigned int b = blocks_for(n, kPassBlock);
     if (persistent) {
-        /* resident blocks of each pass kernel, looked up once */
+        /* resident blocks of each pass kernel, looked up once (contexts may
+         * step from several host threads) */
+        static std::mutex mu;
         static const void *known[4] = {nullptr, nullptr, nullptr, nullptr};
         static int resident[4] = {0, 0, 0, 0};
+        std::lock_guard<std::mutex> lock(mu);
         int k = 0;
         while (k < 4 && known[k] && known[k] != kernel) ++k;
         if (k == 4) k = 3;
@@ -1143,13 +1147,12 @@ void launch_sph_density(const DevParams &p, const unsigned int *cell_start, floa
 /* lanes per particle of the WCSPH force pass: enough that the launch holds
  * about as many threads as the GPU keeps resident (1536 per SM), at most 8 */
 int sph_force_lanes(int n) {
-    static int resident = 0;
-    if (resident == 0) {
+    static const int resident = [] { /* initialised once, thread-safely */
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        resident = std::max(sms, 1) * 1536;
-    }
+        return std::max(sms, 1) * 1536;
+    }();
 #ifdef FSPH_SPH_LANES
     return FSPH_SPH_LANES;
 #else

@@ -452,11 +452,11 @@ void launch_mlp_forward3(const MlpDev *m, const float *x, int n, float *y, cudaS
 }
 void launch_mlp_grad(const MlpDev *m, const float *x, const float *t, int n, float *part, float *loss_part,
                      cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
+    static const bool attr = [] { /* set once, thread-safely */
         cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGradSmem);
-        attr = true;
-    }
+        return true;
+    }();
+    (void)attr;
     k_mlp_grad<<<mlp_grad_blocks(n), 128, kGradSmem, s>>>(m, x, t, n, part, loss_part);
 }
 void launch_mlp_reduce(const float *part, const float *loss_part, int nblocks, int n, float *grad, float *loss,

@@ -527,18 +527,16 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_infer_tma(const MlpDev *__re
 typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiled encode_tiled() { /* the driver's cuTensorMapEncodeTiled, looked up once */
-    static EncodeTiled encode = nullptr;
-    static bool looked = false;
-    if (!looked) {
-        looked = true;
+EncodeTiled encode_tiled() { /* the driver's cuTensorMapEncodeTiled, looked up once, thread-safely */
+    static const EncodeTiled encode = []() -> EncodeTiled {
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            encode = reinterpret_cast<EncodeTiled>(fn);
-    }
+            return reinterpret_cast<EncodeTiled>(fn);
+        return nullptr;
+    }();
     return encode;
 }
 bool feature_tensor_map(CUtensorMap *m, const float *x, int n) {

@@ -1494,7 +1494,11 @@ int fsph_get_array(fsph_ctx *c, int type, void *dst, int where, void *stream) {
     if (n == 0) return FSPH_OK;
     cudaStream_t s = c->stream;
     (void)stream;
-    FSPH_CUDA(c, cudaStreamSynchronize(s));
+    /* the copies below are ordered after the last step on the context's
+     * stream; only the types that read the host copy of the control block
+     * (which ping-pong buffer holds x*) wait for it first */
+    if (type == FSPH_PREDICT_POS || type == FSPH_CORRECTION || type == FSPH_SCALING_FACTOR)
+        FSPH_CUDA(c, cudaStreamSynchronize(s));
     const unsigned int *id = c->set[0].id;
     /* the last step's results after a SetArrayVBO keep that step's order */
     const bool result = type == FSPH_FORCE || type == FSPH_VORTICITY || type == FSPH_PREDICT_POS ||

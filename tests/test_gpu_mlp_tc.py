@@ -61,7 +61,7 @@ def test_tcgen05_warm_start_step(gpu):
     assert np.abs(out[0][1] - out[1][1]).max() < 1e-3 * sc.params.h
 
 
-@pytest.mark.parametrize("n", [4096, 1 << 20])
+@pytest.mark.parametrize("n", [5, 100, 4096, 1 << 20])
 def test_tma_inputs_step_identically(gpu, n):
     """The committed network weights only the 16 local inputs; with
     mlp_tcgen05 = 1 their rows reach shared memory as TMA boxes
@@ -70,9 +70,9 @@ def test_tma_inputs_step_identically(gpu, n):
     steps are bit-identical, including a last, partial 128-row tile."""
     from fltk_sph_ice_gb300 import abi, rxPBDSPH, scenes, warmstart
     blob, _ = warmstart.load_model()
-    side = 8 if n == 4096 else 64
+    side = 64 if n == 1 << 20 else 8
     sc = scenes.pbf_double_dam_break(block=(side, side, 2 * side))
-    keep = sc.n - 37  # a partial last tile
+    keep = sc.n - 37 if n >= 4096 else n  # a partial last tile; fewer rows than one tile
     out = []
     for mode in (1, 2):
         p = abi.FsphParams.from_buffer_copy(sc.params)
@@ -91,4 +91,5 @@ def test_tma_inputs_step_identically(gpu, n):
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
     assert np.array_equal(out[0][2], out[1][2])
-    assert np.abs(out[0][2][:, :3]).max() > 0  # the network ran
+    if keep > 100:
+        assert np.abs(out[0][2][:, :3]).max() > 0  # the network ran

@@ -68,3 +68,25 @@ def test_reference_arm_non_zero_rank_exits_without_work(monkeypatch, capsys):
     args = argparse.Namespace(steps=1, warmup=0)
     assert bench.reference_arm(args) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_prints_the_contract_line(monkeypatch, capsys):
+    """Rank 0 of the reference arm: the reference's CPU step on the sample
+    scene (shortened here: a 2-step pre-roll, one process, 2 iterations) and
+    one JSON line with the GPU arm's metric, unit and direction."""
+    sys.path.insert(0, ROOT)
+    import argparse
+    import json
+    import bench
+    monkeypatch.delenv("RANK", raising=False)
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    monkeypatch.setattr(bench, "host_cores", lambda: 1)
+    monkeypatch.setattr(bench, "REF_ITERS", 2)
+    args = argparse.Namespace(steps=1, warmup=0, preroll=2)
+    assert bench.reference_arm(args) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True and line["value"] > 0
+    assert line["config"]["iterations"] == 2 and line["config"]["processes"] == 1
+    assert line["cpu_baseline"]["cores"] == 1 and line["cpu_baseline"]["kind"] in ("reference", "port")
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
